@@ -1,0 +1,1224 @@
+// engine.cpp -- host side of the counting engine: the C ABI of include/tpcf.h.
+//
+// Responsibilities
+//   * catalogs: host copy + device-resident float4 points;
+//   * spatial views: a catalog range is reordered by a balanced k-d split into
+//     tiles of exactly TILE points (last tile partial), each with an
+//     axis-aligned bounding box; cached per (catalog, range);
+//   * task planning: the reference's loop nest becomes a list of tile triples
+//     (pairs).  Symmetric loop nests (DDD/RRR: i<=j<=k over one array; DRR: j<=k
+//     over one array; DDR: i,j over one array) are enumerated canonically so
+//     that each unordered set of points is visited once; everything else is
+//     enumerated as ordered tile triples with the reference's index predicate
+//     evaluated per triangle.  Tile triples whose bounding boxes prove that no
+//     triangle can reach a counted bin are skipped (exact: a rigorous lower
+//     bound on every side is compared with the largest side any counted
+//     triangle can have);
+//   * launches: one persistent kernel per (kind, binning, precision) group,
+//     then the exact recheck of guard-band triangles, then D2H of the counts;
+//   * glibc acosf exception table for exact theta (built from the host libm by
+//     an exhaustive scan of [-1, 1], cached on disk);
+//   * serving: submit/wait with a worker thread that batches every pending job
+//     of compatible binning into the next launch (continuous batching), with
+//     admission by device-memory footprint.
+#include "../../include/tpcf.h"
+#include "engine.h"
+#include "exact_acos.h"
+
+#include <cuda_runtime.h>
+#include <dlfcn.h>
+#include <gnu/libc-version.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <thread>
+#include <tuple>
+#include <vector>
+
+using namespace tpcf;
+
+namespace {
+
+thread_local std::string g_tls_error;
+
+struct CudaError {
+    cudaError_t e;
+};
+
+#define CK(x)                                             \
+    do {                                                  \
+        cudaError_t _e = (x);                             \
+        if (_e != cudaSuccess) throw CudaError{_e};       \
+    } while (0)
+
+struct InvalidArg {
+    std::string msg;
+};
+
+// ---------------------------------------------------------------------------
+// device buffers
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void reserve(size_t m) {
+        if (m <= n) return;
+        release();
+        CK(cudaMalloc((void**)&p, std::max<size_t>(m, 1) * sizeof(T)));
+        n = m;
+    }
+    size_t bytes() const { return n * sizeof(T); }
+};
+
+struct Box {
+    float lo[3], hi[3];
+};
+
+struct Catalog {
+    std::vector<float> x, y, z;
+    int64_t n = 0;
+};
+
+struct View {
+    int64_t n = 0;
+    int ntiles = 0;
+    DevBuf<float4> pts;          // sorted points, .w = loop index (int bits)
+    DevBuf<int32_t> tile_start;  // ntiles + 1
+    std::vector<int32_t> h_tile_start;
+    std::vector<Box> boxes;
+    size_t bytes() const { return pts.bytes() + tile_start.bytes(); }
+};
+
+// Balanced k-d split: order[lo, hi) is split along the widest axis so that the
+// left part holds a multiple of TILE points, recursively, until parts hold at
+// most TILE points.  Leaves appear in order, giving spatially compact tiles.
+void kd_order(const float* xyz, std::vector<int32_t>& order, int64_t lo, int64_t hi) {
+    int64_t n = hi - lo;
+    if (n <= TILE) return;
+    float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int64_t i = lo; i < hi; i++)
+        for (int a = 0; a < 3; a++) {
+            float v = xyz[3 * (int64_t)order[i] + a];
+            mn[a] = std::min(mn[a], v);
+            mx[a] = std::max(mx[a], v);
+        }
+    int ax = 0;
+    for (int a = 1; a < 3; a++)
+        if (mx[a] - mn[a] > mx[ax] - mn[ax]) ax = a;
+    int64_t ntile = (n + TILE - 1) / TILE;
+    int64_t left = ((ntile + 1) / 2) * TILE;
+    if (left >= n) left = n - TILE;
+    int64_t mid = lo + left;
+    std::nth_element(order.begin() + lo, order.begin() + mid, order.begin() + hi, [&](int32_t p, int32_t q) {
+        float vp = xyz[3 * (int64_t)p + ax], vq = xyz[3 * (int64_t)q + ax];
+        return vp < vq || (vp == vq && p < q);
+    });
+    kd_order(xyz, order, lo, mid);
+    kd_order(xyz, order, mid, hi);
+}
+
+// Lower bound on the reference's float side length between any point of box
+// a and any point of box b (computed in double, then reduced by a relative
+// margin that covers the float rounding of the reference's distance).
+double box_lower_bound(const Box& a, const Box& b) {
+    double s = 0;
+    for (int k = 0; k < 3; k++) {
+        double g = std::max({0.0, (double)a.lo[k] - (double)b.hi[k], (double)b.lo[k] - (double)a.hi[k]});
+        s += g * g;
+    }
+    return sqrt(s) * (1.0 - 1e-5);
+}
+
+// ---------------------------------------------------------------------------
+// exact glibc acosf exception table
+
+struct AcosHost {
+    std::vector<uint32_t> keys, vals, bucket;
+};
+
+std::string cache_dir() {
+    const char* env = getenv("TPCF_CACHE_DIR");
+    if (env && *env) return env;
+    Dl_info info;
+    if (dladdr((void*)&cache_dir, &info) && info.dli_fname) {
+        std::string p = info.dli_fname;
+        size_t s = p.rfind('/');
+        std::string dir = s == std::string::npos ? "." : p.substr(0, s);
+        return dir + "/../_cache";
+    }
+    return "/tmp/tpcf_cache";
+}
+
+void mkdirs(const std::string& d) {
+    std::string cur;
+    for (size_t i = 0; i < d.size(); i++) {
+        cur += d[i];
+        if (d[i] == '/' && cur.size() > 1) mkdir(cur.c_str(), 0755);
+    }
+    mkdir(d.c_str(), 0755);
+}
+
+uint32_t fbits(float f) {
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    return u;
+}
+float ffrom(uint32_t u) {
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+}
+
+// Exhaustive scan of every float c in [-1, 1]: record where the host libm's
+// acosf differs from (float)tpcf_acos_d(c).
+AcosHost build_acos_table() {
+    const uint32_t spans[2][2] = {{0x00000000u, 0x3f800001u}, {0x80000000u, 0xbf800001u}};
+    unsigned nt = std::max(1u, std::thread::hardware_concurrency());
+    const uint32_t chunks = 512;
+    struct Part {
+        std::vector<uint32_t> k, v;
+    };
+    std::vector<Part> parts(2 * chunks);
+    std::atomic<uint32_t> next(0);
+    auto work = [&]() {
+        for (;;) {
+            uint32_t c = next.fetch_add(1);
+            if (c >= 2 * chunks) break;
+            uint32_t side = c / chunks, part = c % chunks;
+            uint64_t lo = spans[side][0], hi = spans[side][1];
+            uint64_t len = hi - lo;
+            uint64_t a = lo + len * part / chunks, b = lo + len * (part + 1) / chunks;
+            Part& P = parts[c];
+            for (uint64_t u = a; u < b; u++) {
+                float x = ffrom((uint32_t)u);
+                float g = acosf(x);
+                float r = (float)tpcf_acos_d((double)x);
+                if (fbits(g) != fbits(r)) {
+                    P.k.push_back((uint32_t)u);
+                    P.v.push_back(fbits(g));
+                }
+            }
+        }
+    };
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nt; t++) th.emplace_back(work);
+    for (auto& t : th) t.join();
+    AcosHost h;
+    for (auto& P : parts) {
+        h.keys.insert(h.keys.end(), P.k.begin(), P.k.end());
+        h.vals.insert(h.vals.end(), P.v.begin(), P.v.end());
+    }
+    h.bucket.assign(65537, 0);
+    size_t i = 0;
+    for (uint32_t b = 0; b <= 65536; b++) {
+        while (i < h.keys.size() && (h.keys[i] >> 16) < b) i++;
+        h.bucket[b] = (uint32_t)i;
+    }
+    return h;
+}
+
+std::string acos_cache_path() {
+    char name[256];
+    // the table depends on the C library's acosf, the architecture and this
+    // file's tpcf_acos_d; a probe value keys the latter
+    uint32_t probe = fbits((float)tpcf_acos_d(0.3)) ^ fbits((float)tpcf_acos_d(-0.87));
+#if defined(__aarch64__)
+    const char* arch = "aarch64";
+#elif defined(__x86_64__)
+    const char* arch = "x86_64";
+#else
+    const char* arch = "other";
+#endif
+    snprintf(name, sizeof(name), "/acosf_exc_v1_%s_glibc%s_%08x.bin", arch, gnu_get_libc_version(), probe);
+    return cache_dir() + name;
+}
+
+AcosHost load_or_build_acos_table() {
+    std::string path = acos_cache_path();
+    FILE* f = fopen(path.c_str(), "rb");
+    if (f) {
+        AcosHost h;
+        uint32_t n = 0;
+        bool ok = fread(&n, 4, 1, f) == 1 && n < (1u << 28);
+        if (ok) {
+            h.keys.resize(n);
+            h.vals.resize(n);
+            h.bucket.resize(65537);
+            ok = fread(h.keys.data(), 4, n, f) == n && fread(h.vals.data(), 4, n, f) == n &&
+                 fread(h.bucket.data(), 4, 65537, f) == 65537;
+        }
+        fclose(f);
+        if (ok) return h;
+    }
+    AcosHost h = build_acos_table();
+    mkdirs(cache_dir());
+    std::string tmp = path + ".tmp" + std::to_string(getpid());
+    f = fopen(tmp.c_str(), "wb");
+    if (f) {
+        uint32_t n = (uint32_t)h.keys.size();
+        bool ok = fwrite(&n, 4, 1, f) == 1 && fwrite(h.keys.data(), 4, n, f) == n &&
+                  fwrite(h.vals.data(), 4, n, f) == n && fwrite(h.bucket.data(), 4, 65537, f) == 65537;
+        fclose(f);
+        if (ok) rename(tmp.c_str(), path.c_str());
+        else unlink(tmp.c_str());
+    }
+    return h;
+}
+
+// ---------------------------------------------------------------------------
+// binning
+
+struct Binning {
+    int kind = 0;
+    TriParams tri{};
+    ThreeParams three{};
+    PairParams pair{};
+    int len = 0;
+    double lmax = INFINITY;   // no counted triangle/pair has a side >= lmax
+    double lmin_pair = 0;     // pairs: no counted pair has d < lmin_pair
+};
+
+float ref_bw(float lo, float hi, int n) {
+    // (hist_max - hist_min)/nbins in float, as distance_to_bin computes it
+    volatile float d = hi - lo;
+    volatile float r = d / (float)n;
+    return r;
+}
+
+Binning make_binning(const tpcf_spec& sp) {
+    Binning b;
+    b.kind = sp.kind;
+    auto check_axis = [](const tpcf_axis& a, const char* what) {
+        if (a.nbins <= 0 || a.nbins > 100000) throw InvalidArg{std::string("bad nbins for ") + what};
+        if (!(a.hi > a.lo)) throw InvalidArg{std::string("need hi > lo for ") + what};
+    };
+    if (sp.kind == TPCF_THREE_SIDE) {
+        check_axis(sp.axis[0], "three-side axis");
+        ThreeParams& p = b.three;
+        p.n = sp.axis[0].nbins;
+        if ((int64_t)p.n * p.n * p.n > (1 << 29)) throw InvalidArg{"three-side nbins too large"};
+        p.lo = sp.axis[0].lo;
+        p.hi = sp.axis[0].hi;
+        p.bw = ref_bw(p.lo, p.hi, p.n);
+        p.clean = sp.overflow == TPCF_OVERFLOW_CLEAN;
+        p.len = p.n * p.n * p.n;
+        b.len = p.len;
+        if (p.clean) b.lmax = (double)p.hi * (1 + 1e-6);
+    } else if (sp.kind == TPCF_TRIANGLE) {
+        for (int a = 0; a < 3; a++) check_axis(sp.axis[a], "triangle axis");
+        TriParams& p = b.tri;
+        p.S = sp.axis[0].nbins;
+        p.Q = sp.axis[1].nbins;
+        p.T = sp.axis[2].nbins;
+        if ((int64_t)p.S * p.Q * p.T > (1 << 26)) throw InvalidArg{"triangle binning too large"};
+        p.len = p.S * p.Q * p.T;
+        p.s_lo = sp.axis[0].lo;
+        p.s_hi = sp.axis[0].hi;
+        p.s_bw = ref_bw(p.s_lo, p.s_hi, p.S);
+        p.q_lo = sp.axis[1].lo;
+        p.q_hi = sp.axis[1].hi;
+        p.q_bw = ref_bw(p.q_lo, p.q_hi, p.Q);
+        p.t_lo = sp.axis[2].lo;
+        p.t_hi = sp.axis[2].hi;
+        p.t_bw = ref_bw(p.t_lo, p.t_hi, p.T);
+        p.nan_zero = sp.nan_policy == TPCF_NAN_ZERO;
+        // q coordinate: (q - q_lo)/q_bw; guard covers |fast - reference| <= ~9 ulp(q)/q_bw
+        double qs = 1.0 / (double)p.q_bw;
+        p.q_scale = (float)qs;
+        p.q_off = (float)(-(double)p.q_lo * qs - 0.5);
+        double qmax = std::max(fabs((double)p.q_lo), fabs((double)p.q_hi));
+        p.q_thr = (float)(0.5 - (8e-7 * qmax * qs + 2e-6));
+        // theta coordinate: acos(c)/(pi' t_bw) - t_lo/t_bw with pi' = 3.14159
+        const double pi_ref = 3.14159, pi = 3.14159265358979323846;
+        double K = 1.0 / (pi_ref * (double)p.t_bw);
+        static const double coef[6] = {1.5707956894727488, -0.2145428141209928, 0.08817102789580339,
+                                       -0.0459271445289548, 0.020619951348088413, -0.004911124693855812};
+        for (int i = 0; i < 6; i++) p.t_coef[i] = (float)(coef[i] * K);
+        p.t_half = (float)(K * pi / 2);
+        p.t_off0 = (float)(K * pi / 2 - (double)p.t_lo / (double)p.t_bw - 0.5);
+        // fixed part: polynomial (6.4e-7 rad) + float evaluation + reference
+        // acosf (<= 1.5 ulp) and roundings, bounded by 4e-6 rad; plus relative
+        // rounding of the coordinate itself
+        double tmax = std::max(fabs((double)p.t_lo), fabs((double)p.t_hi)) / (double)p.t_bw + K * pi;
+        double A = 4e-6 * K + 1e-6 * tmax + 2e-6;
+        p.t_thrA = (float)(0.5 - A);
+        // c-dependent part: |dc| <= 5e-7 |c| amplified by 1/sqrt(1-c^2) <= 1/sqrt(1-|c|)
+        p.t_thrB = (float)(5e-7 * K);
+        p.t2_off = (float)((1.0 - 3.0 * (double)p.t_lo) / (double)p.t_bw - 1.5);
+        p.theta_full = (p.t_lo <= 0.f && p.t_hi >= 1.f);
+        b.len = p.len;
+        // every counted permutation needs shortest or middle side < s_hi and a
+        // ratio < q_hi; all sides are then below s_hi (1 + q_hi)
+        if (p.s_hi > 0 && p.q_hi > 0) b.lmax = (double)p.s_hi * (1.0 + (double)p.q_hi) * (1 + 1e-5) + 1e-6;
+    } else if (sp.kind == TPCF_PAIR) {
+        check_axis(sp.axis[0], "pair axis");
+        PairParams& p = b.pair;
+        p.n = sp.axis[0].nbins;
+        p.lo = sp.axis[0].lo;
+        p.hi = sp.axis[0].hi;
+        p.bw = ref_bw(p.lo, p.hi, p.n);
+        b.len = p.n;
+        b.lmax = (double)p.hi * (1 + 1e-6) + 1e-6;
+    } else {
+        throw InvalidArg{"unknown kind"};
+    }
+    if (!sp.prune) b.lmax = INFINITY;
+    return b;
+}
+
+bool same_binning(const tpcf_spec& a, const tpcf_spec& b) {
+    if (a.kind != b.kind || a.precision != b.precision) return false;
+    if (a.kind == TPCF_TRIANGLE && a.nan_policy != b.nan_policy) return false;
+    if (a.kind == TPCF_THREE_SIDE && a.overflow != b.overflow) return false;
+    int na = a.kind == TPCF_TRIANGLE ? 3 : 1;
+    for (int i = 0; i < na; i++)
+        if (a.axis[i].lo != b.axis[i].lo || a.axis[i].hi != b.axis[i].hi || a.axis[i].nbins != b.axis[i].nbins)
+            return false;
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// loop units (the reference's numcalc / fake_tot)
+
+uint64_t loop_units(int kind, int loop, const int64_t n[3]) {
+    if (kind == TPCF_THREE_SIDE) return (uint64_t)n[0] * n[1] * n[2];
+    if (kind == TPCF_PAIR) {
+        if (loop == TPCF_LOOP_SAME) {
+            uint64_t u = 0;
+            for (int64_t i = 0; i < n[0]; i++) u += i < n[1] ? (uint64_t)(n[1] - i) : 0;
+            return u;
+        }
+        return (uint64_t)n[0] * n[1];
+    }
+    if (loop == TPCF_LOOP_ALL) return (uint64_t)n[0] * n[1] * n[2];
+    uint64_t u = 0;
+    for (int64_t j = 0; j < n[1]; j++) {
+        uint64_t ks = j < n[2] ? (uint64_t)(n[2] - j) : 0;
+        uint64_t is = loop == TPCF_LOOP_SAME ? (uint64_t)std::min<int64_t>(n[0], j + 1) : (uint64_t)n[0];
+        u += is * ks;
+    }
+    return u;
+}
+
+// ---------------------------------------------------------------------------
+// context
+
+struct Pending {
+    uint64_t ticket;
+    tpcf_spec spec;
+    tpcf_job job;
+    std::vector<uint64_t> result;
+    tpcf_status status = 1;  // 1 = pending
+    bool cancelled = false;
+};
+
+struct GroupJob {
+    const tpcf_spec* spec;
+    const tpcf_job* job;
+    uint64_t* out;
+};
+
+}  // namespace
+
+struct tpcf_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_mid = nullptr;
+    uint64_t h2d = 0, d2h = 0;  // bytes copied since the last stats reset
+    std::recursive_mutex mu;  // serialises device work on this context
+    std::string last_error;
+    uint64_t next_handle = 1;
+    std::map<uint64_t, std::shared_ptr<Catalog>> catalogs;
+    std::map<uint64_t, std::shared_ptr<DevBuf<float4>>> cat_dev;  // unsorted points (resident)
+    std::map<std::tuple<uint64_t, int64_t, int64_t>, std::shared_ptr<View>> views;
+    // acos table
+    bool acos_ready = false;
+    DevBuf<uint32_t> acos_keys, acos_vals, acos_bucket;
+    uint32_t acos_n = 0;
+    // scratch
+    DevBuf<DevJob> d_jobs;
+    DevBuf<uint4> d_tasks;
+    DevBuf<unsigned int> d_counters;  // [0] task counter, [1] recheck count
+    DevBuf<uint4> d_queue;
+    DevBuf<unsigned long long> d_hist;
+    std::vector<unsigned long long> h_hist;
+    tpcf_stats stats{};
+    // serving
+    std::mutex qmu;
+    std::condition_variable qcv;
+    std::deque<std::shared_ptr<Pending>> queue;
+    std::map<uint64_t, std::shared_ptr<Pending>> tickets;
+    uint64_t next_ticket = 1;
+    std::thread worker;
+    bool stop = false;
+    int64_t admit_bytes = (int64_t)8 << 30;
+};
+
+namespace {
+
+tpcf_status fail(tpcf_ctx* ctx, tpcf_status s, const std::string& msg) {
+    if (ctx) ctx->last_error = msg;
+    g_tls_error = msg;
+    return s;
+}
+
+std::shared_ptr<View> get_view(tpcf_ctx* ctx, uint64_t handle, int64_t begin, int64_t end) {
+    auto it = ctx->catalogs.find(handle);
+    if (it == ctx->catalogs.end()) throw InvalidArg{"unknown catalog handle"};
+    const Catalog& c = *it->second;
+    if (end < 0) end = c.n;
+    if (begin < 0 || begin > end || end > c.n) throw InvalidArg{"catalog range out of bounds"};
+    auto key = std::make_tuple(handle, begin, end);
+    auto vi = ctx->views.find(key);
+    if (vi != ctx->views.end()) return vi->second;
+    auto v = std::make_shared<View>();
+    int64_t n = end - begin;
+    v->n = n;
+    std::vector<float> xyz(3 * (size_t)n);
+    for (int64_t i = 0; i < n; i++) {
+        xyz[3 * i] = c.x[begin + i];
+        xyz[3 * i + 1] = c.y[begin + i];
+        xyz[3 * i + 2] = c.z[begin + i];
+    }
+    std::vector<int32_t> order(n);
+    std::iota(order.begin(), order.end(), 0);
+    kd_order(xyz.data(), order, 0, n);
+    v->ntiles = (int)((n + TILE - 1) / TILE);
+    std::vector<float4> pts(std::max<int64_t>(n, 1));
+    for (int64_t i = 0; i < n; i++) {
+        int32_t o = order[i];
+        float4 p;
+        p.x = xyz[3 * (size_t)o];
+        p.y = xyz[3 * (size_t)o + 1];
+        p.z = xyz[3 * (size_t)o + 2];
+        int32_t key_i = o;  // loop index inside the range
+        memcpy(&p.w, &key_i, 4);
+        pts[i] = p;
+    }
+    v->h_tile_start.resize(v->ntiles + 1);
+    v->boxes.resize(v->ntiles);
+    for (int t = 0; t <= v->ntiles; t++) v->h_tile_start[t] = (int32_t)std::min<int64_t>((int64_t)t * TILE, n);
+    for (int t = 0; t < v->ntiles; t++) {
+        Box b;
+        for (int a = 0; a < 3; a++) {
+            b.lo[a] = INFINITY;
+            b.hi[a] = -INFINITY;
+        }
+        for (int i = v->h_tile_start[t]; i < v->h_tile_start[t + 1]; i++) {
+            const float* q = &pts[i].x;
+            for (int a = 0; a < 3; a++) {
+                b.lo[a] = std::min(b.lo[a], q[a]);
+                b.hi[a] = std::max(b.hi[a], q[a]);
+            }
+        }
+        v->boxes[t] = b;
+    }
+    v->pts.reserve(pts.size());
+    CK(cudaMemcpyAsync(v->pts.p, pts.data(), pts.size() * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
+    ctx->h2d += pts.size() * sizeof(float4) + (v->ntiles + 1) * sizeof(int32_t);
+    v->tile_start.reserve(v->ntiles + 1);
+    CK(cudaMemcpyAsync(v->tile_start.p, v->h_tile_start.data(), (v->ntiles + 1) * sizeof(int32_t),
+                       cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->views[key] = v;
+    return v;
+}
+
+void ensure_acos(tpcf_ctx* ctx) {
+    if (ctx->acos_ready) return;
+    AcosHost h = load_or_build_acos_table();
+    ctx->acos_n = (uint32_t)h.keys.size();
+    ctx->acos_keys.reserve(std::max<size_t>(h.keys.size(), 1));
+    ctx->acos_vals.reserve(std::max<size_t>(h.vals.size(), 1));
+    ctx->acos_bucket.reserve(65537);
+    if (!h.keys.empty()) {
+        CK(cudaMemcpy(ctx->acos_keys.p, h.keys.data(), h.keys.size() * 4, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(ctx->acos_vals.p, h.vals.data(), h.vals.size() * 4, cudaMemcpyHostToDevice));
+    }
+    CK(cudaMemcpy(ctx->acos_bucket.p, h.bucket.data(), 65537 * 4, cudaMemcpyHostToDevice));
+    ctx->acos_ready = true;
+}
+
+AcosTable acos_table(tpcf_ctx* ctx) {
+    AcosTable t;
+    t.keys = ctx->acos_keys.p;
+    t.vals = ctx->acos_vals.p;
+    t.bucket = ctx->acos_bucket.p;
+    t.n = ctx->acos_n;
+    return t;
+}
+
+struct PlannedJob {
+    std::shared_ptr<View> v[3];
+    uint64_t loop_units = 0;
+};
+
+inline bool close_enough(const View& a, int ta, const View& b, int tb, double lmax) {
+    if (!(lmax < INFINITY)) return true;
+    return box_lower_bound(a.boxes[ta], b.boxes[tb]) < lmax;
+}
+
+std::vector<std::vector<int>> neighbours(const View& a, const View& b, double lmax) {
+    std::vector<std::vector<int>> nb(a.ntiles);
+    for (int i = 0; i < a.ntiles; i++)
+        for (int j = 0; j < b.ntiles; j++)
+            if (close_enough(a, i, b, j, lmax)) nb[i].push_back(j);
+    return nb;
+}
+
+uint64_t task_units3(const View& A, int a, const View& B, int b, const View& C, int c, uint32_t flags) {
+    uint64_t na = A.h_tile_start[a + 1] - A.h_tile_start[a];
+    uint64_t nb = B.h_tile_start[b + 1] - B.h_tile_start[b];
+    uint64_t nc = C.h_tile_start[c + 1] - C.h_tile_start[c];
+    bool dij = flags & TASK_DIAG_IJ, djk = flags & TASK_DIAG_JK;
+    if (dij && djk) return na * (na - 1) * (na - 2) / 6;
+    if (dij) return na * (na - 1) / 2 * nc;
+    if (djk) return na * (nb * (nb - 1) / 2);
+    return na * nb * nc;
+}
+
+// Tile tasks of one triangle/three-side job.
+void plan_triplets(const tpcf_spec& sp, const PlannedJob& pj, uint32_t slot, double lmax,
+                   std::vector<std::pair<uint64_t, uint4>>& tasks, uint64_t& evaluated) {
+    const View &A = *pj.v[0], &B = *pj.v[1], &C = *pj.v[2];
+    const bool sameAB = pj.v[0] == pj.v[1], sameBC = pj.v[1] == pj.v[2];
+    auto add = [&](int a, int b, int c, uint32_t pred, uint32_t flags) {
+        uint64_t u = task_units3(A, a, B, b, C, c, flags);
+        if (u == 0) return;
+        evaluated += u;
+        tasks.push_back({u, make_uint4(slot | (pred << TASK_PRED_SHIFT) | flags, (uint32_t)a, (uint32_t)b,
+                                       (uint32_t)c)});
+    };
+    if (A.ntiles == 0 || B.ntiles == 0 || C.ntiles == 0) return;
+    auto nAB = neighbours(A, B, lmax);
+    auto nAC = neighbours(A, C, lmax);
+    std::vector<std::vector<char>> okBC;
+    const bool prune = lmax < INFINITY;
+    if (prune) {
+        okBC.assign(B.ntiles, std::vector<char>(C.ntiles, 0));
+        for (int b = 0; b < B.ntiles; b++)
+            for (int c = 0; c < C.ntiles; c++) okBC[b][c] = close_enough(B, b, C, c, lmax);
+    }
+    auto bc_ok = [&](int b, int c) { return !prune || okBC[b][c]; };
+    if (sp.kind == TPCF_TRIANGLE && sp.loop == TPCF_LOOP_SAME && sameAB && sameBC) {
+        // i <= j <= k over one array: unordered distinct triples
+        for (int a = 0; a < A.ntiles; a++)
+            for (int b : nAB[a]) {
+                if (b < a) continue;
+                for (int c : nAC[a]) {
+                    if (c < b || !bc_ok(b, c)) continue;
+                    uint32_t f = (a == b ? TASK_DIAG_IJ : 0) | (b == c ? TASK_DIAG_JK : 0);
+                    add(a, b, c, PRED_NONE, f);
+                }
+            }
+    } else if (sp.kind == TPCF_TRIANGLE && sp.loop == TPCF_LOOP_ONE && sameBC) {
+        // j <= k over one array (j == k has a zero side): unordered pairs
+        for (int a = 0; a < A.ntiles; a++)
+            for (int b : nAB[a])
+                for (int c : nAC[a]) {
+                    if (c < b || !bc_ok(b, c)) continue;
+                    add(a, b, c, PRED_NONE, b == c ? TASK_DIAG_JK : 0);
+                }
+    } else if (sp.kind == TPCF_TRIANGLE && sp.loop == TPCF_LOOP_ONE && sameAB) {
+        // every ordered (i, j) of one array, k >= j: unordered {i, j} with
+        // weight [k >= i] + [k >= j]
+        for (int a = 0; a < A.ntiles; a++)
+            for (int b : nAB[a]) {
+                if (b < a) continue;
+                for (int c : nAC[a]) {
+                    if (!bc_ok(b, c)) continue;
+                    add(a, b, c, PRED_DDR, a == b ? TASK_DIAG_IJ : 0);
+                }
+            }
+    } else {
+        uint32_t pred = PRED_NONE;
+        if (sp.kind == TPCF_TRIANGLE) pred = sp.loop == TPCF_LOOP_SAME ? PRED_SAME : sp.loop == TPCF_LOOP_ONE ? PRED_ONE : PRED_NONE;
+        for (int a = 0; a < A.ntiles; a++)
+            for (int b : nAB[a])
+                for (int c : nAC[a])
+                    if (bc_ok(b, c)) add(a, b, c, pred, 0);
+    }
+}
+
+void plan_pairs(const tpcf_spec& sp, const PlannedJob& pj, uint32_t slot, double lmax,
+                std::vector<std::pair<uint64_t, uint4>>& tasks, uint64_t& evaluated) {
+    const View &A = *pj.v[0], &B = *pj.v[1];
+    if (A.ntiles == 0 || B.ntiles == 0) return;
+    const bool same = pj.v[0] == pj.v[1] && sp.loop == TPCF_LOOP_SAME;
+    for (int a = 0; a < A.ntiles; a++)
+        for (int b = same ? a : 0; b < B.ntiles; b++) {
+            if (!close_enough(A, a, B, b, lmax)) continue;
+            uint64_t na = A.h_tile_start[a + 1] - A.h_tile_start[a], nb = B.h_tile_start[b + 1] - B.h_tile_start[b];
+            uint32_t flags = 0, pred = PRED_NONE;
+            uint64_t u = na * nb;
+            if (same && a == b) {
+                flags = TASK_DIAG_IJ;
+                u = na * (na + 1) / 2;
+            } else if (!same && sp.loop == TPCF_LOOP_SAME) {
+                pred = PRED_SAME;
+            }
+            evaluated += u;
+            tasks.push_back({u, make_uint4(slot | (pred << TASK_PRED_SHIFT) | flags, (uint32_t)a, (uint32_t)b, 0)});
+        }
+}
+
+int occupancy_grid(tpcf_ctx* ctx, int kind, size_t smem, int fp64, uint64_t ntasks) {
+    (void)kind;
+    (void)fp64;
+    int per_sm = 1;
+    int max_smem = 0;
+    cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx->device);
+    if (smem > 0) per_sm = std::max(1, std::min(4, (int)(max_smem / (smem + 1024))));
+    else per_sm = 4;
+    uint64_t g = (uint64_t)ctx->num_sms * per_sm;
+    if (g > ntasks) g = std::max<uint64_t>(ntasks, 1);
+    return (int)g;
+}
+
+// Runs one group of jobs that share kind, binning and precision in a single
+// persistent launch.  outs[i] receives hist_len counts.
+void run_group(tpcf_ctx* ctx, const std::vector<GroupJob>& group) {
+    auto t_wall0 = std::chrono::steady_clock::now();
+    const tpcf_spec& sp = *group[0].spec;
+    Binning bin = make_binning(sp);
+    const int ncat = sp.kind == TPCF_PAIR ? 2 : 3;
+    if (group.size() > 0xFFFF) throw InvalidArg{"too many jobs in one batch"};
+    std::vector<PlannedJob> pj(group.size());
+    std::vector<DevJob> dj(group.size());
+    std::vector<std::pair<uint64_t, uint4>> tasks;
+    uint64_t evaluated = 0, units = 0;
+    size_t hist_total = (size_t)bin.len * group.size();
+    ctx->d_hist.reserve(hist_total);
+    for (size_t g = 0; g < group.size(); g++) {
+        const tpcf_job& job = *group[g].job;
+        int64_t n[3] = {0, 0, 0};
+        for (int r = 0; r < ncat; r++) {
+            pj[g].v[r] = get_view(ctx, job.catalog[r], job.begin[r], job.end[r]);
+            n[r] = pj[g].v[r]->n;
+        }
+        if (ncat == 2) pj[g].v[2] = pj[g].v[1];
+        pj[g].loop_units = loop_units(sp.kind, sp.loop, n);
+        units += pj[g].loop_units;
+        for (int r = 0; r < 3; r++) {
+            dj[g].pts[r] = pj[g].v[r]->pts.p;
+            dj[g].tile_start[r] = pj[g].v[r]->tile_start.p;
+        }
+        dj[g].hist = ctx->d_hist.p + (size_t)bin.len * g;
+        if (sp.kind == TPCF_PAIR) plan_pairs(sp, pj[g], (uint32_t)g, bin.lmax, tasks, evaluated);
+        else plan_triplets(sp, pj[g], (uint32_t)g, bin.lmax, tasks, evaluated);
+    }
+    // largest tasks first (dynamic fetch then balances the tail)
+    std::stable_sort(tasks.begin(), tasks.end(),
+                     [](const std::pair<uint64_t, uint4>& a, const std::pair<uint64_t, uint4>& b) { return a.first > b.first; });
+    std::vector<uint4> h_tasks(tasks.size());
+    for (size_t i = 0; i < tasks.size(); i++) h_tasks[i] = tasks[i].second;
+    ctx->d_jobs.reserve(dj.size());
+    ctx->d_tasks.reserve(std::max<size_t>(h_tasks.size(), 1));
+    ctx->d_counters.reserve(4);
+    cudaStream_t st = ctx->stream;
+    CK(cudaMemcpyAsync(ctx->d_jobs.p, dj.data(), dj.size() * sizeof(DevJob), cudaMemcpyHostToDevice, st));
+    ctx->h2d += dj.size() * sizeof(DevJob) + h_tasks.size() * sizeof(uint4);
+    if (!h_tasks.empty())
+        CK(cudaMemcpyAsync(ctx->d_tasks.p, h_tasks.data(), h_tasks.size() * sizeof(uint4), cudaMemcpyHostToDevice, st));
+    const bool fp64 = sp.precision == TPCF_PLAIN_FP64;
+    if (sp.kind == TPCF_TRIANGLE) ensure_acos(ctx);
+    uint64_t launches = 0;
+    unsigned int queue_cap = (unsigned int)std::max<size_t>(ctx->d_queue.n, (size_t)1 << 22);
+    for (int attempt = 0; attempt < 3; attempt++) {
+        CK(cudaMemsetAsync(ctx->d_hist.p, 0, hist_total * sizeof(unsigned long long), st));
+        CK(cudaMemsetAsync(ctx->d_counters.p, 0, 4 * sizeof(unsigned int), st));
+        CK(cudaEventRecord(ctx->ev0, st));
+        unsigned int nt = (unsigned int)h_tasks.size();
+        launches = 0;
+        if (sp.kind == TPCF_TRIANGLE) {
+            int copies = 8;
+            size_t smem_cap = 200 * 1024;
+            while (copies > 1 && triangle_smem_bytes(bin.len, copies) > smem_cap) copies /= 2;
+            if (triangle_smem_bytes(bin.len, copies) > 227 * 1024) throw InvalidArg{"triangle histogram too large for shared memory"};
+            size_t smem = triangle_smem_bytes(bin.len, copies);
+            int grid = occupancy_grid(ctx, sp.kind, smem, fp64, nt);
+            if (fp64) {
+                CK(launch_triangle_fp64(ctx->d_jobs.p, ctx->d_tasks.p, nt, ctx->d_counters.p, bin.tri, acos_table(ctx),
+                                        grid, copies, st));
+                CK(cudaEventRecord(ctx->ev_mid, st));
+                launches = 1;
+            } else {
+                ctx->d_queue.reserve(queue_cap);
+                RecheckQueue q;
+                q.items = ctx->d_queue.p;
+                q.count = ctx->d_counters.p + 1;
+                q.cap = queue_cap;
+                CK(launch_triangle_fast(ctx->d_jobs.p, ctx->d_tasks.p, nt, ctx->d_counters.p, bin.tri, q, grid, copies, st));
+                CK(cudaEventRecord(ctx->ev_mid, st));
+                CK(launch_triangle_recheck(ctx->d_jobs.p, q, bin.tri, acos_table(ctx), ctx->num_sms * 8, st));
+                launches = 2;
+            }
+        } else if (sp.kind == TPCF_THREE_SIDE) {
+            int copies = 8;
+            size_t smem_cap = 200 * 1024;
+            while (copies > 0 && three_side_smem_bytes(bin.len, copies) > smem_cap) copies /= 2;
+            size_t smem = three_side_smem_bytes(copies ? bin.len : 0, copies);
+            int grid = occupancy_grid(ctx, sp.kind, smem, fp64, nt);
+            CK(launch_three_side(ctx->d_jobs.p, ctx->d_tasks.p, nt, ctx->d_counters.p, bin.three, fp64, grid, copies, st));
+            CK(cudaEventRecord(ctx->ev_mid, st));
+            launches = 1;
+        } else {
+            int copies = 8;
+            while (copies > 1 && pair_smem_bytes(bin.len, copies) > 200 * 1024) copies /= 2;
+            if (pair_smem_bytes(bin.len, copies) > 227 * 1024) throw InvalidArg{"pair histogram too large"};
+            size_t smem = pair_smem_bytes(bin.len, copies);
+            int grid = occupancy_grid(ctx, sp.kind, smem, fp64, nt);
+            CK(launch_pairs(ctx->d_jobs.p, ctx->d_tasks.p, nt, ctx->d_counters.p, bin.pair, fp64, grid, copies, st));
+            CK(cudaEventRecord(ctx->ev_mid, st));
+            launches = 1;
+        }
+        CK(cudaEventRecord(ctx->ev1, st));
+        unsigned int counters[4];
+        CK(cudaMemcpyAsync(counters, ctx->d_counters.p, sizeof(counters), cudaMemcpyDeviceToHost, st));
+        ctx->h_hist.resize(hist_total);
+        CK(cudaMemcpyAsync(ctx->h_hist.data(), ctx->d_hist.p, hist_total * sizeof(unsigned long long),
+                           cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        ctx->d2h += sizeof(counters) + hist_total * sizeof(unsigned long long);
+        ctx->stats.recheck_units = counters[1];
+        if (sp.kind == TPCF_TRIANGLE && !fp64 && counters[1] > queue_cap) {
+            // the recheck queue overflowed: grow it and count again
+            queue_cap = (unsigned int)std::min<uint64_t>((uint64_t)counters[1] + (counters[1] >> 2) + 1024, 0xF0000000ull);
+            continue;
+        }
+        break;
+    }
+    float ms = 0, ms_main = 0;
+    CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    CK(cudaEventElapsedTime(&ms_main, ctx->ev0, ctx->ev_mid));
+    ctx->stats.main_kernel_ms = ms_main;
+    for (size_t g = 0; g < group.size(); g++)
+        memcpy(group[g].out, ctx->h_hist.data() + (size_t)bin.len * g, (size_t)bin.len * sizeof(uint64_t));
+    ctx->stats.kernel_ms = ms;
+    ctx->stats.loop_units = units;
+    ctx->stats.evaluated_units = evaluated;
+    ctx->stats.tasks = h_tasks.size();
+    ctx->stats.kernel_launches = launches;
+    ctx->stats.total_ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_wall0).count();
+}
+
+void validate(const tpcf_spec* sp, const tpcf_job* job) {
+    if (!sp || !job) throw InvalidArg{"null spec or job"};
+    if (sp->kind != TPCF_THREE_SIDE && sp->kind != TPCF_TRIANGLE && sp->kind != TPCF_PAIR) throw InvalidArg{"bad kind"};
+    if (sp->loop < TPCF_LOOP_ALL || sp->loop > TPCF_LOOP_ONE) throw InvalidArg{"bad loop"};
+    if (sp->precision != TPCF_GUARDED_FP32 && sp->precision != TPCF_PLAIN_FP64) throw InvalidArg{"bad precision"};
+    (void)make_binning(*sp);
+}
+
+template <typename F>
+tpcf_status guarded(tpcf_ctx* ctx, F&& f) {
+    try {
+        f();
+        return TPCF_OK;
+    } catch (const InvalidArg& e) {
+        return fail(ctx, TPCF_ERR_INVALID, e.msg);
+    } catch (const CudaError& e) {
+        cudaGetLastError();
+        if (e.e == cudaErrorMemoryAllocation) return fail(ctx, TPCF_ERR_OOM, cudaGetErrorString(e.e));
+        return fail(ctx, TPCF_ERR_CUDA, cudaGetErrorString(e.e));
+    } catch (const std::bad_alloc&) {
+        return fail(ctx, TPCF_ERR_OOM, "host allocation failed");
+    } catch (...) {
+        return fail(ctx, TPCF_ERR_INTERNAL, "unexpected exception");
+    }
+}
+
+// footprint estimate of a job for admission (views are shared and cached)
+int64_t job_bytes(tpcf_ctx* ctx, const tpcf_spec& sp, const tpcf_job& job) {
+    int64_t b = 0;
+    int nc = sp.kind == TPCF_PAIR ? 2 : 3;
+    for (int r = 0; r < nc; r++) {
+        auto it = ctx->catalogs.find(job.catalog[r]);
+        if (it == ctx->catalogs.end()) continue;
+        int64_t e = job.end[r] < 0 ? it->second->n : job.end[r];
+        b += (e - job.begin[r]) * (int64_t)sizeof(float4);
+    }
+    int64_t len = 0;
+    tpcf_hist_len(&sp, &len);
+    return b + len * 8;
+}
+
+void worker_loop(tpcf_ctx* ctx) {
+    for (;;) {
+        std::vector<std::shared_ptr<Pending>> batch;
+        {
+            std::unique_lock<std::mutex> lk(ctx->qmu);
+            ctx->qcv.wait(lk, [&] { return ctx->stop || !ctx->queue.empty(); });
+            if (ctx->stop && ctx->queue.empty()) return;
+            // admit the oldest job and every compatible pending job while the
+            // device-memory footprint stays within the admission budget
+            auto first = ctx->queue.front();
+            int64_t budget = ctx->admit_bytes, used = 0;
+            for (auto it = ctx->queue.begin(); it != ctx->queue.end();) {
+                auto& p = *it;
+                if (p->cancelled) {
+                    p->status = TPCF_ERR_CANCELLED;
+                    it = ctx->queue.erase(it);
+                    continue;
+                }
+                if (!same_binning(p->spec, first->spec) || p->spec.loop != first->spec.loop) {
+                    ++it;
+                    continue;
+                }
+                int64_t jb = job_bytes(ctx, p->spec, p->job);
+                if (!batch.empty() && used + jb > budget) break;
+                used += jb;
+                batch.push_back(p);
+                it = ctx->queue.erase(it);
+                if (batch.size() >= 4096) break;
+            }
+        }
+        ctx->qcv.notify_all();
+        if (batch.empty()) continue;
+        std::vector<GroupJob> group;
+        int64_t len = 0;
+        tpcf_hist_len(&batch[0]->spec, &len);
+        for (auto& p : batch) {
+            p->result.assign((size_t)len, 0);
+            group.push_back({&p->spec, &p->job, p->result.data()});
+        }
+        tpcf_status st;
+        {
+            std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+            st = guarded(ctx, [&] { run_group(ctx, group); });
+        }
+        {
+            std::lock_guard<std::mutex> lk(ctx->qmu);
+            for (auto& p : batch) p->status = st;
+        }
+        ctx->qcv.notify_all();
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+
+extern "C" {
+
+int32_t tpcf_abi_version(void) { return TPCF_ABI_VERSION; }
+
+const char* tpcf_status_string(tpcf_status s) {
+    switch (s) {
+        case TPCF_OK: return "ok";
+        case TPCF_ERR_INVALID: return "invalid argument";
+        case TPCF_ERR_CUDA: return "CUDA error";
+        case TPCF_ERR_NO_DEVICE: return "no CUDA device";
+        case TPCF_ERR_OOM: return "out of memory";
+        case TPCF_ERR_TIMEOUT: return "timeout";
+        case TPCF_ERR_NOT_FOUND: return "not found";
+        case TPCF_ERR_CANCELLED: return "cancelled";
+        case TPCF_ERR_INTERNAL: return "internal error";
+        case TPCF_ERR_IO: return "I/O error";
+        default: return "unknown status";
+    }
+}
+
+const char* tpcf_last_error(tpcf_ctx* ctx) { return ctx ? ctx->last_error.c_str() : g_tls_error.c_str(); }
+
+tpcf_status tpcf_create(tpcf_ctx** out, int32_t device) {
+    if (!out) return fail(nullptr, TPCF_ERR_INVALID, "null output pointer");
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) {
+        cudaGetLastError();
+        return fail(nullptr, TPCF_ERR_NO_DEVICE, "no CUDA device visible");
+    }
+    if (device < 0 || device >= count) return fail(nullptr, TPCF_ERR_INVALID, "device index out of range");
+    tpcf_ctx* ctx = new tpcf_ctx();
+    tpcf_status s = guarded(ctx, [&] {
+        ctx->device = device;
+        CK(cudaSetDevice(device));
+        CK(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device));
+        CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+        CK(cudaEventCreate(&ctx->ev0));
+        CK(cudaEventCreate(&ctx->ev1));
+        CK(cudaEventCreate(&ctx->ev_mid));
+        const char* adm = getenv("TPCF_ADMIT_BYTES");
+        if (adm) ctx->admit_bytes = atoll(adm);
+    });
+    if (s != TPCF_OK) {
+        g_tls_error = ctx->last_error;
+        delete ctx;
+        return s;
+    }
+    ctx->worker = std::thread(worker_loop, ctx);
+    *out = ctx;
+    return TPCF_OK;
+}
+
+tpcf_status tpcf_destroy(tpcf_ctx* ctx) {
+    if (!ctx) return TPCF_ERR_INVALID;
+    {
+        std::lock_guard<std::mutex> lk(ctx->qmu);
+        ctx->stop = true;
+    }
+    ctx->qcv.notify_all();
+    if (ctx->worker.joinable()) ctx->worker.join();
+    {
+        std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+        cudaSetDevice(ctx->device);
+        ctx->views.clear();
+        ctx->cat_dev.clear();
+        ctx->d_jobs.release();
+        ctx->d_tasks.release();
+        ctx->d_counters.release();
+        ctx->d_queue.release();
+        ctx->d_hist.release();
+        ctx->acos_keys.release();
+        ctx->acos_vals.release();
+        ctx->acos_bucket.release();
+        if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+        if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+        if (ctx->ev_mid) cudaEventDestroy(ctx->ev_mid);
+        if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    }
+    delete ctx;
+    return TPCF_OK;
+}
+
+tpcf_status tpcf_catalog_create(tpcf_ctx* ctx, const float* x, const float* y, const float* z, int64_t n,
+                                uint64_t* handle) {
+    if (!ctx || !handle || n < 0 || (n > 0 && (!x || !y || !z))) return fail(ctx, TPCF_ERR_INVALID, "bad catalog arguments");
+    if (n > (int64_t)1 << 30) return fail(ctx, TPCF_ERR_INVALID, "catalog too large");
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    return guarded(ctx, [&] {
+        CK(cudaSetDevice(ctx->device));
+        auto c = std::make_shared<Catalog>();
+        c->n = n;
+        c->x.assign(x, x + n);
+        c->y.assign(y, y + n);
+        c->z.assign(z, z + n);
+        auto d = std::make_shared<DevBuf<float4>>();
+        d->reserve(std::max<int64_t>(n, 1));
+        std::vector<float4> p(std::max<int64_t>(n, 1));
+        for (int64_t i = 0; i < n; i++) {
+            p[i].x = x[i];
+            p[i].y = y[i];
+            p[i].z = z[i];
+            int32_t k = (int32_t)i;
+            memcpy(&p[i].w, &k, 4);
+        }
+        CK(cudaMemcpy(d->p, p.data(), p.size() * sizeof(float4), cudaMemcpyHostToDevice));
+        ctx->h2d += p.size() * sizeof(float4);
+        uint64_t h = ctx->next_handle++;
+        ctx->catalogs[h] = c;
+        ctx->cat_dev[h] = d;
+        *handle = h;
+    });
+}
+
+tpcf_status tpcf_catalog_release(tpcf_ctx* ctx, uint64_t handle) {
+    if (!ctx) return TPCF_ERR_INVALID;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!ctx->catalogs.count(handle)) return fail(ctx, TPCF_ERR_NOT_FOUND, "unknown catalog handle");
+    ctx->catalogs.erase(handle);
+    ctx->cat_dev.erase(handle);
+    for (auto it = ctx->views.begin(); it != ctx->views.end();) {
+        if (std::get<0>(it->first) == handle) it = ctx->views.erase(it);
+        else ++it;
+    }
+    return TPCF_OK;
+}
+
+tpcf_status tpcf_resident_bytes(tpcf_ctx* ctx, int64_t* bytes) {
+    if (!ctx || !bytes) return TPCF_ERR_INVALID;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    int64_t b = 0;
+    for (auto& kv : ctx->cat_dev) b += (int64_t)kv.second->bytes();
+    for (auto& kv : ctx->views) b += (int64_t)kv.second->bytes();
+    *bytes = b;
+    return TPCF_OK;
+}
+
+tpcf_status tpcf_hist_len(const tpcf_spec* sp, int64_t* len) {
+    if (!sp || !len) return TPCF_ERR_INVALID;
+    if (sp->kind == TPCF_THREE_SIDE) *len = (int64_t)sp->axis[0].nbins * sp->axis[0].nbins * sp->axis[0].nbins;
+    else if (sp->kind == TPCF_TRIANGLE) *len = (int64_t)sp->axis[0].nbins * sp->axis[1].nbins * sp->axis[2].nbins;
+    else if (sp->kind == TPCF_PAIR) *len = sp->axis[0].nbins;
+    else return TPCF_ERR_INVALID;
+    return TPCF_OK;
+}
+
+tpcf_status tpcf_loop_units(tpcf_ctx* ctx, const tpcf_spec* sp, const tpcf_job* job, uint64_t* units) {
+    if (!ctx || !sp || !job || !units) return TPCF_ERR_INVALID;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    int64_t n[3] = {0, 0, 0};
+    int nc = sp->kind == TPCF_PAIR ? 2 : 3;
+    for (int r = 0; r < nc; r++) {
+        auto it = ctx->catalogs.find(job->catalog[r]);
+        if (it == ctx->catalogs.end()) return fail(ctx, TPCF_ERR_NOT_FOUND, "unknown catalog handle");
+        int64_t e = job->end[r] < 0 ? it->second->n : job->end[r];
+        n[r] = e - job->begin[r];
+    }
+    *units = loop_units(sp->kind, sp->loop, n);
+    return TPCF_OK;
+}
+
+tpcf_status tpcf_count_batch(tpcf_ctx* ctx, const tpcf_spec* specs, const tpcf_job* jobs, int32_t n,
+                             uint64_t* const* hists) {
+    if (!ctx || !specs || !jobs || !hists || n < 0) return fail(ctx, TPCF_ERR_INVALID, "bad batch arguments");
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    return guarded(ctx, [&] {
+        CK(cudaSetDevice(ctx->device));
+        for (int i = 0; i < n; i++) {
+            validate(&specs[i], &jobs[i]);
+            if (!hists[i]) throw InvalidArg{"null histogram pointer"};
+        }
+        // group by (binning, loop); each group is one persistent launch
+        std::vector<char> done(n, 0);
+        tpcf_stats acc{};
+        for (int i = 0; i < n; i++) {
+            if (done[i]) continue;
+            std::vector<GroupJob> g;
+            for (int k = i; k < n; k++)
+                if (!done[k] && same_binning(specs[k], specs[i]) && specs[k].loop == specs[i].loop &&
+                    specs[k].prune == specs[i].prune) {
+                    g.push_back({&specs[k], &jobs[k], hists[k]});
+                    done[k] = 1;
+                }
+            run_group(ctx, g);
+            acc.kernel_ms += ctx->stats.kernel_ms;
+            acc.total_ms += ctx->stats.total_ms;
+            acc.loop_units += ctx->stats.loop_units;
+            acc.evaluated_units += ctx->stats.evaluated_units;
+            acc.recheck_units += ctx->stats.recheck_units;
+            acc.tasks += ctx->stats.tasks;
+            acc.kernel_launches += ctx->stats.kernel_launches;
+        }
+        ctx->stats = acc;
+    });
+}
+
+tpcf_status tpcf_count(tpcf_ctx* ctx, const tpcf_spec* spec, const tpcf_job* job, uint64_t* hist, int64_t hist_len) {
+    if (!ctx || !spec || !job || !hist) return fail(ctx, TPCF_ERR_INVALID, "null argument");
+    int64_t len = 0;
+    if (tpcf_hist_len(spec, &len) != TPCF_OK || len != hist_len) return fail(ctx, TPCF_ERR_INVALID, "hist_len mismatch");
+    uint64_t* hp[1] = {hist};
+    return tpcf_count_batch(ctx, spec, job, 1, hp);
+}
+
+tpcf_status tpcf_submit(tpcf_ctx* ctx, const tpcf_spec* spec, const tpcf_job* job, uint64_t* ticket) {
+    if (!ctx || !spec || !job || !ticket) return fail(ctx, TPCF_ERR_INVALID, "null argument");
+    tpcf_status s = guarded(ctx, [&] {
+        std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+        validate(spec, job);
+        int nc = spec->kind == TPCF_PAIR ? 2 : 3;
+        for (int r = 0; r < nc; r++)
+            if (!ctx->catalogs.count(job->catalog[r])) throw InvalidArg{"unknown catalog handle"};
+    });
+    if (s != TPCF_OK) return s;
+    auto p = std::make_shared<Pending>();
+    p->spec = *spec;
+    p->job = *job;
+    {
+        std::lock_guard<std::mutex> lk(ctx->qmu);
+        p->ticket = ctx->next_ticket++;
+        ctx->queue.push_back(p);
+        ctx->tickets[p->ticket] = p;
+        *ticket = p->ticket;
+    }
+    ctx->qcv.notify_all();
+    return TPCF_OK;
+}
+
+tpcf_status tpcf_wait(tpcf_ctx* ctx, uint64_t ticket, uint64_t* hist, int64_t hist_len, int64_t timeout_ms) {
+    if (!ctx) return TPCF_ERR_INVALID;
+    std::unique_lock<std::mutex> lk(ctx->qmu);
+    auto it = ctx->tickets.find(ticket);
+    if (it == ctx->tickets.end()) return fail(ctx, TPCF_ERR_NOT_FOUND, "unknown ticket");
+    auto p = it->second;
+    auto ready = [&] { return p->status != 1; };
+    if (timeout_ms < 0) ctx->qcv.wait(lk, ready);
+    else if (!ctx->qcv.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready)) return TPCF_ERR_TIMEOUT;
+    ctx->tickets.erase(ticket);
+    if (p->status != TPCF_OK) return p->status;
+    if (hist) {
+        if ((int64_t)p->result.size() != hist_len) return fail(ctx, TPCF_ERR_INVALID, "hist_len mismatch");
+        memcpy(hist, p->result.data(), p->result.size() * sizeof(uint64_t));
+    }
+    return TPCF_OK;
+}
+
+tpcf_status tpcf_cancel(tpcf_ctx* ctx, uint64_t ticket) {
+    if (!ctx) return TPCF_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->qmu);
+    auto it = ctx->tickets.find(ticket);
+    if (it == ctx->tickets.end()) return TPCF_ERR_NOT_FOUND;
+    if (it->second->status != 1) return TPCF_ERR_INVALID;  // already ran
+    it->second->cancelled = true;
+    for (auto q = ctx->queue.begin(); q != ctx->queue.end(); ++q)
+        if ((*q)->ticket == ticket) {
+            (*q)->status = TPCF_ERR_CANCELLED;
+            ctx->queue.erase(q);
+            break;
+        }
+    ctx->qcv.notify_all();
+    return TPCF_OK;
+}
+
+tpcf_status tpcf_last_stats(tpcf_ctx* ctx, tpcf_stats* stats) {
+    if (!ctx || !stats) return TPCF_ERR_INVALID;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    *stats = ctx->stats;
+    // byte counters cover everything copied since the previous stats read
+    stats->h2d_bytes = ctx->h2d;
+    stats->d2h_bytes = ctx->d2h;
+    ctx->h2d = ctx->d2h = 0;
+    return TPCF_OK;
+}
+
+// test hook (not in the public header): checks the device exception table
+// against its own entries; returns the mismatch count or -1.
+int64_t tpcf_debug_acos_selfcheck(tpcf_ctx* ctx, int64_t* table_size) {
+    if (!ctx) return -1;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    int64_t r = -1;
+    guarded(ctx, [&] {
+        CK(cudaSetDevice(ctx->device));
+        ensure_acos(ctx);
+        DevBuf<unsigned int> mm;
+        mm.reserve(1);
+        CK(cudaMemset(mm.p, 0, 4));
+        CK(launch_acos_check(acos_table(ctx), 0, ctx->acos_n, mm.p, ctx->stream));
+        unsigned int h = 0;
+        CK(cudaMemcpyAsync(&h, mm.p, 4, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        r = h;
+        if (table_size) *table_size = ctx->acos_n;
+    });
+    return r;
+}
+
+}  // extern "C"

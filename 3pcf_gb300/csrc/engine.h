@@ -1,0 +1,124 @@
+// engine.h -- internal structures shared by the host engine (engine.cpp) and
+// the CUDA kernels (kernels.cu).  Not part of the public ABI (include/tpcf.h).
+#ifndef TPCF_ENGINE_H
+#define TPCF_ENGINE_H
+
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+namespace tpcf {
+
+// Points per spatial tile.  A triangle task covers one tile of each role.
+constexpr int TILE = 64;
+
+// Per-triangle predicate of a task (how the reference's loop bounds restrict
+// the triples of a tile triple).
+enum Pred : uint32_t {
+    PRED_NONE = 0,   // every triple of the tile triple counts once
+    PRED_DDR = 1,    // weight [key_k >= key_i] + [key_k >= key_j]  (loop ONE, roles A == B)
+    PRED_SAME = 2,   // key_i <= key_j <= key_k                      (loop SAME, generic arrays)
+    PRED_ONE = 3     // key_j <= key_k                               (loop ONE, generic arrays)
+};
+// Task flag bits (task.x bits 24..31)
+constexpr uint32_t TASK_DIAG_IJ = 1u << 24;  // tiles I and J are the same tile of one view: j > i
+constexpr uint32_t TASK_DIAG_JK = 1u << 25;  // tiles J and K are the same tile of one view: k > j
+constexpr uint32_t TASK_SLOT_MASK = 0xFFFFu;
+constexpr int TASK_PRED_SHIFT = 16;          // bits 16..23: Pred
+
+// Encodings of per-side codes in the triangle kernels (values are multiplied
+// by Q*T; invalid codes make every derived index negative or too large).
+constexpr int CODE_ZERO = -(1 << 28);   // side length exactly 0
+constexpr int CODE_BELOW = -(1 << 27);  // 0 < side < s_lo
+constexpr int CODE_ABOVE = (1 << 27);   // side >= s_hi
+
+// Three-side codes: "at or above hist_max" in clean mode.
+constexpr uint32_t CODE3_CLEAN_FAR = 1u << 28;
+
+// A histogram target of one launch.
+struct DevJob {
+    const float4* pts[3];        // spatially sorted points of roles A, B, C; .w = loop index (int bits)
+    const int32_t* tile_start[3];// tile -> first point, ntiles+1 entries
+    unsigned long long* hist;    // global uint64 histogram (hist_len entries)
+    int32_t weight_pred;         // unused by kernels (kept for stats)
+    int32_t pad;
+};
+
+// Launch-wide binning constants for the triangle kernels.
+struct TriParams {
+    int S, Q, T, len;            // len = S*Q*T
+    float s_lo, s_hi, s_bw;      // reference float values
+    float q_lo, q_hi, q_bw;
+    float t_lo, t_hi, t_bw;
+    int nan_zero;
+    // guarded fast path (all in units of bins)
+    float q_scale;               // 1/q_bw
+    float q_off;                 // -q_lo/q_bw - 0.5
+    float q_thr;                 // 0.5 - guard half-width for q
+    float t_coef[6];             // acos(|c|) ~ sqrt(1-|c|) * poly(|c|), scaled by 1/(pi' t_bw)
+    float t_half;                // pi/(2 pi' t_bw)
+    float t_off0;                // t_half - t_lo/t_bw - 0.5
+    float t_thrA;                // 0.5 - fixed guard half-width for theta
+    float t_thrB;                // slope of the c-dependent guard half-width
+    float t2_off;                // (1 - 3 t_lo)/t_bw - 0.5 - 2*(-0.5) handled in code
+    int theta_full;              // theta range covers (0,1): skip range checks
+};
+
+struct ThreeParams {
+    int n;                       // nbins
+    float lo, hi, bw;
+    int clean;
+    int len;                     // n^3
+};
+
+struct PairParams {
+    int n;
+    float lo, hi, bw;
+};
+
+// Exact glibc-acosf exception table on the device.
+struct AcosTable {
+    const uint32_t* keys;        // sorted float bit patterns of c
+    const uint32_t* vals;        // glibc acosf(c) bit patterns
+    const uint32_t* bucket;      // 65537 offsets by key >> 16
+    uint32_t n;
+};
+
+// Guard-band recheck queue (device scratch).
+struct RecheckQueue {
+    uint4* items;                // {slot | weight << 16, ia, ib, ic}
+    unsigned int* count;
+    unsigned int cap;
+};
+
+struct LaunchStats {
+    unsigned int* error_flag;    // set by kernels on an internal invariant failure
+};
+
+// ---- kernel launchers (kernels.cu) ----
+cudaError_t launch_triangle_fast(const DevJob* jobs, const uint4* tasks, unsigned int ntasks,
+                                 unsigned int* task_counter, const TriParams& p, RecheckQueue q,
+                                 int grid, int hist_copies, cudaStream_t st);
+cudaError_t launch_triangle_recheck(const DevJob* jobs, RecheckQueue q, const TriParams& p, AcosTable t,
+                                    int grid, cudaStream_t st);
+cudaError_t launch_triangle_fp64(const DevJob* jobs, const uint4* tasks, unsigned int ntasks,
+                                 unsigned int* task_counter, const TriParams& p, AcosTable t, int grid,
+                                 int hist_copies, cudaStream_t st);
+cudaError_t launch_three_side(const DevJob* jobs, const uint4* tasks, unsigned int ntasks,
+                              unsigned int* task_counter, const ThreeParams& p, int fp64, int grid,
+                              int hist_copies, cudaStream_t st);
+cudaError_t launch_pairs(const DevJob* jobs, const uint4* tasks, unsigned int ntasks,
+                         unsigned int* task_counter, const PairParams& p, int fp64, int grid,
+                         int hist_copies, cudaStream_t st);
+cudaError_t launch_acos_check(AcosTable t, uint32_t key_begin, uint32_t count, unsigned int* mismatches,
+                              cudaStream_t st);
+
+// shared-memory bytes of a launch (for occupancy / admission)
+size_t triangle_smem_bytes(int hist_len, int hist_copies);
+size_t three_side_smem_bytes(int hist_len, int hist_copies);
+size_t pair_smem_bytes(int hist_len, int hist_copies);
+int triangle_block_threads();
+int three_side_block_threads();
+int pair_block_threads();
+
+}  // namespace tpcf
+#endif

@@ -1,0 +1,776 @@
+// kernels.cu -- sm_103a counting kernels.
+//
+// All kernels are persistent: a grid of (SM count x resident CTAs) pulls tile
+// tasks from a device counter.  A task names one spatial tile (<= 64 points)
+// of each role; the CTA stages the tiles' points in shared memory, computes the
+// side lengths of the tile pairs once (exactly as the reference does), and then
+// walks the triangles with one warp per point of role A, a loop over role B
+// and the 32 lanes spanning role C.  Counts go to warp-private shared
+// histograms (32-bit) that are flushed with 64-bit global atomics when the
+// task's histogram changes, after a bounded number of tasks, and at exit.
+//
+// Exactness: side lengths and their bins are computed with IEEE
+// round-to-nearest intrinsics in the reference's operation order, so they equal
+// the reference's floats.  The triangle-parametrization fast path then works
+// with approximate reciprocals/arc cosines and sends every triangle whose q or
+// theta value lies within a bounded guard band of a bin edge to a recheck
+// queue; the recheck kernel recomputes those triangles with the reference's
+// exact arithmetic (including glibc's acosf through an exception table).
+#include <stdint.h>
+#include <limits.h>
+#include <cuda_runtime.h>
+
+#include "engine.h"
+#include "exact_acos.h"
+
+namespace tpcf {
+
+// ---------------------------------------------------------------------------
+// Exact reference arithmetic.  FOps<false>: IEEE float intrinsics (never
+// contracted).  FOps<true>: each float operation computed in FP64 and rounded
+// to float -- identical results for + - * / sqrt (double rounding is innocuous
+// when the wide format has at least 2p+2 bits, Figueroa 1995).
+template <bool FP64>
+struct FOps;
+template <>
+struct FOps<false> {
+    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
+    static __device__ __forceinline__ float sqrt(float a) { return __fsqrt_rn(a); }
+};
+template <>
+struct FOps<true> {
+    static __device__ __forceinline__ float add(float a, float b) { return __double2float_rn(__dadd_rn(a, b)); }
+    static __device__ __forceinline__ float sub(float a, float b) { return __double2float_rn(__dsub_rn(a, b)); }
+    static __device__ __forceinline__ float mul(float a, float b) { return __double2float_rn(__dmul_rn(a, b)); }
+    static __device__ __forceinline__ float div(float a, float b) { return __double2float_rn(__ddiv_rn(a, b)); }
+    static __device__ __forceinline__ float sqrt(float a) { return __double2float_rn(__dsqrt_rn(a)); }
+};
+
+// |p0 - p1| as the reference computes it: sqrt((dx*dx + dy*dy) + dz*dz) in
+// float (src/3pcf_C_version.cc:57-60, src/3pcf_C_version_triangle_parametrization.cc:119-122,
+// src/2pcf_C_version.cc:92-95).  Symmetric in its arguments bit for bit.
+template <bool FP64>
+__device__ __forceinline__ float ref_dist(float4 a, float4 b) {
+    typedef FOps<FP64> F;
+    float dx = F::sub(a.x, b.x), dy = F::sub(a.y, b.y), dz = F::sub(a.z, b.z);
+    float s = F::mul(dx, dx);
+    s = F::add(s, F::mul(dy, dy));
+    s = F::add(s, F::mul(dz, dz));
+    return F::sqrt(s);
+}
+
+// distance_to_bin of the triangle and pair programs
+// (src/3pcf_C_version_triangle_parametrization.cc:84-113, src/2pcf_C_version.cc:57-86).
+template <bool FP64>
+__device__ __forceinline__ int ref_bin_tp(float v, float lo, float hi, int n, int nan_zero) {
+    typedef FOps<FP64> F;
+    float bw = F::div(F::sub(hi, lo), (float)n);
+    if (v < lo) return -999;
+    if (v >= hi) return -999;
+    if (v != v) return nan_zero ? 0 : INT_MIN;  // int(NaN): aarch64 0, x86-64 INT_MIN
+    return __float2int_rz(F::div(F::sub(v, lo), bw));
+}
+
+// glibc acosf reproduced exactly: (float)tpcf_acos_d(c) unless c is listed in
+// the exception table built on the host from the host's own libm.
+__device__ __forceinline__ float acosf_ref(float c, const AcosTable& t) {
+    if (!(c >= -1.0f && c <= 1.0f)) return __int_as_float(0x7fc00000);
+    float r = __double2float_rn(tpcf_acos_d((double)c));
+    uint32_t key = __float_as_uint(c);
+    uint32_t lo = t.bucket[key >> 16], hi = t.bucket[(key >> 16) + 1];
+    while (lo < hi) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (t.keys[mid] < key) lo = mid + 1;
+        else hi = mid;
+    }
+    if (lo < t.n && t.keys[lo] == key) r = __uint_as_float(t.vals[lo]);
+    return r;
+}
+
+// distance() of the triangle program (:116-240) after the side lengths:
+// three histogram indices, or -1 for "not counted" (out of range, zero side, or
+// an index past the array end, which the reference never prints).
+template <bool FP64>
+__device__ void tp_exact(float dist0, float dist1, float dist2, const TriParams& p, const AcosTable& t,
+                         int out[3]) {
+    typedef FOps<FP64> F;
+    float shortest, middle, longest;
+    if (dist0 > dist1) {
+        if (dist0 > dist2) {
+            longest = dist0;
+            if (dist1 > dist2) { middle = dist1; shortest = dist2; }
+            else { middle = dist2; shortest = dist1; }
+        } else {
+            middle = dist0;
+            if (dist1 > dist2) { longest = dist1; shortest = dist2; }
+            else { longest = dist2; shortest = dist1; }
+        }
+    } else {
+        if (dist1 > dist2) {
+            longest = dist1;
+            if (dist0 > dist2) { middle = dist0; shortest = dist2; }
+            else { middle = dist2; shortest = dist0; }
+        } else {
+            middle = dist1; longest = dist2; shortest = dist0;
+        }
+    }
+    float s2 = F::mul(shortest, shortest), m2 = F::mul(middle, middle), l2 = F::mul(longest, longest);
+    bool zero = dist0 == 0.f || dist1 == 0.f || dist2 == 0.f;
+    float th0 = 0.f, th1 = 0.f;
+    for (int k = 0; k < 3; k++) {
+        float s, q;
+        int i2;
+        if (k == 0) {
+            s = shortest;
+            q = F::div(middle, shortest);
+            float c = F::div(F::sub(F::add(s2, m2), l2), F::mul(F::mul(2.f, shortest), middle));
+            th0 = __double2float_rn(__ddiv_rn((double)acosf_ref(c, t), 3.14159));
+            i2 = ref_bin_tp<FP64>(th0, p.t_lo, p.t_hi, p.T, p.nan_zero);
+        } else if (k == 1) {
+            s = middle;
+            q = F::div(longest, middle);
+            float c = F::div(F::sub(F::add(m2, l2), s2), F::mul(F::mul(2.f, middle), longest));
+            th1 = __double2float_rn(__ddiv_rn((double)acosf_ref(c, t), 3.14159));
+            i2 = ref_bin_tp<FP64>(th1, p.t_lo, p.t_hi, p.T, p.nan_zero);
+        } else {
+            s = shortest;
+            q = F::div(longest, shortest);
+            float th2 = __double2float_rn(__dsub_rn(__dsub_rn(1.0, (double)th0), (double)th1));
+            i2 = ref_bin_tp<FP64>(th2, p.t_lo, p.t_hi, p.T, p.nan_zero);
+        }
+        int i0 = ref_bin_tp<FP64>(s, p.s_lo, p.s_hi, p.S, p.nan_zero);
+        int i1 = ref_bin_tp<FP64>(q, p.q_lo, p.q_hi, p.Q, p.nan_zero);
+        int tot = -1;
+        if (!(i0 < 0 || i1 < 0 || i2 < 0) && !zero) {
+            long long idx = (long long)p.Q * p.T * i0 + (long long)p.T * i1 + i2;
+            if (idx < p.len) tot = (int)idx;
+        }
+        out[k] = tot;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Persistent-task plumbing.
+
+constexpr unsigned int FLUSH_EVERY = 256;  // tasks between histogram flushes (u32 safety)
+constexpr uint32_t TASK_NONE = 0xFFFFFFFFu;
+
+__device__ __forceinline__ void flush_hist(unsigned int* H, int copies, int len, unsigned long long* g) {
+    __syncthreads();
+    for (int b = threadIdx.x; b < len; b += blockDim.x) {
+        unsigned long long sum = 0;
+        for (int c = 0; c < copies; c++) {
+            sum += H[c * len + b];
+            H[c * len + b] = 0;
+        }
+        if (sum) atomicAdd(g + b, sum);
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float rsqrt_approx(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// Triangle parametrization, guarded FP32.
+
+constexpr int TRI_WARPS = 8;
+constexpr int TRI_THREADS = TRI_WARPS * 32;
+constexpr size_t TRI_SMEM_FIXED = 3 * TILE * sizeof(float4) + TILE * TILE * sizeof(int2) +
+                                  TRI_WARPS * TILE * sizeof(int2);
+
+// s-bin code of one side, monotone in the side length, multiplied by Q*T.
+template <bool FP64>
+__device__ __forceinline__ int tri_side_code(float d, const TriParams& p) {
+    typedef FOps<FP64> F;
+    if (d == 0.f) return CODE_ZERO;
+    if (d < p.s_lo) return CODE_BELOW;
+    if (d >= p.s_hi) return CODE_ABOVE;
+    return __float2int_rz(F::div(F::sub(d, p.s_lo), p.s_bw)) * (p.Q * p.T);
+}
+
+// 1.5 * 2^23: adding it rounds a float in (-2^22, 2^22) to an integer held in
+// the low mantissa bits.
+#define MAGIC 12582912.0f
+#define MAGIC_BITS 0x4B400000
+
+struct GuardedBin {
+    int bin;      // floor of the bin coordinate (valid if not near an edge)
+    float err;    // signed distance of the coordinate from its bin centre (in [-0.5, 0.5])
+};
+
+// f_m = coordinate - 0.5; returns floor(coordinate) and the offset used by the guard
+__device__ __forceinline__ GuardedBin magic_floor(float f_m) {
+    float tm = __fadd_rn(f_m, MAGIC);
+    float dd = __fsub_rn(tm, MAGIC);
+    GuardedBin g;
+    g.bin = __float_as_int(tm) - MAGIC_BITS;
+    g.err = __fsub_rn(f_m, dd);
+    return g;
+}
+
+// theta coordinate of a cosine (approximate), its guard threshold
+__device__ __forceinline__ void theta_fast(float c, const TriParams& p, float& f_m, float& thr) {
+    float x = fabsf(c);
+    float t = __fsub_rn(1.0f, x);
+    float y = rsqrt_approx(t);
+    float sq = __fmul_rn(t, y);
+    float P = p.t_coef[5];
+    P = __fmaf_rn(P, x, p.t_coef[4]);
+    P = __fmaf_rn(P, x, p.t_coef[3]);
+    P = __fmaf_rn(P, x, p.t_coef[2]);
+    P = __fmaf_rn(P, x, p.t_coef[1]);
+    P = __fmaf_rn(P, x, p.t_coef[0]);
+    float a = __fmaf_rn(sq, P, -p.t_half);                         // K*acos(|c|) - K*pi/2
+    a = __int_as_float(__float_as_int(a) ^ (__float_as_int(c) & 0x80000000));  // acos(-x) = pi - acos(x)
+    f_m = __fadd_rn(a, p.t_off0);
+    thr = __fmaf_rn(-p.t_thrB, y, p.t_thrA);
+}
+
+template <int PRED>
+__device__ __forceinline__ void triangle_one(float a, int ca, float b, int cb, float c, int cc, unsigned w,
+                                             const TriParams& p, unsigned int* Hw, RecheckQueue& q,
+                                             uint32_t slot, uint32_t ia, uint32_t ib, uint32_t ic) {
+    const int SQT = p.len;  // S*Q*T: valid offsets are [0, SQT)
+    float lo_ab = fminf(a, b), hi_ab = fmaxf(a, b);
+    float s = fminf(lo_ab, c);
+    float l = fmaxf(hi_ab, c);
+    float m = fmaxf(lo_ab, fminf(hi_ab, c));
+    int clo = min(ca, cb), chi = max(ca, cb);
+    int off_s = min(clo, cc);
+    int off_m = max(clo, min(chi, cc));
+    bool v02 = (unsigned)off_s < (unsigned)SQT && w;
+    bool v1 = (unsigned)off_m < (unsigned)SQT && off_s != CODE_ZERO && w;
+    if (!__any_sync(0xffffffffu, v02 || v1)) return;
+
+    float s2 = __fmul_rn(s, s), m2 = __fmul_rn(m, m), l2 = __fmul_rn(l, l);
+    float rs = rcp_approx(s), rm = rcp_approx(m);
+    float rsq = __fmul_rn(rs, p.q_scale), rmq = __fmul_rn(rm, p.q_scale);
+    GuardedBin q0 = magic_floor(__fmaf_rn(m, rsq, p.q_off));
+    GuardedBin q1 = magic_floor(__fmaf_rn(l, rmq, p.q_off));
+    GuardedBin q2 = magic_floor(__fmaf_rn(l, rsq, p.q_off));
+
+    float num0 = __fsub_rn(__fadd_rn(s2, m2), l2);
+    float num1 = __fsub_rn(__fadd_rn(m2, l2), s2);
+    float c0 = __fmul_rn(__fmul_rn(num0, rcp_approx(__fmul_rn(s, m))), 0.5f);
+    float c1 = __fmul_rn(__fmul_rn(num1, rcp_approx(__fmul_rn(m, l))), 0.5f);
+    float f0m, thr0, f1m, thr1;
+    theta_fast(c0, p, f0m, thr0);
+    theta_fast(c1, p, f1m, thr1);
+    float f2m = __fsub_rn(__fsub_rn(p.t2_off, f0m), f1m);
+    float thr2 = __fadd_rn(__fadd_rn(thr0, thr1), -0.5f - 1e-6f);
+    GuardedBin t0 = magic_floor(f0m), t1 = magic_floor(f1m), t2 = magic_floor(f2m);
+
+    // guard: any permutation that could count has a value near a bin edge
+    bool gq0 = !(fabsf(q0.err) <= p.q_thr), gq1 = !(fabsf(q1.err) <= p.q_thr), gq2 = !(fabsf(q2.err) <= p.q_thr);
+    bool gt0 = !(fabsf(t0.err) <= thr0), gt1 = !(fabsf(t1.err) <= thr1), gt2 = !(fabsf(t2.err) <= thr2);
+    bool guard = (v02 && (gq0 || gt0 || gq2 || gt2)) || (v1 && (gq1 || gt1));
+
+    bool ok0 = v02 && (unsigned)q0.bin < (unsigned)p.Q && (unsigned)t0.bin < (unsigned)p.T && !guard;
+    bool ok1 = v1 && (unsigned)q1.bin < (unsigned)p.Q && (unsigned)t1.bin < (unsigned)p.T && !guard;
+    bool ok2 = v02 && (unsigned)q2.bin < (unsigned)p.Q && (unsigned)t2.bin < (unsigned)p.T && !guard;
+    if (ok0) atomicAdd(Hw + off_s + q0.bin * p.T + t0.bin, w);
+    if (ok1) atomicAdd(Hw + off_m + q1.bin * p.T + t1.bin, w);
+    if (ok2) atomicAdd(Hw + off_s + q2.bin * p.T + t2.bin, w);
+    if (guard) {
+        unsigned int pos = atomicAdd(q.count, 1u);
+        if (pos < q.cap) q.items[pos] = make_uint4(slot | (w << 16), ia, ib, ic);
+    }
+}
+
+struct TaskGeom {
+    int a0, nA, b0, nB, c0, nC;
+};
+
+__device__ __forceinline__ TaskGeom task_geom(const DevJob& J, uint4 task) {
+    TaskGeom g;
+    g.a0 = J.tile_start[0][task.y];
+    g.nA = J.tile_start[0][task.y + 1] - g.a0;
+    g.b0 = J.tile_start[1][task.z];
+    g.nB = J.tile_start[1][task.z + 1] - g.b0;
+    g.c0 = J.tile_start[2][task.w];
+    g.nC = J.tile_start[2][task.w + 1] - g.c0;
+    return g;
+}
+
+__device__ __forceinline__ void load_points(float4* P, const DevJob& J, const TaskGeom& g) {
+    for (int t = threadIdx.x; t < 3 * TILE; t += blockDim.x) {
+        int role = t / TILE, idx = t % TILE;
+        int n = role == 0 ? g.nA : (role == 1 ? g.nB : g.nC);
+        int base = role == 0 ? g.a0 : (role == 1 ? g.b0 : g.c0);
+        P[t] = idx < n ? J.pts[role][base + idx] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
+__device__ __forceinline__ int pkey(float4 p) { return __float_as_int(p.w); }
+
+template <int PRED>
+__device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams& p, float4* P, int2* JK,
+                                   int2* IJ, unsigned int* Hw, RecheckQueue& q) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const TaskGeom g = task_geom(J, task);
+    const uint32_t slot = task.x & TASK_SLOT_MASK;
+    const bool diag_ij = task.x & TASK_DIAG_IJ, diag_jk = task.x & TASK_DIAG_JK;
+    load_points(P, J, g);
+    __syncthreads();
+    for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
+        int j = e / TILE, k = e % TILE;
+        if (j < g.nB && k < g.nC) {
+            float d = ref_dist<false>(P[TILE + j], P[2 * TILE + k]);
+            JK[e] = make_int2(__float_as_int(d), tri_side_code<false>(d, p));
+        }
+    }
+    __syncthreads();
+    int2* row = IJ + warp * TILE;
+    for (int i = warp; i < g.nA; i += TRI_WARPS) {
+        const float4 pi = P[i];
+        float dik[2];
+        int cik[2];
+#pragma unroll
+        for (int r = 0; r < 2; r++) {
+            int k = lane + 32 * r;
+            float d = k < g.nC ? ref_dist<false>(pi, P[2 * TILE + k]) : 0.f;
+            dik[r] = d;
+            cik[r] = tri_side_code<false>(d, p);
+            int j = k;
+            if (j < g.nB) {
+                float dj = ref_dist<false>(pi, P[TILE + j]);
+                row[j] = make_int2(__float_as_int(dj), tri_side_code<false>(dj, p));
+            }
+        }
+        __syncwarp();
+        const int ki = pkey(pi);
+        for (int j = diag_ij ? i + 1 : 0; j < g.nB; j++) {
+            const int2 ij = row[j];
+            const float4 pj = P[TILE + j];
+            const int kj = pkey(pj);
+            if (PRED == PRED_SAME && !(ki <= kj)) continue;  // uniform over the warp
+#pragma unroll
+            for (int r = 0; r < 2; r++) {
+                const int k = lane + 32 * r;
+                const int kk = k < g.nC ? k : g.nC - 1 < 0 ? 0 : g.nC - 1;
+                const int2 jk = JK[j * TILE + kk];
+                unsigned w = (k < g.nC && (!diag_jk || k > j)) ? 1u : 0u;
+                const int kkey = pkey(P[2 * TILE + kk]);
+                if (PRED == PRED_DDR) w = w ? (unsigned)(kkey >= ki) + (unsigned)(kkey >= kj) : 0u;
+                if (PRED == PRED_SAME || PRED == PRED_ONE) w = (w && kj <= kkey) ? 1u : 0u;
+                triangle_one<PRED>(__int_as_float(ij.x), ij.y, dik[r], cik[r], __int_as_float(jk.x), jk.y, w, p, Hw,
+                                   q, slot, (uint32_t)(g.a0 + i), (uint32_t)(g.b0 + j), (uint32_t)(g.c0 + kk));
+            }
+        }
+        __syncwarp();
+    }
+}
+
+__global__ void __launch_bounds__(TRI_THREADS, 1)
+triangle_fast_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ tasks, unsigned int ntasks,
+                     unsigned int* task_counter, TriParams p, RecheckQueue q, int copies) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    float4* P = reinterpret_cast<float4*>(smem);
+    int2* JK = reinterpret_cast<int2*>(smem + 3 * TILE * sizeof(float4));
+    int2* IJ = JK + TILE * TILE;
+    unsigned int* H = reinterpret_cast<unsigned int*>(IJ + TRI_WARPS * TILE);
+    __shared__ uint4 s_task;
+    for (int b = threadIdx.x; b < copies * p.len; b += blockDim.x) H[b] = 0;
+    unsigned int* Hw = H + ((threadIdx.x >> 5) % copies) * p.len;
+    int cur = -1;
+    unsigned int since = 0;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned int t = atomicAdd(task_counter, 1u);
+            s_task = t < ntasks ? tasks[t] : make_uint4(TASK_NONE, 0, 0, 0);
+        }
+        __syncthreads();
+        const uint4 task = s_task;
+        const int slot = task.x == TASK_NONE ? -1 : (int)(task.x & TASK_SLOT_MASK);
+        if ((slot != cur || since >= FLUSH_EVERY) && cur >= 0) {
+            flush_hist(H, copies, p.len, jobs[cur].hist);
+            since = 0;
+        }
+        cur = slot;
+        if (slot < 0) break;
+        since++;
+        const DevJob& J = jobs[slot];
+        switch ((task.x >> TASK_PRED_SHIFT) & 0xFF) {
+            case PRED_NONE: triangle_task_fast<PRED_NONE>(J, task, p, P, JK, IJ, Hw, q); break;
+            case PRED_DDR: triangle_task_fast<PRED_DDR>(J, task, p, P, JK, IJ, Hw, q); break;
+            case PRED_SAME: triangle_task_fast<PRED_SAME>(J, task, p, P, JK, IJ, Hw, q); break;
+            default: triangle_task_fast<PRED_ONE>(J, task, p, P, JK, IJ, Hw, q); break;
+        }
+    }
+}
+
+// Exact recomputation of queued guard-band triangles.
+__global__ void triangle_recheck_kernel(const DevJob* __restrict__ jobs, RecheckQueue q, TriParams p, AcosTable t) {
+    unsigned int n = *q.count;
+    if (n > q.cap) n = q.cap;
+    for (unsigned int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        uint4 it = q.items[e];
+        const DevJob& J = jobs[it.x & 0xFFFF];
+        unsigned w = it.x >> 16;
+        float4 pa = J.pts[0][it.y], pb = J.pts[1][it.z], pc = J.pts[2][it.w];
+        int out[3];
+        tp_exact<false>(ref_dist<false>(pa, pb), ref_dist<false>(pa, pc), ref_dist<false>(pb, pc), p, t, out);
+        for (int k = 0; k < 3; k++)
+            if (out[k] >= 0) atomicAdd(J.hist + out[k], (unsigned long long)w);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Triangle parametrization, plain FP64: every triangle through the exact
+// reference arithmetic with each float operation done in FP64.
+
+template <int PRED>
+__device__ void triangle_task_fp64(const DevJob& J, uint4 task, const TriParams& p, const AcosTable& t,
+                                   float4* P, int2* JK, int2* IJ, unsigned int* Hw) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const TaskGeom g = task_geom(J, task);
+    const bool diag_ij = task.x & TASK_DIAG_IJ, diag_jk = task.x & TASK_DIAG_JK;
+    load_points(P, J, g);
+    __syncthreads();
+    for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
+        int j = e / TILE, k = e % TILE;
+        if (j < g.nB && k < g.nC) JK[e].x = __float_as_int(ref_dist<true>(P[TILE + j], P[2 * TILE + k]));
+    }
+    __syncthreads();
+    int2* row = IJ + warp * TILE;
+    for (int i = warp; i < g.nA; i += TRI_WARPS) {
+        const float4 pi = P[i];
+        float dik[2];
+#pragma unroll
+        for (int r = 0; r < 2; r++) {
+            int k = lane + 32 * r;
+            dik[r] = k < g.nC ? ref_dist<true>(pi, P[2 * TILE + k]) : 0.f;
+            if (k < g.nB) row[k].x = __float_as_int(ref_dist<true>(pi, P[TILE + k]));
+        }
+        __syncwarp();
+        const int ki = pkey(pi);
+        for (int j = diag_ij ? i + 1 : 0; j < g.nB; j++) {
+            const float dij = __int_as_float(row[j].x);
+            const int kj = pkey(P[TILE + j]);
+            if (PRED == PRED_SAME && !(ki <= kj)) continue;
+#pragma unroll
+            for (int r = 0; r < 2; r++) {
+                const int k = lane + 32 * r;
+                if (k >= g.nC || (diag_jk && k <= j)) continue;
+                unsigned w = 1u;
+                const int kkey = pkey(P[2 * TILE + k]);
+                if (PRED == PRED_DDR) w = (unsigned)(kkey >= ki) + (unsigned)(kkey >= kj);
+                if (PRED == PRED_SAME || PRED == PRED_ONE) w = kj <= kkey ? 1u : 0u;
+                if (!w) continue;
+                int out[3];
+                tp_exact<true>(dij, dik[r], __int_as_float(JK[j * TILE + k].x), p, t, out);
+                for (int b = 0; b < 3; b++)
+                    if (out[b] >= 0) atomicAdd(Hw + out[b], w);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+__global__ void __launch_bounds__(TRI_THREADS, 1)
+triangle_fp64_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ tasks, unsigned int ntasks,
+                     unsigned int* task_counter, TriParams p, AcosTable t, int copies) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    float4* P = reinterpret_cast<float4*>(smem);
+    int2* JK = reinterpret_cast<int2*>(smem + 3 * TILE * sizeof(float4));
+    int2* IJ = JK + TILE * TILE;
+    unsigned int* H = reinterpret_cast<unsigned int*>(IJ + TRI_WARPS * TILE);
+    __shared__ uint4 s_task;
+    for (int b = threadIdx.x; b < copies * p.len; b += blockDim.x) H[b] = 0;
+    unsigned int* Hw = H + ((threadIdx.x >> 5) % copies) * p.len;
+    int cur = -1;
+    unsigned int since = 0;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned int tt = atomicAdd(task_counter, 1u);
+            s_task = tt < ntasks ? tasks[tt] : make_uint4(TASK_NONE, 0, 0, 0);
+        }
+        __syncthreads();
+        const uint4 task = s_task;
+        const int slot = task.x == TASK_NONE ? -1 : (int)(task.x & TASK_SLOT_MASK);
+        if ((slot != cur || since >= FLUSH_EVERY) && cur >= 0) {
+            flush_hist(H, copies, p.len, jobs[cur].hist);
+            since = 0;
+        }
+        cur = slot;
+        if (slot < 0) break;
+        since++;
+        const DevJob& J = jobs[slot];
+        switch ((task.x >> TASK_PRED_SHIFT) & 0xFF) {
+            case PRED_NONE: triangle_task_fp64<PRED_NONE>(J, task, p, t, P, JK, IJ, Hw); break;
+            case PRED_DDR: triangle_task_fp64<PRED_DDR>(J, task, p, t, P, JK, IJ, Hw); break;
+            case PRED_SAME: triangle_task_fp64<PRED_SAME>(J, task, p, t, P, JK, IJ, Hw); break;
+            default: triangle_task_fp64<PRED_ONE>(J, task, p, t, P, JK, IJ, Hw); break;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Three-side histogram (src/3pcf_C_version.cc): every ordered triple, sides in
+// source order d01 -> i0, d02 -> i1, d12 -> i2, index n^2 i2 + n i1 + i0.
+
+constexpr int TS_WARPS = 8;
+constexpr int TS_THREADS = TS_WARPS * 32;
+constexpr size_t TS_SMEM_FIXED = 3 * TILE * sizeof(float4) + TILE * TILE * sizeof(uint32_t) +
+                                 TS_WARPS * TILE * sizeof(uint32_t);
+constexpr uint32_t TS_FAR = 1u << 30;
+
+// distance_to_bin of src/3pcf_C_version.cc:23-51, times 'scale'; sides at or
+// above hist_max give nbins+1 (reference) or, in clean mode, a value that
+// pushes every derived index out of range.
+template <bool FP64>
+__device__ __forceinline__ uint32_t side_code3(float d, const ThreeParams& p, uint32_t scale) {
+    typedef FOps<FP64> F;
+    if (d < p.lo) return 0u;
+    if (d >= p.hi) return p.clean ? TS_FAR : (uint32_t)(p.n + 1) * scale;
+    return (uint32_t)__float2int_rz(F::div(F::sub(d, p.lo), p.bw)) * scale;
+}
+
+template <bool FP64, bool GLOBAL_HIST>
+__device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& p, float4* P, uint32_t* JK,
+                                uint32_t* IJ, unsigned int* Hw) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const TaskGeom g = task_geom(J, task);
+    const uint32_t n = p.n, n2 = (uint32_t)p.n * p.n, len = (uint32_t)p.len;
+    load_points(P, J, g);
+    __syncthreads();
+    for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
+        int j = e / TILE, k = e % TILE;
+        if (j < g.nB && k < g.nC) JK[e] = side_code3<FP64>(ref_dist<FP64>(P[TILE + j], P[2 * TILE + k]), p, n2);
+    }
+    __syncthreads();
+    uint32_t* row = IJ + warp * TILE;
+    for (int i = warp; i < g.nA; i += TS_WARPS) {
+        const float4 pi = P[i];
+        uint32_t cik[2];
+#pragma unroll
+        for (int r = 0; r < 2; r++) {
+            int k = lane + 32 * r;
+            cik[r] = k < g.nC ? side_code3<FP64>(ref_dist<FP64>(pi, P[2 * TILE + k]), p, n) : TS_FAR;
+            if (k < g.nB) row[k] = side_code3<FP64>(ref_dist<FP64>(pi, P[TILE + k]), p, 1u);
+        }
+        __syncwarp();
+        for (int j = 0; j < g.nB; j++) {
+            const uint32_t cij = row[j];
+#pragma unroll
+            for (int r = 0; r < 2; r++) {
+                const int k = lane + 32 * r;
+                const uint32_t idx = JK[j * TILE + (k < g.nC ? k : 0)] + cik[r] + cij;
+                if (idx < len) {
+                    if (GLOBAL_HIST) atomicAdd(J.hist + idx, 1ull);
+                    else atomicAdd(Hw + idx, 1u);
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+template <bool FP64, bool GLOBAL_HIST>
+__global__ void __launch_bounds__(TS_THREADS)
+three_side_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ tasks, unsigned int ntasks,
+                  unsigned int* task_counter, ThreeParams p, int copies) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    float4* P = reinterpret_cast<float4*>(smem);
+    uint32_t* JK = reinterpret_cast<uint32_t*>(smem + 3 * TILE * sizeof(float4));
+    uint32_t* IJ = JK + TILE * TILE;
+    unsigned int* H = IJ + TS_WARPS * TILE;
+    __shared__ uint4 s_task;
+    if (!GLOBAL_HIST)
+        for (int b = threadIdx.x; b < copies * p.len; b += blockDim.x) H[b] = 0;
+    unsigned int* Hw = H + (GLOBAL_HIST ? 0 : ((threadIdx.x >> 5) % copies) * p.len);
+    int cur = -1;
+    unsigned int since = 0;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned int t = atomicAdd(task_counter, 1u);
+            s_task = t < ntasks ? tasks[t] : make_uint4(TASK_NONE, 0, 0, 0);
+        }
+        __syncthreads();
+        const uint4 task = s_task;
+        const int slot = task.x == TASK_NONE ? -1 : (int)(task.x & TASK_SLOT_MASK);
+        if (!GLOBAL_HIST && (slot != cur || since >= 64) && cur >= 0) {
+            flush_hist(H, copies, p.len, jobs[cur].hist);
+            since = 0;
+        }
+        cur = slot;
+        if (slot < 0) break;
+        since++;
+        three_side_task<FP64, GLOBAL_HIST>(jobs[slot], task, p, P, JK, IJ, Hw);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Pair counts (src/2pcf_C_version.cc).  Tasks name a tile of each role (w unused).
+
+constexpr int PR_WARPS = 8;
+constexpr int PR_THREADS = PR_WARPS * 32;
+constexpr size_t PR_SMEM_FIXED = 2 * TILE * sizeof(float4);
+
+template <bool FP64, int PRED>
+__device__ void pair_task(const DevJob& J, uint4 task, const PairParams& p, float4* P, unsigned int* Hw) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int a0 = J.tile_start[0][task.y], nA = J.tile_start[0][task.y + 1] - a0;
+    const int b0 = J.tile_start[1][task.z], nB = J.tile_start[1][task.z + 1] - b0;
+    const bool diag = task.x & TASK_DIAG_IJ;
+    for (int t = threadIdx.x; t < 2 * TILE; t += blockDim.x) {
+        int role = t / TILE, idx = t % TILE;
+        int nn = role == 0 ? nA : nB, base = role == 0 ? a0 : b0;
+        P[t] = idx < nn ? J.pts[role][base + idx] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncthreads();
+    for (int i = warp; i < nA; i += PR_WARPS) {
+        const float4 pi = P[i];
+        const int ki = pkey(pi);
+#pragma unroll
+        for (int r = 0; r < 2; r++) {
+            const int j = lane + 32 * r;
+            if (j >= nB) continue;
+            if (diag && j < i) continue;  // self pairs (j == i) are counted, as the reference's j >= i
+            const float4 pj = P[TILE + j];
+            if (PRED == PRED_SAME && pkey(pj) < ki) continue;
+            const int b = ref_bin_tp<FP64>(ref_dist<FP64>(pi, pj), p.lo, p.hi, p.n, 0);
+            if (b >= 0 && b < p.n) atomicAdd(Hw + b, 1u);
+        }
+    }
+    __syncthreads();
+}
+
+template <bool FP64>
+__global__ void __launch_bounds__(PR_THREADS)
+pair_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ tasks, unsigned int ntasks,
+            unsigned int* task_counter, PairParams p, int copies) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    float4* P = reinterpret_cast<float4*>(smem);
+    unsigned int* H = reinterpret_cast<unsigned int*>(smem + PR_SMEM_FIXED);
+    __shared__ uint4 s_task;
+    for (int b = threadIdx.x; b < copies * p.n; b += blockDim.x) H[b] = 0;
+    unsigned int* Hw = H + ((threadIdx.x >> 5) % copies) * p.n;
+    int cur = -1;
+    unsigned int since = 0;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned int t = atomicAdd(task_counter, 1u);
+            s_task = t < ntasks ? tasks[t] : make_uint4(TASK_NONE, 0, 0, 0);
+        }
+        __syncthreads();
+        const uint4 task = s_task;
+        const int slot = task.x == TASK_NONE ? -1 : (int)(task.x & TASK_SLOT_MASK);
+        if ((slot != cur || since >= 4096) && cur >= 0) {
+            flush_hist(H, copies, p.n, jobs[cur].hist);
+            since = 0;
+        }
+        cur = slot;
+        if (slot < 0) break;
+        since++;
+        if (((task.x >> TASK_PRED_SHIFT) & 0xFF) == PRED_SAME) pair_task<FP64, PRED_SAME>(jobs[slot], task, p, P, Hw);
+        else pair_task<FP64, PRED_NONE>(jobs[slot], task, p, P, Hw);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Self-check of the exception table: counts floats whose table-driven value
+// differs from the table entry (should be 0) -- used by tests.
+__global__ void acos_check_kernel(AcosTable t, uint32_t key_begin, uint32_t count, unsigned int* mismatches) {
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < count; e += gridDim.x * blockDim.x) {
+        uint32_t idx = key_begin + e;
+        if (idx >= t.n) break;
+        float c = __uint_as_float(t.keys[idx]);
+        if (__float_as_uint(acosf_ref(c, t)) != t.vals[idx]) atomicAdd(mismatches, 1u);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+
+size_t triangle_smem_bytes(int hist_len, int copies) { return TRI_SMEM_FIXED + (size_t)hist_len * copies * 4; }
+size_t three_side_smem_bytes(int hist_len, int copies) { return TS_SMEM_FIXED + (size_t)hist_len * copies * 4; }
+size_t pair_smem_bytes(int hist_len, int copies) { return PR_SMEM_FIXED + (size_t)hist_len * copies * 4; }
+int triangle_block_threads() { return TRI_THREADS; }
+int three_side_block_threads() { return TS_THREADS; }
+int pair_block_threads() { return PR_THREADS; }
+
+cudaError_t launch_triangle_fast(const DevJob* jobs, const uint4* tasks, unsigned int ntasks,
+                                 unsigned int* task_counter, const TriParams& p, RecheckQueue q, int grid,
+                                 int copies, cudaStream_t st) {
+    size_t smem = triangle_smem_bytes(p.len, copies);
+    cudaError_t e = cudaFuncSetAttribute(triangle_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    triangle_fast_kernel<<<grid, TRI_THREADS, smem, st>>>(jobs, tasks, ntasks, task_counter, p, q, copies);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_triangle_recheck(const DevJob* jobs, RecheckQueue q, const TriParams& p, AcosTable t, int grid,
+                                    cudaStream_t st) {
+    triangle_recheck_kernel<<<grid, 128, 0, st>>>(jobs, q, p, t);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_triangle_fp64(const DevJob* jobs, const uint4* tasks, unsigned int ntasks,
+                                 unsigned int* task_counter, const TriParams& p, AcosTable t, int grid, int copies,
+                                 cudaStream_t st) {
+    size_t smem = triangle_smem_bytes(p.len, copies);
+    cudaError_t e = cudaFuncSetAttribute(triangle_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    triangle_fp64_kernel<<<grid, TRI_THREADS, smem, st>>>(jobs, tasks, ntasks, task_counter, p, t, copies);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_three_side(const DevJob* jobs, const uint4* tasks, unsigned int ntasks,
+                              unsigned int* task_counter, const ThreeParams& p, int fp64, int grid, int copies,
+                              cudaStream_t st) {
+    const bool global = copies == 0;
+    size_t smem = three_side_smem_bytes(global ? 0 : p.len, global ? 0 : copies);
+    cudaError_t e;
+#define TS_LAUNCH(FP, GL)                                                                                   \
+    e = cudaFuncSetAttribute(three_side_kernel<FP, GL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    if (e != cudaSuccess) return e;                                                                         \
+    three_side_kernel<FP, GL><<<grid, TS_THREADS, smem, st>>>(jobs, tasks, ntasks, task_counter, p, copies > 0 ? copies : 1);
+    if (fp64) {
+        if (global) { TS_LAUNCH(true, true) } else { TS_LAUNCH(true, false) }
+    } else {
+        if (global) { TS_LAUNCH(false, true) } else { TS_LAUNCH(false, false) }
+    }
+#undef TS_LAUNCH
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pairs(const DevJob* jobs, const uint4* tasks, unsigned int ntasks, unsigned int* task_counter,
+                         const PairParams& p, int fp64, int grid, int copies, cudaStream_t st) {
+    size_t smem = pair_smem_bytes(p.n, copies);
+    cudaError_t e;
+    if (fp64) {
+        e = cudaFuncSetAttribute(pair_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        pair_kernel<true><<<grid, PR_THREADS, smem, st>>>(jobs, tasks, ntasks, task_counter, p, copies);
+    } else {
+        e = cudaFuncSetAttribute(pair_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        pair_kernel<false><<<grid, PR_THREADS, smem, st>>>(jobs, tasks, ntasks, task_counter, p, copies);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_acos_check(AcosTable t, uint32_t key_begin, uint32_t count, unsigned int* mismatches,
+                              cudaStream_t st) {
+    acos_check_kernel<<<1024, 256, 0, st>>>(t, key_begin, count, mismatches);
+    return cudaGetLastError();
+}
+
+}  // namespace tpcf

@@ -1,0 +1,433 @@
+#!/usr/bin/env python3
+"""Benchmark of the triplet-counting hot path.
+
+Default workload (one "step"): the full triangle-parametrization DDD, DDR, DRR
+and RRR histograms of a 10,000-point clustered catalog (20 Gaussian blobs,
+sigma 5, centres uniform in a 100^3 cube) against 10,000 uniform randoms in a
+200^3 cube, binned s: 8 bins on [2,10), q: 8 bins on [1,3), theta: 16 bins on
+[0, pi) (theta/3.14159 on [0,1) as the reference computes it), counted in one
+batched launch with bit-exact histograms.  The unit is the triangle as the
+reference's loop nest visits it (its numcalc counter): 1.334e12 per step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Timing: device time of the engine's kernels from CUDA events on the engine's
+stream, summed over K steps after W warm-up steps; L2 is flushed before every
+step (256 MiB write).  e2e repeats the step through the C ABI from host
+buffers: catalog upload, count, histogram download, catalog release.
+Under torchrun every rank counts its own replica of the workload (different
+seeds, no collective on the data path: weak scaling) and the slowest rank's
+time is reported.
+"""
+import argparse
+import json
+import os
+import platform
+import shutil
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "3pcf_gb300")
+ORACLE = os.path.join(ROOT, "oracle")
+for _p in (PKG, ORACLE):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+W_TP = 58  # issue slots per triangle of the triangle-parametrization path (fixed constant)
+SPEC_AXES = [(8, 2.0, 10.0), (8, 1.0, 3.0), (16, 0.0, 1.0)]
+N_D, N_R = 10000, 10000
+METRIC = "triangles/s (bit-exact histos), guarded-FP32 batched vs plain FP64; p50/p99 ms"
+
+
+def workload(rank):
+    import synth
+    d = synth.blobs(N_D, n_blobs=20, sigma=5.0, box=100.0, seed=1 + 1000 * rank)
+    r = synth.uniform(N_R, box=200.0, seed=0 + 1000 * rank)
+    return d, r
+
+
+def loop_units_tp(n):
+    # DDD/RRR: i<=j<=k; DDR/DRR: every i, every j, k>=j
+    same = n * (n + 1) * (n + 2) // 6
+    one = lambda n0, n1, n2: n0 * sum(max(0, n2 - j) for j in range(n1))
+    return same, one
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f), "measured"
+    return {"sm_max_mhz": 2070.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        if shutil.which("nvidia-smi"):
+            q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def init_dist(world, local):
+    if world <= 1:
+        return None
+    import torch
+    import torch.distributed as dist
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    return dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class L2Flush:
+    def __init__(self, device):
+        self.buf = None
+        try:
+            import torch
+            if torch.cuda.is_available():
+                self.buf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda:%d" % device)
+                self.torch = torch
+        except Exception:
+            self.buf = None
+
+    def __call__(self):
+        if self.buf is not None:
+            self.buf.zero_()
+            self.torch.cuda.synchronize()
+
+
+def reference_binary():
+    import ref_build
+    if not ref_build.binary("tp_s8_q8_t16"):
+        try:
+            ref_build.write_configured()
+            ref_build.compile_all()
+        except Exception:
+            pass
+    return ref_build.binary("tp_s8_q8_t16")
+
+
+def run_reference_job(exe, cats, flags, workdir):
+    t0 = time.perf_counter()
+    r = subprocess.run([exe] + cats + flags + ["-o", os.path.join(workdir, "out_%d.dat" % os.getpid())],
+                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True, cwd=workdir)
+    dt = time.perf_counter() - t0
+    n = 0
+    for line in r.stdout.splitlines()[::-1]:
+        if line.startswith("numcalc:"):
+            n = int(line.split()[1])
+            break
+    return n, dt, r.returncode
+
+
+def cpu_baseline_single(d):
+    """The reference program itself, single-threaded as it runs, on a bounded
+    sample: DDD of the first 1000 points of the clustered catalog."""
+    import synth
+    exe = reference_binary()
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "D1000.dat")
+        synth.write_7col_catalog(path, d[:1000])
+        if exe:
+            n, dt, rc = run_reference_job(exe, [path, path, path], [], tmp)
+            if rc == 0 and n > 0:
+                return {"value": n / dt, "unit": "triangles/s", "cores": 1, "kind": "reference",
+                        "sample": "reference TP program (s8 q8 t16 build), DDD on the first 1000 points of the "
+                                  "clustered catalog, %d triangles in %.1f s, 1 process" % (n, dt)}
+    import oracle
+    t0 = time.perf_counter()
+    _, n = oracle.triangle([d[:1000]] * 3, 0, SPEC_AXES, nthreads=1)
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": "triangles/s", "cores": 1, "kind": "port",
+            "sample": "oracle restatement, DDD on the first 1000 points, %d triangles, 1 thread" % n}
+
+
+def impl_reference(args):
+    """The reference's own CPU program on every host core: job-level
+    parallelism with its -X/-x index chunks (one process per core), which is
+    how the reference spreads work (examples/run_CPU_calculation_each_voxels.csh)."""
+    world, rank, local = dist_env()
+    if rank != 0:
+        return 0
+    import synth
+    exe = reference_binary()
+    try:
+        cores = len(os.sched_getaffinity(0))
+    except Exception:
+        cores = os.cpu_count() or 1
+    if not exe:
+        print(json.dumps({"impl": "reference", "unavailable": "reference TP program could not be built here"}))
+        return 0
+    d, r = workload(0)
+    div = 16
+    with tempfile.TemporaryDirectory() as tmp:
+        dp, rp = os.path.join(tmp, "D.dat"), os.path.join(tmp, "R.dat")
+        synth.write_7col_catalog(dp, d)
+        synth.write_7col_catalog(rp, r)
+        combos = [[dp, dp, dp], [dp, dp, rp], [dp, rp, rp], [rp, rp, rp]]
+        step_id = [0]
+
+        def step():
+            jobs = []
+            for p in range(cores):
+                s = step_id[0] * cores + p
+                cats = combos[s % 4]
+                a, b, c = (s // 4) % div, (s // 64) % div, (s // 7) % div
+                jobs.append((cats, ["-X", str(div), "-x", "%03d%03d%03d" % (a, b, c)]))
+            step_id[0] += 1
+            t0 = time.perf_counter()
+            import concurrent.futures
+            with concurrent.futures.ThreadPoolExecutor(max_workers=cores) as ex:
+                res = list(ex.map(lambda j: run_reference_job(exe, j[0], j[1], tmp), jobs))
+            dt = time.perf_counter() - t0
+            return sum(n for n, _, _ in res), dt
+
+        for _ in range(args.warmup):
+            step()
+        tot_n, tot_t, per = 0, 0.0, []
+        for _ in range(args.steps):
+            n, dt = step()
+            tot_n += n
+            tot_t += dt
+            per.append(dt * 1e3)
+    value = tot_n / tot_t
+    sample = ("reference TP program (s8 q8 t16 build), %d concurrent processes per step, each one -X %d index-chunk "
+              "job of the DDD/DDR/DRR/RRR workload (~%.2e triangles per step)" % (cores, div, tot_n / args.steps))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "triangles/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": tot_t * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "triangle parametrization DDD+DDR+DRR+RRR, 10k clustered + 10k uniform, "
+                                   "s8[2,10) q8[1,3) theta16[0,1)", "l2": "inputs resident in host memory"},
+            "p50_ms": statistics.median(per), "p99_ms": float(np.percentile(per, 99)),
+            "cpu_baseline": {"value": value, "unit": "triangles/s", "cores": cores, "kind": "reference",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "triangles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def traffic_per_launch():
+    p = os.path.join(ROOT, "profiles", "triangle_fast_tp10k.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            j = json.load(f)
+        return j.get("dram_bytes_per_launch")
+    return None
+
+
+def impl_ours(args):
+    world, rank, local = dist_env()
+    dist = init_dist(world, local)
+    import tpcf
+    d, r = workload(rank)
+    nan = tpcf.NAN_ZERO if platform.machine() == "aarch64" else tpcf.NAN_INT_MIN
+    eng = tpcf.Engine(local)
+    loops = [tpcf.LOOP_SAME, tpcf.LOOP_ONE, tpcf.LOOP_ONE, tpcf.LOOP_SAME]
+
+    def specs(precision):
+        return [tpcf.make_spec(tpcf.TRIANGLE, lp, SPEC_AXES, precision=precision, nan_policy=nan) for lp in loops]
+
+    hd, hr = eng.catalog(d), eng.catalog(r)
+    jobs = [eng.job([hd, hd, hd]), eng.job([hd, hd, hr]), eng.job([hd, hr, hr]), eng.job([hr, hr, hr])]
+    sp32 = specs(tpcf.GUARDED_FP32)
+    flush = L2Flush(local)
+    for _ in range(args.warmup):
+        eng.count_batch(sp32, jobs)
+    eng.stats()
+    dev_ms, main_ms, wall_ms = [], [], []
+    launches = 0
+    units = evaluated = recheck = 0
+    ref_hists = None
+    with ClockSampler(local) as clocks:
+        barrier(dist)
+        for _ in range(args.steps):
+            flush()
+            t0 = time.perf_counter()
+            hists = eng.count_batch(sp32, jobs)
+            wall_ms.append((time.perf_counter() - t0) * 1e3)
+            st = eng.stats()
+            dev_ms.append(st["kernel_ms"])
+            main_ms.append(st["main_kernel_ms"])
+            launches += st["kernel_launches"]
+            units, evaluated, recheck = st["loop_units"], st["evaluated_units"], st["recheck_units"]
+            if ref_hists is None:
+                ref_hists = hists
+            elif any(not np.array_equal(a, b) for a, b in zip(hists, ref_hists)):
+                raise RuntimeError("histograms differ between steps")
+        barrier(dist)
+    total_s = max_over_ranks(dist, sum(dev_ms) / 1e3)
+    all_units = sum_over_ranks(dist, units * args.steps)
+    value = all_units / total_s
+    ms_per_step = total_s * 1e3 / args.steps
+
+    # e2e through the C ABI from host buffers (upload, count, download, release)
+    e2e_ms = []
+    h2d = d2h = 0
+    barrier(dist)
+    for _ in range(max(3, min(args.steps, 10))):
+        flush()
+        eng.stats()
+        t0 = time.perf_counter()
+        a, b = eng.catalog(d), eng.catalog(r)
+        js = [eng.job([a, a, a]), eng.job([a, a, b]), eng.job([a, b, b]), eng.job([b, b, b])]
+        hs = eng.count_batch(sp32, js)
+        eng.release(a)
+        eng.release(b)
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        st = eng.stats()
+        h2d, d2h = st["h2d_bytes"], st["d2h_bytes"]
+        if any(not np.array_equal(x, y) for x, y in zip(hs, ref_hists)):
+            raise RuntimeError("e2e histograms differ")
+    barrier(dist)
+    e2e_s = max_over_ranks(dist, statistics.mean(e2e_ms) / 1e3)
+    e2e_value = sum_over_ranks(dist, units) / e2e_s
+
+    # plain FP64 kernel on the same jobs (one step; the >=3x comparison)
+    fp64 = None
+    if not args.no_fp64:
+        h64 = eng.count_batch(specs(tpcf.PLAIN_FP64), jobs)
+        st = eng.stats()
+        if any(not np.array_equal(x, y) for x, y in zip(h64, ref_hists)):
+            raise RuntimeError("plain FP64 histograms differ from the guarded FP32 ones")
+        fp64 = {"value": units / (st["kernel_ms"] / 1e3), "unit": "triangles/s", "ms_per_step": st["kernel_ms"],
+                "guarded_over_fp64": (units / (statistics.mean(dev_ms) / 1e3)) / (units / (st["kernel_ms"] / 1e3))}
+
+    if rank != 0:
+        eng.close()
+        return 0
+    peaks, peak_kind = measured_peaks()
+    try:
+        import torch
+        nsm = torch.cuda.get_device_properties(local).multi_processor_count
+    except Exception:
+        nsm = 152
+    peak = nsm * 128 * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
+    achieved = W_TP * evaluated / (statistics.mean(main_ms) / 1e3) / 1e12
+    cpu = None if args.no_cpu_baseline else cpu_baseline_single(d)
+    csum = clocks.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": "triangles/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "triangle parametrization DDD+DDR+DRR+RRR, 10k clustered (20 blobs, sigma 5, 100^3) "
+                               "+ 10k uniform (200^3), s8[2,10) q8[1,3) theta16[0,1), guarded FP32, one batched launch",
+                   "triangles_per_step": units, "evaluated_triangles_per_step": evaluated,
+                   "rechecked_triangles_per_step": recheck, "l2": "flushed before every step (256 MiB write)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "p50_ms": statistics.median(dev_ms), "p99_ms": float(np.percentile(dev_ms, 99)),
+        "wall_ms_per_step": statistics.mean(wall_ms),
+        "gpu_launches": launches,
+        "e2e": {"value": e2e_value, "unit": "triangles/s", "ms_per_step": e2e_s * 1e3, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "plain_fp64": fp64,
+        "roofline": {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "Tinst/s",
+                     "frac": achieved / peak, "traffic": traffic_per_launch(),
+                     "kernel": "triangle_fast_kernel", "per_unit": "%d lane-instructions per evaluated triangle" % W_TP,
+                     "peak_source": "%d SMs x 128 lanes x sm_max_mhz (%s MEASURED_PEAKS)" % (nsm, peak_kind)},
+        "cpu_baseline": cpu,
+        "clocks": csum,
+    }
+    print(json.dumps(line))
+    eng.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return impl_reference(args)
+    return impl_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,191 @@
+/*
+ * tpcf.h -- C ABI of the GB300 triplet/pair counting engine.
+ *
+ * The reference (mattbellis/3pcf) has no library interface: each histogram is a
+ * stand-alone program whose main() reads catalogs, runs a nested loop over point
+ * triples (or pairs) and writes a histogram file.  This ABI exposes exactly that
+ * loop as a call, with the reference's semantics (same loop bounds, same float
+ * arithmetic, same bins, bit-identical integer counts), computed on one GPU.
+ * The command-line shims (tpcf_3side, tpcf_tp, tpcf_2pcf) are thin callers of
+ * this ABI that keep the reference's flags and file formats.
+ *
+ * Conventions
+ *   - plain C types and pointers only; every call returns a tpcf_status
+ *     (0 = success, negative = error) and never throws;
+ *   - histograms returned to the caller are uint64 counts in the reference's
+ *     index layout; the reference's own unsigned-int wrap (triangle and pair
+ *     programs) is applied only by the file writers;
+ *   - a context is bound to one CUDA device and is not thread-safe: use one
+ *     context per host thread (calls on one context are serialised internally);
+ *   - catalogs are uploaded once and stay resident in device memory until
+ *     released or the context is destroyed.
+ */
+#ifndef TPCF_H
+#define TPCF_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TPCF_ABI_VERSION 1
+
+typedef int32_t tpcf_status;
+enum {
+    TPCF_OK = 0,
+    TPCF_ERR_INVALID = -1,        /* bad argument (message in tpcf_last_error) */
+    TPCF_ERR_CUDA = -2,           /* CUDA runtime error */
+    TPCF_ERR_NO_DEVICE = -3,      /* no CUDA device, or extension built without one */
+    TPCF_ERR_OOM = -4,            /* device memory admission failed */
+    TPCF_ERR_TIMEOUT = -5,        /* tpcf_wait timed out; the job keeps running */
+    TPCF_ERR_NOT_FOUND = -6,      /* unknown catalog handle or ticket */
+    TPCF_ERR_CANCELLED = -7,      /* job cancelled before it ran */
+    TPCF_ERR_INTERNAL = -8,       /* invariant violated (device error flag set) */
+    TPCF_ERR_IO = -9              /* file could not be read or written */
+};
+
+/* Which histogram. */
+enum {
+    TPCF_THREE_SIDE = 0, /* src/3pcf_C_version.cc: sides d01,d02,d12 binned unsorted */
+    TPCF_TRIANGLE = 1,   /* src/3pcf_C_version_triangle_parametrization.cc: (s,q,theta) */
+    TPCF_PAIR = 2        /* src/2pcf_C_version.cc: pair separation */
+};
+
+/* Loop nest.  The reference decides it from argv string identity and keeps it
+ * in a bool (src/3pcf_C_version_triangle_parametrization.cc:333-353), so only
+ * two nests exist in the triangle and pair programs. */
+enum {
+    TPCF_LOOP_ALL = 0,  /* every ordered triple: the three-side loop,
+                           src/3pcf_C_version.cc:363-432; pairs: every (i,j) */
+    TPCF_LOOP_SAME = 1, /* j >= i, k >= j (which_three_input_files == 0, :484-509);
+                           pairs: j >= i (src/2pcf_C_version.cc:365-370) */
+    TPCF_LOOP_ONE = 2   /* j from 0, k >= j (which_three_input_files == 1) */
+};
+
+/* Arithmetic of the per-triangle kernel; both give identical histograms. */
+enum {
+    TPCF_GUARDED_FP32 = 0, /* FP32 fast path; values within a bounded guard band of
+                              a bin edge are recomputed exactly */
+    TPCF_PLAIN_FP64 = 1    /* every reference float operation done in FP64 and
+                              rounded to float (exact for + - * / sqrt) */
+};
+
+/* int(NaN) in distance_to_bin (src/3pcf_C_version_triangle_parametrization.cc:99)
+ * is platform-defined in the reference: x86-64 cvttss2si yields INT_MIN (the
+ * permutation is dropped); aarch64 fcvtzs yields 0 (counted in bin 0). */
+enum {
+    TPCF_NAN_INT_MIN = 0,
+    TPCF_NAN_ZERO = 1
+};
+
+/* Three-side handling of sides at or above hist_max. */
+enum {
+    TPCF_OVERFLOW_COMPAT = 0, /* reference: bin nbins+1, index aliases; indices
+                                 past nbins^3 are not counted */
+    TPCF_OVERFLOW_CLEAN = 1   /* skip triples with any side >= hist_max */
+};
+
+typedef struct {
+    float lo;       /* lower edge, as the float the reference converts it to */
+    float hi;       /* upper edge */
+    int32_t nbins;
+} tpcf_axis;
+
+typedef struct {
+    int32_t kind;       /* TPCF_THREE_SIDE / TPCF_TRIANGLE / TPCF_PAIR */
+    int32_t loop;       /* TPCF_LOOP_* */
+    int32_t precision;  /* TPCF_GUARDED_FP32 / TPCF_PLAIN_FP64 */
+    int32_t nan_policy; /* TPCF_NAN_* (triangle only) */
+    int32_t overflow;   /* TPCF_OVERFLOW_* (three-side only) */
+    int32_t prune;      /* 1: skip point tiles that provably cannot contribute
+                           (exact); 0: visit every tile of the loop nest */
+    tpcf_axis axis[3];  /* three-side: axis[0]; triangle: s, q, theta; pair: axis[0] */
+} tpcf_spec;
+
+/* One histogram request: 3 catalog ranges (2 for pairs).  The loop indices of
+ * the reference are positions inside [begin, end) of each range, which is how
+ * the reference's -X/-x index chunks (vox2gal, :52-80) behave. */
+typedef struct {
+    uint64_t catalog[3];
+    int64_t begin[3];
+    int64_t end[3];     /* -1: to the end of the catalog */
+} tpcf_job;
+
+typedef struct {
+    double kernel_ms;            /* device time of the counting kernels */
+    double total_ms;             /* wall time of the last call */
+    uint64_t loop_units;         /* triangles (pairs) the reference's loop visits */
+    uint64_t evaluated_units;    /* triangles (pairs) the kernels evaluated */
+    uint64_t recheck_units;      /* guard-band cases recomputed exactly */
+    uint64_t tasks;              /* tile tasks launched */
+    uint64_t kernel_launches;    /* engine kernels launched by the last call */
+    double main_kernel_ms;       /* device time of the counting kernel alone (no recheck) */
+    uint64_t h2d_bytes;          /* host-to-device bytes copied since the previous tpcf_last_stats */
+    uint64_t d2h_bytes;          /* device-to-host bytes copied since the previous tpcf_last_stats */
+} tpcf_stats;
+
+typedef struct tpcf_ctx tpcf_ctx;
+
+/* ---- context -------------------------------------------------------------- */
+/* New context on a CUDA device.  Fails with TPCF_ERR_NO_DEVICE without a GPU. */
+tpcf_status tpcf_create(tpcf_ctx** ctx, int32_t device);
+tpcf_status tpcf_destroy(tpcf_ctx* ctx);
+const char* tpcf_last_error(tpcf_ctx* ctx);
+const char* tpcf_status_string(tpcf_status s);
+int32_t tpcf_abi_version(void);
+
+/* ---- catalogs --------------------------------------------------------------- */
+/* Upload n points (SoA float arrays) as a resident catalog.  Replaces the
+ * reference's per-program read + malloc of h_x/h_y/h_z
+ * (src/3pcf_C_version.cc:311-332, src/3pcf_C_version_triangle_parametrization.cc:366-439). */
+tpcf_status tpcf_catalog_create(tpcf_ctx* ctx, const float* x, const float* y, const float* z,
+                                int64_t n, uint64_t* handle);
+tpcf_status tpcf_catalog_release(tpcf_ctx* ctx, uint64_t handle);
+/* Device bytes held by catalogs and their cached spatial views. */
+tpcf_status tpcf_resident_bytes(tpcf_ctx* ctx, int64_t* bytes);
+
+/* ---- counting ------------------------------------------------------------- */
+/* Number of histogram entries of a spec: nbins^3, S*Q*T or nbins. */
+tpcf_status tpcf_hist_len(const tpcf_spec* spec, int64_t* len);
+
+/* Synchronous count.  Replaces the hot loops and their distance()/
+ * distance_to_bin() helpers:
+ *   three-side  src/3pcf_C_version.cc:363-432, :54-142, :23-51
+ *   triangle    src/3pcf_C_version_triangle_parametrization.cc:477-533, :116-240, :84-113
+ *   pairs       src/2pcf_C_version.cc:358-387, :89-113, :57-86
+ * hist (host, hist_len entries) receives the counts. */
+tpcf_status tpcf_count(tpcf_ctx* ctx, const tpcf_spec* spec, const tpcf_job* job, uint64_t* hist,
+                       int64_t hist_len);
+
+/* Batched count: n jobs in one persistent launch (e.g. DDD, DDR, DRR and RRR,
+ * or every voxel job of a decomposition).  hists[i] receives job i. */
+tpcf_status tpcf_count_batch(tpcf_ctx* ctx, const tpcf_spec* specs, const tpcf_job* jobs, int32_t n,
+                             uint64_t* const* hists);
+
+/* Asynchronous submit / wait (serving).  Jobs submitted while others run are
+ * admitted into the next launch; tpcf_wait blocks up to timeout_ms (<0: forever). */
+tpcf_status tpcf_submit(tpcf_ctx* ctx, const tpcf_spec* spec, const tpcf_job* job, uint64_t* ticket);
+tpcf_status tpcf_wait(tpcf_ctx* ctx, uint64_t ticket, uint64_t* hist, int64_t hist_len, int64_t timeout_ms);
+tpcf_status tpcf_cancel(tpcf_ctx* ctx, uint64_t ticket);
+
+tpcf_status tpcf_last_stats(tpcf_ctx* ctx, tpcf_stats* stats);
+
+/* Number of reference loop iterations (triangles or pairs) of a job, the
+ * reference's numcalc / fake_tot counter (:520, src/3pcf_C_version.cc:429). */
+tpcf_status tpcf_loop_units(tpcf_ctx* ctx, const tpcf_spec* spec, const tpcf_job* job, uint64_t* units);
+
+/* ---- reference catalog files ---------------------------------------------- */
+/* Read a catalog file exactly as the reference's fscanf loops do.
+ * format 0: header-count "N" then "x y z" lines, divided by scale_factor in
+ *           float (src/3pcf_C_version.cc:311-332);
+ * format 1: seven columns "id ra dec z x y z" until EOF, columns 5-7 kept,
+ *           at most 1e6 rows (src/3pcf_C_version_triangle_parametrization.cc:364-394).
+ * Call with x == NULL to get the count in *n; then with arrays of *n floats. */
+tpcf_status tpcf_read_catalog(const char* path, int32_t format, float scale_factor, float* x, float* y,
+                              float* z, int64_t* n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TPCF_H */

@@ -19,7 +19,7 @@ class _Cat(ctypes.Structure):
 def lib():
     global _LIB
     if _LIB is None:
-        import build
+        import oracle_build as build
         path = build.build_oracle()
         L = ctypes.CDLL(path)
         L.oracle_three_side.restype = ctypes.c_ulonglong

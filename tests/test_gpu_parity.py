@@ -1,0 +1,285 @@
+"""GPU parity: the CUDA engine, called through the C ABI, against the
+reference's own outputs (golden files and compiled-reference fixtures) and the
+oracle restatement.  Integer histograms must be identical (tolerance 0)."""
+import os
+import platform
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+import refformat as rf
+import synth
+import tpcf
+
+pytestmark = pytest.mark.gpu
+
+SANDBOX = os.path.join(rf.GOLDEN, "sandbox")
+SANDBOX_SPEC = ((50, 2.0, 12.0), (16, 0.9, 4.1), (25, 0.0, 1.0))
+WIDE_SPEC = ((60, 0.0, 120.0), (16, 0.9, 4.1), (25, 0.0, 1.0))
+NATIVE_NAN = tpcf.NAN_ZERO if platform.machine() == "aarch64" else tpcf.NAN_INT_MIN
+
+
+@pytest.fixture(scope="module")
+def eng():
+    e = tpcf.Engine(0)
+    yield e
+    e.close()
+
+
+def _tp_spec(spec, loop, precision=tpcf.GUARDED_FP32, nan=tpcf.NAN_INT_MIN, prune=True):
+    return tpcf.make_spec(tpcf.TRIANGLE, loop, spec, precision=precision, nan_policy=nan, prune=prune)
+
+
+def _loop_of(which):
+    return tpcf.LOOP_ONE if which else tpcf.LOOP_SAME
+
+
+CASES = rf.ref_cases()["cases"]
+
+
+def _case_inputs(eng, name):
+    case = CASES[name]
+    program, spec = rf.ref_binning(case["variant"])
+    flags = case["flags"]
+    if "-m" in flags or "-s" in flags:
+        cats = [oracle.read_header(os.path.join(rf.GOLDEN, "ref", c + ".dat"), rf.flags_scale(flags))
+                for c in case["catalogs"]]
+    else:
+        cats = [rf.load_catalog(c) for c in case["catalogs"]]
+    ngal = [len(c) for c in cats]
+    # one engine catalog per distinct argv string, as the reference CLI sees them
+    handles = {}
+    for cname, c in zip(case["catalogs"], cats):
+        if cname not in handles:
+            handles[cname] = eng.catalog(c)
+    hs = [handles[c] for c in case["catalogs"]]
+    ranges = None
+    if "-X" in flags:
+        div = int(flags[flags.index("-X") + 1])
+        idx = rf.voxel_indices(int(flags[flags.index("-x") + 1]), len(cats))
+        ranges = [rf.vox2gal(div, idx[a], len(c)) for a, c in enumerate(cats)]
+    return case, program, spec, cats, ngal, hs, ranges
+
+
+@pytest.mark.parametrize("precision", [tpcf.GUARDED_FP32, tpcf.PLAIN_FP64])
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_engine_matches_compiled_reference(eng, name, precision):
+    case, program, spec, cats, ngal, hs, ranges = _case_inputs(eng, name)
+    which = rf.which_mode(case["catalogs"])
+    want = rf.read_bytes(os.path.join(rf.GOLDEN, "ref", name + ".dat.gz"))
+    job = eng.job(hs, ranges)
+    if program == "3side":
+        n, lo, hi = spec
+        s = tpcf.make_spec(tpcf.THREE_SIDE, tpcf.LOOP_ALL, [spec], precision=precision)
+        got = rf.format_three_side(eng.count(s, job), n)
+    elif program == "tp":
+        got = rf.format_triangle(eng.count(_tp_spec(spec, _loop_of(which), precision), job), ngal, spec)
+    else:
+        n, lo, hi = spec
+        s = tpcf.make_spec(tpcf.PAIR, _loop_of(which), [spec], precision=precision)
+        got = rf.format_pair(eng.count(s, job), ngal, n, lo, hi)
+    for h in set(hs):
+        eng.release(h)
+    assert got == want
+
+
+def _sandbox_cat(tmp_path, name):
+    return tpcf.read_catalog(rf.gunzip_to(os.path.join(SANDBOX, name + ".gz"), str(tmp_path / name)), 1)
+
+
+@pytest.mark.parametrize("vox", ["000000000", "000000001", "000001000", "000001001",
+                                 "001000000", "001000001", "001001000", "001001001"])
+def test_sandbox_voxel2(eng, tmp_path, vox):
+    cat = _sandbox_cat(tmp_path, "MICE_5degx5deg_1k_randomized.dat")
+    h = eng.catalog(cat)
+    idx = rf.voxel_indices(int(vox), 3)
+    ranges = [rf.vox2gal(2, idx[a], len(cat)) for a in range(3)]
+    got = eng.count(_tp_spec(SANDBOX_SPEC, tpcf.LOOP_SAME), eng.job([h, h, h], ranges))
+    eng.release(h)
+    want = rf.read_bytes(os.path.join(SANDBOX, "DDD_voxel2_%s_evenbinning_CPU_5degx5deg_LRG_binning_1k.dat.gz" % vox))
+    assert rf.format_triangle(got, [len(cat)] * 3, SANDBOX_SPEC) == want
+
+
+SETS = {
+    "lrg": ("MICE_LRGs_10degx10deg.dat", "flat_MICE_LRGs_10degx10deg.dat",
+            "%s_Debbie_LRG_CPU_10degx10deg_LRG_binning_SLAC_1k.dat", SANDBOX_SPEC),
+    "5deg10k": ("MICE_5degx5deg_10k_randomized.dat", "flat_MICE_5degx5deg_10k.dat",
+                "%s_evenbinning_CPU_5degx5deg_LRG_binning_10k.dat", SANDBOX_SPEC),
+    "20deg10k": ("MICE_20degx20deg_10k_randomized.dat", "flat_MICE_20degx20deg_10k.dat",
+                 "%s_evenbinning_CPU_20degx20deg_10k.dat", WIDE_SPEC),
+}
+
+
+@pytest.mark.parametrize("setname", sorted(SETS))
+def test_sandbox_full_sets(eng, tmp_path, setname):
+    """Full DDD/DDR/DRR/RRR golden sets of the reference (up to 1.6e12
+    triangles each); compared token by token (some goldens carry an extra
+    trailing newline written by the reference's voxel-summing script)."""
+    dname, rname, pattern, spec = SETS[setname]
+    d, r = _sandbox_cat(tmp_path, dname), _sandbox_cat(tmp_path, rname)
+    hd, hr = eng.catalog(d), eng.catalog(r)
+    combos = {"DDD": ([hd, hd, hd], tpcf.LOOP_SAME, [d, d, d]), "DDR": ([hd, hd, hr], tpcf.LOOP_ONE, [d, d, r]),
+              "DRR": ([hd, hr, hr], tpcf.LOOP_ONE, [d, r, r]), "RRR": ([hr, hr, hr], tpcf.LOOP_SAME, [r, r, r])}
+    names = sorted(combos)
+    hists = eng.count_batch([_tp_spec(spec, combos[k][1]) for k in names], [eng.job(combos[k][0]) for k in names])
+    bad = []
+    for k, h in zip(names, hists):
+        got = rf.format_triangle(h, [len(c) for c in combos[k][2]], spec)
+        want = rf.read_bytes(os.path.join(SANDBOX, (pattern % k) + ".gz"))
+        if got.split() != want.split():
+            bad.append(k)
+    eng.release(hd)
+    eng.release(hr)
+    assert not bad, "histograms differ from the reference goldens: %s" % bad
+
+
+def _random_case(seed, n_d=220, n_r=200):
+    d = synth.blobs(n_d, n_blobs=3, sigma=4.0, box=40.0, seed=seed)
+    r = synth.uniform(n_r, box=28.0, seed=seed + 1)
+    return d, r
+
+
+@pytest.mark.parametrize("seed", [101, 202])
+@pytest.mark.parametrize("spec", [((8, 2.0, 10.0), (8, 1.0, 3.0), (16, 0.0, 1.0)),
+                                  ((50, 2.0, 12.0), (16, 0.9, 4.1), (32, 0.0, 1.0)),
+                                  ((6, 0.0, 15.0), (5, 1.0, 2.5), (7, 0.1, 0.9))])
+def test_triangle_vs_oracle_native_nan(eng, seed, spec):
+    """All four loop nests plus the generic three-array nest, with the NaN
+    convention of the machine the oracle runs on."""
+    d, r = _random_case(seed)
+    x = synth.blobs(150, n_blobs=2, sigma=3.0, box=25.0, seed=seed + 2)
+    hd, hr, hx = eng.catalog(d), eng.catalog(r), eng.catalog(x)
+    combos = [([hd, hd, hd], [d, d, d], 0), ([hd, hd, hr], [d, d, r], 1), ([hd, hr, hr], [d, r, r], 1),
+              ([hr, hr, hr], [r, r, r], 0), ([hd, hr, hx], [d, r, x], 0), ([hd, hr, hd], [d, r, d], 0),
+              ([hr, hd, hx], [r, d, x], 1)]
+    specs = [_tp_spec(spec, _loop_of(w), nan=NATIVE_NAN) for _, _, w in combos]
+    hists = eng.count_batch(specs, [eng.job(h) for h, _, _ in combos])
+    for (h, cats, w), got in zip(combos, hists):
+        want, _ = oracle.triangle(cats, w, spec, nan_zero=NATIVE_NAN == tpcf.NAN_ZERO)
+        assert np.array_equal(got, want), (w, int((got != want).sum()))
+    for h in (hd, hr, hx):
+        eng.release(h)
+
+
+def test_lattice_nan_policies(eng):
+    """Degenerate lattice triangles produce rounded cosines beyond +-1; both
+    int(NaN) conventions must match the oracle."""
+    cat = rf.load_catalog("c_lattice")
+    h = eng.catalog(cat)
+    spec = ((8, 2.0, 10.0), (8, 1.0, 3.0), (16, 0.0, 1.0))
+    for nan in (tpcf.NAN_INT_MIN, tpcf.NAN_ZERO):
+        for prec in (tpcf.GUARDED_FP32, tpcf.PLAIN_FP64):
+            got = eng.count(_tp_spec(spec, tpcf.LOOP_SAME, prec, nan), eng.job([h, h, h]))
+            want, _ = oracle.triangle([cat] * 3, 0, spec, nan_zero=nan == tpcf.NAN_ZERO)
+            assert np.array_equal(got, want), (nan, prec)
+    eng.release(h)
+
+
+def test_prune_is_exact(eng):
+    d, r = _random_case(7, 600, 500)
+    hd, hr = eng.catalog(d), eng.catalog(r)
+    spec = ((8, 2.0, 10.0), (8, 1.0, 3.0), (16, 0.0, 1.0))
+    for hs, loop in (([hd, hd, hd], tpcf.LOOP_SAME), ([hd, hd, hr], tpcf.LOOP_ONE), ([hd, hr, hr], tpcf.LOOP_ONE)):
+        a = eng.count(_tp_spec(spec, loop, prune=True), eng.job(hs))
+        st_a = eng.stats()
+        b = eng.count(_tp_spec(spec, loop, prune=False), eng.job(hs))
+        st_b = eng.stats()
+        assert np.array_equal(a, b)
+        assert st_a["loop_units"] == st_b["loop_units"]
+        assert st_a["evaluated_units"] <= st_b["evaluated_units"]
+    eng.release(hd)
+    eng.release(hr)
+
+
+@pytest.mark.parametrize("overflow", [tpcf.OVERFLOW_COMPAT, tpcf.OVERFLOW_CLEAN])
+@pytest.mark.parametrize("axis", [(16, 0.0, 40.0), (32, 0.0, 32.0), (8, 5.0, 25.0)])
+def test_three_side_vs_oracle(eng, overflow, axis):
+    d = synth.blobs(140, n_blobs=4, sigma=5.0, box=60.0, seed=31)
+    r = synth.lattice_mix(120, box=40.0, frac=0.5, seed=32)
+    hd, hr = eng.catalog(d), eng.catalog(r)
+    for hs, cats in (([hd, hd, hd], [d, d, d]), ([hd, hr, hr], [d, r, r]), ([hr, hd, hr], [r, d, r])):
+        for prec in (tpcf.GUARDED_FP32, tpcf.PLAIN_FP64):
+            s = tpcf.make_spec(tpcf.THREE_SIDE, tpcf.LOOP_ALL, [axis], precision=prec, overflow=overflow)
+            got = eng.count(s, eng.job(hs))
+            want, n = oracle.three_side(cats, axis[1], axis[2], axis[0], clean=overflow == tpcf.OVERFLOW_CLEAN)
+            assert np.array_equal(got, want)
+            assert eng.stats()["loop_units"] == n
+    eng.release(hd)
+    eng.release(hr)
+
+
+@pytest.mark.parametrize("axis", [(700, 0.0, 70.0), (40, 1.0, 21.0)])
+def test_pairs_vs_oracle(eng, axis):
+    d = synth.blobs(3000, n_blobs=10, sigma=5.0, box=100.0, seed=41)
+    r = synth.uniform(2500, box=100.0, seed=42)
+    hd, hr = eng.catalog(d), eng.catalog(r)
+    for hs, cats, w in (([hd, hd], [d, d], 0), ([hd, hr], [d, r], 1), ([hr, hr], [r, r], 0)):
+        s = tpcf.make_spec(tpcf.PAIR, _loop_of(w), [axis])
+        got = eng.count(s, eng.job(hs))
+        want, n = oracle.pair(cats, w, axis[1], axis[2], axis[0])
+        assert np.array_equal(got, want)
+        assert eng.stats()["loop_units"] == n
+    # index chunks of one catalog: the reference's j >= i on chunk-local indices
+    got = eng.count(tpcf.make_spec(tpcf.PAIR, tpcf.LOOP_SAME, [axis]), eng.job([hd, hd], [(1500, 3000), (0, 1500)]))
+    want, _ = oracle.pair([d[1500:3000], d[0:1500]], 0, axis[1], axis[2], axis[0])
+    assert np.array_equal(got, want)
+    eng.release(hd)
+    eng.release(hr)
+
+
+def test_empty_and_tiny_catalogs(eng):
+    spec = ((8, 2.0, 10.0), (8, 1.0, 3.0), (16, 0.0, 1.0))
+    one = np.array([[1.0, 2.0, 3.0]], dtype=np.float32)
+    two = np.array([[1.0, 2.0, 3.0], [4.0, 2.0, 3.0]], dtype=np.float32)
+    h0 = eng.catalog(np.zeros((0, 3), dtype=np.float32))
+    h1, h2 = eng.catalog(one), eng.catalog(two)
+    for hs in ([h0, h0, h0], [h1, h1, h1], [h2, h2, h2], [h2, h2, h0], [h2, h0, h0]):
+        got = eng.count(_tp_spec(spec, tpcf.LOOP_SAME), eng.job(hs))
+        assert got.sum() == 0
+    for h in (h0, h1, h2):
+        eng.release(h)
+
+
+def test_duplicate_points_zero_sides(eng):
+    """Coincident points give zero sides: the reference drops all three
+    permutations even when the low s edge is 0."""
+    base = synth.blobs(80, n_blobs=1, sigma=3.0, box=10.0, seed=51)
+    cat = np.concatenate([base, base[:30], base[:10]])
+    h = eng.catalog(cat)
+    for spec in (((6, 0.0, 15.0), (5, 1.0, 2.5), (7, 0.1, 0.9)), ((8, 2.0, 10.0), (8, 1.0, 3.0), (16, 0.0, 1.0))):
+        for loop, w in ((tpcf.LOOP_SAME, 0), (tpcf.LOOP_ONE, 1)):
+            got = eng.count(_tp_spec(spec, loop), eng.job([h, h, h]))
+            want, _ = oracle.triangle([cat] * 3, w, spec)
+            assert np.array_equal(got, want)
+    eng.release(h)
+
+
+@pytest.mark.parametrize("name", ["tp_s8_q8_t16_DDR", "tp_s8_q8_t16_vox3_DDD", "tp_default_DRR",
+                                  "3side_n16_0_40_DDR", "2pcf_default_DD", "2pcf_default_vox2"])
+def test_cli_byte_exact(tmp_path, name):
+    case = CASES[name]
+    var = case["variant"]
+    prog = {"3side": "tpcf_3side", "tp": "tpcf_tp", "2pcf": "tpcf_2pcf"}[rf.ref_binning(var)[0]]
+    program, spec = rf.ref_binning(var)
+    extra = []
+    if program == "tp":
+        extra = ["--s-axis", "%d,%r,%r" % spec[0], "--q-axis", "%d,%r,%r" % spec[1],
+                 "--theta-axis", "%d,%r,%r" % spec[2], "--nan-policy", "int_min"]
+    elif program == "3side":
+        extra = ["--nbins", str(spec[0]), "--hist-min", repr(spec[1]), "--hist-max", repr(spec[2])]
+    else:
+        extra = ["--pair-axis", "%d,%r,%r" % spec]
+    cats = [os.path.join(rf.GOLDEN, "ref", c + ".dat") for c in case["catalogs"]]
+    out = tmp_path / "out.dat"
+    r = subprocess.run([os.path.join(tpcf.BIN_DIR, prog)] + cats + case["flags"] + extra + ["-o", str(out), "--quiet"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert out.read_bytes() == rf.read_bytes(os.path.join(rf.GOLDEN, "ref", name + ".dat.gz"))
+
+
+def test_acos_exception_table(eng):
+    mism, n = eng.acos_selfcheck()
+    assert mism == 0
+    assert 1_000_000 < n < 20_000_000
