@@ -152,6 +152,16 @@ double box_lower_bound(const Box& a, const Box& b) {
     return sqrt(s) * (1.0 - 1e-5);
 }
 
+// Upper bound on the reference's float side length between box a and box b.
+double box_upper_bound(const Box& a, const Box& b) {
+    double s = 0;
+    for (int k = 0; k < 3; k++) {
+        double g = std::max((double)a.hi[k] - (double)b.lo[k], (double)b.hi[k] - (double)a.lo[k]);
+        s += g * g;
+    }
+    return sqrt(s) * (1.0 + 1e-5) + 1e-30;
+}
+
 // ---------------------------------------------------------------------------
 // exact glibc acosf exception table
 
@@ -298,6 +308,8 @@ struct Binning {
     PairParams pair{};
     int len = 0;
     double lmax = INFINITY;   // no counted triangle/pair has a side >= lmax
+    bool tri_prune = false;   // triangle: test the s and q ranges on tile-triple side bounds
+    double s_lo = 0, s_hi = 0, q_hi = 0;
     double lmin_pair = 0;     // pairs: no counted pair has d < lmin_pair
 };
 
@@ -333,7 +345,7 @@ Binning make_binning(const tpcf_spec& sp) {
         p.S = sp.axis[0].nbins;
         p.Q = sp.axis[1].nbins;
         p.T = sp.axis[2].nbins;
-        if ((int64_t)p.S * p.Q * p.T > (1 << 26)) throw InvalidArg{"triangle binning too large"};
+        if ((int64_t)p.S * p.Q * p.T > MAX_TRI_BINS) throw InvalidArg{"triangle binning too large"};
         p.len = p.S * p.Q * p.T;
         p.s_lo = sp.axis[0].lo;
         p.s_hi = sp.axis[0].hi;
@@ -373,6 +385,10 @@ Binning make_binning(const tpcf_spec& sp) {
         // every counted permutation needs shortest or middle side < s_hi and a
         // ratio < q_hi; all sides are then below s_hi (1 + q_hi)
         if (p.s_hi > 0 && p.q_hi > 0) b.lmax = (double)p.s_hi * (1.0 + (double)p.q_hi) * (1 + 1e-5) + 1e-6;
+        b.tri_prune = true;
+        b.s_lo = p.s_lo;
+        b.s_hi = p.s_hi;
+        b.q_hi = (double)p.q_hi * (1 + 1e-5);
     } else if (sp.kind == TPCF_PAIR) {
         check_axis(sp.axis[0], "pair axis");
         PairParams& p = b.pair;
@@ -385,7 +401,13 @@ Binning make_binning(const tpcf_spec& sp) {
     } else {
         throw InvalidArg{"unknown kind"};
     }
-    if (!sp.prune) b.lmax = INFINITY;
+    if (!sp.prune) {
+        b.lmax = INFINITY;
+        b.tri_prune = false;
+    }
+    // device copy of the bound, rounded up so that a float side >= it is >= lmax
+    if (sp.kind == TPCF_TRIANGLE)
+        b.tri.lmax = b.lmax < 3e38 ? nextafterf((float)b.lmax, INFINITY) : INFINITY;
     return b;
 }
 
@@ -602,11 +624,28 @@ uint64_t task_units3(const View& A, int a, const View& B, int b, const View& C, 
 }
 
 // Tile tasks of one triangle/three-side job.
-void plan_triplets(const tpcf_spec& sp, const PlannedJob& pj, uint32_t slot, double lmax,
+// Whether a tile triple can hold a counted triangle-parametrization triangle:
+// with the three pair bounds sorted (L1<=L2<=L3 lower, U1<=U2<=U3 upper) the
+// shortest side lies in [L1,U1], the middle in [L2,U2], the longest in [L3,U3];
+// permutations 0/2 need s_lo <= shortest < s_hi and middle < q_hi*shortest,
+// permutation 1 needs s_lo <= middle < s_hi and longest < q_hi*middle.
+bool tri_triple_possible(const Binning& bin, const Box& a, const Box& b, const Box& c) {
+    double L[3] = {box_lower_bound(a, b), box_lower_bound(a, c), box_lower_bound(b, c)};
+    double U[3] = {box_upper_bound(a, b), box_upper_bound(a, c), box_upper_bound(b, c)};
+    std::sort(L, L + 3);
+    std::sort(U, U + 3);
+    bool p0 = L[0] < bin.s_hi && U[0] >= bin.s_lo && L[1] < bin.q_hi * U[0];
+    bool p1 = L[1] < bin.s_hi && U[1] >= bin.s_lo && L[2] < bin.q_hi * U[1];
+    return p0 || p1;
+}
+
+void plan_triplets(const tpcf_spec& sp, const PlannedJob& pj, uint32_t slot, const Binning& bin,
                    std::vector<std::pair<uint64_t, uint4>>& tasks, uint64_t& evaluated) {
+    const double lmax = bin.lmax;
     const View &A = *pj.v[0], &B = *pj.v[1], &C = *pj.v[2];
     const bool sameAB = pj.v[0] == pj.v[1], sameBC = pj.v[1] == pj.v[2];
     auto add = [&](int a, int b, int c, uint32_t pred, uint32_t flags) {
+        if (bin.tri_prune && !tri_triple_possible(bin, A.boxes[a], B.boxes[b], C.boxes[c])) return;
         uint64_t u = task_units3(A, a, B, b, C, c, flags);
         if (u == 0) return;
         evaluated += u;
@@ -721,15 +760,16 @@ void run_group(tpcf_ctx* ctx, const std::vector<GroupJob>& group) {
             n[r] = pj[g].v[r]->n;
         }
         if (ncat == 2) pj[g].v[2] = pj[g].v[1];
-        pj[g].loop_units = loop_units(sp.kind, sp.loop, n);
+        const tpcf_spec& jsp = *group[g].spec;  // same binning as sp; the loop nest may differ
+        pj[g].loop_units = loop_units(jsp.kind, jsp.loop, n);
         units += pj[g].loop_units;
         for (int r = 0; r < 3; r++) {
             dj[g].pts[r] = pj[g].v[r]->pts.p;
             dj[g].tile_start[r] = pj[g].v[r]->tile_start.p;
         }
         dj[g].hist = ctx->d_hist.p + (size_t)bin.len * g;
-        if (sp.kind == TPCF_PAIR) plan_pairs(sp, pj[g], (uint32_t)g, bin.lmax, tasks, evaluated);
-        else plan_triplets(sp, pj[g], (uint32_t)g, bin.lmax, tasks, evaluated);
+        if (jsp.kind == TPCF_PAIR) plan_pairs(jsp, pj[g], (uint32_t)g, bin.lmax, tasks, evaluated);
+        else plan_triplets(jsp, pj[g], (uint32_t)g, bin, tasks, evaluated);
     }
     // largest tasks first (dynamic fetch then balances the tail)
     std::stable_sort(tasks.begin(), tasks.end(),
@@ -748,6 +788,7 @@ void run_group(tpcf_ctx* ctx, const std::vector<GroupJob>& group) {
     if (sp.kind == TPCF_TRIANGLE) ensure_acos(ctx);
     uint64_t launches = 0;
     unsigned int queue_cap = (unsigned int)std::max<size_t>(ctx->d_queue.n, (size_t)1 << 22);
+    uint64_t dev_evaluated = 0;
     for (int attempt = 0; attempt < 3; attempt++) {
         CK(cudaMemsetAsync(ctx->d_hist.p, 0, hist_total * sizeof(unsigned long long), st));
         CK(cudaMemsetAsync(ctx->d_counters.p, 0, 4 * sizeof(unsigned int), st));
@@ -772,6 +813,7 @@ void run_group(tpcf_ctx* ctx, const std::vector<GroupJob>& group) {
                 q.items = ctx->d_queue.p;
                 q.count = ctx->d_counters.p + 1;
                 q.cap = queue_cap;
+                q.evaluated = reinterpret_cast<unsigned long long*>(ctx->d_counters.p + 2);
                 CK(launch_triangle_fast(ctx->d_jobs.p, ctx->d_tasks.p, nt, ctx->d_counters.p, bin.tri, q, grid, copies, st));
                 CK(cudaEventRecord(ctx->ev_mid, st));
                 CK(launch_triangle_recheck(ctx->d_jobs.p, q, bin.tri, acos_table(ctx), ctx->num_sms * 8, st));
@@ -805,6 +847,7 @@ void run_group(tpcf_ctx* ctx, const std::vector<GroupJob>& group) {
         CK(cudaStreamSynchronize(st));
         ctx->d2h += sizeof(counters) + hist_total * sizeof(unsigned long long);
         ctx->stats.recheck_units = counters[1];
+        memcpy(&dev_evaluated, &counters[2], sizeof(dev_evaluated));
         if (sp.kind == TPCF_TRIANGLE && !fp64 && counters[1] > queue_cap) {
             // the recheck queue overflowed: grow it and count again
             queue_cap = (unsigned int)std::min<uint64_t>((uint64_t)counters[1] + (counters[1] >> 2) + 1024, 0xF0000000ull);
@@ -820,7 +863,10 @@ void run_group(tpcf_ctx* ctx, const std::vector<GroupJob>& group) {
         memcpy(group[g].out, ctx->h_hist.data() + (size_t)bin.len * g, (size_t)bin.len * sizeof(uint64_t));
     ctx->stats.kernel_ms = ms;
     ctx->stats.loop_units = units;
-    ctx->stats.evaluated_units = evaluated;
+    // the fast triangle kernel skips (i,j) pairs that no counted triangle can
+    // contain and counts the triangles it walks; other kernels walk every
+    // triangle of their tasks
+    ctx->stats.evaluated_units = (sp.kind == TPCF_TRIANGLE && !fp64) ? dev_evaluated : evaluated;
     ctx->stats.tasks = h_tasks.size();
     ctx->stats.kernel_launches = launches;
     ctx->stats.total_ms =
@@ -886,7 +932,7 @@ void worker_loop(tpcf_ctx* ctx) {
                     it = ctx->queue.erase(it);
                     continue;
                 }
-                if (!same_binning(p->spec, first->spec) || p->spec.loop != first->spec.loop) {
+                if (!same_binning(p->spec, first->spec) || p->spec.prune != first->spec.prune) {
                     ++it;
                     continue;
                 }
@@ -1103,8 +1149,7 @@ tpcf_status tpcf_count_batch(tpcf_ctx* ctx, const tpcf_spec* specs, const tpcf_j
             if (done[i]) continue;
             std::vector<GroupJob> g;
             for (int k = i; k < n; k++)
-                if (!done[k] && same_binning(specs[k], specs[i]) && specs[k].loop == specs[i].loop &&
-                    specs[k].prune == specs[i].prune) {
+                if (!done[k] && same_binning(specs[k], specs[i]) && specs[k].prune == specs[i].prune) {
                     g.push_back({&specs[k], &jobs[k], hists[k]});
                     done[k] = 1;
                 }

@@ -25,11 +25,23 @@ constexpr uint32_t TASK_DIAG_JK = 1u << 25;  // tiles J and K are the same tile 
 constexpr uint32_t TASK_SLOT_MASK = 0xFFFFu;
 constexpr int TASK_PRED_SHIFT = 16;          // bits 16..23: Pred
 
-// Encodings of per-side codes in the triangle kernels (values are multiplied
-// by Q*T; invalid codes make every derived index negative or too large).
-constexpr int CODE_ZERO = -(1 << 28);   // side length exactly 0
-constexpr int CODE_BELOW = -(1 << 27);  // 0 < side < s_lo
-constexpr int CODE_ABOVE = (1 << 27);   // side >= s_hi
+// Per-side word of the triangle kernels: word = code * 128 + class_weight.
+// code is the side's s-bin times Q*T (monotone in the side length, so the
+// codes of the shortest and middle side are the min and median of the three
+// words, >> 7); the special codes below keep that order.  class_weight counts
+// side classes so that the sum of a triangle's three weights tells whether any
+// permutation can be counted: below s_lo: 4, at/above s_hi (or rounding to bin
+// S): 1, in range: 0, zero length or at/above the largest side a counted
+// triangle can have: 32 (rejects the triangle).
+constexpr int CODE_ZERO = -(1 << 23);   // side length exactly 0
+constexpr int CODE_BELOW = -(1 << 22);  // 0 < side < s_lo
+constexpr int CODE_ABOVE = (1 << 22);   // side >= s_hi
+constexpr int CW_IN = 0, CW_ABOVE = 1, CW_BELOW = 4, CW_REJECT = 32;
+constexpr int MAX_TRI_BINS = (1 << 22) - 1;  // S*Q*T limit of the fast kernel encodings
+// weight sum (4*nBelow + nAbove, >= 32 if rejected) -> permutation validity
+constexpr unsigned VALID_ANY = 0x37u;   // shortest or middle side in range
+constexpr unsigned VALID_02 = 0x07u;    // shortest side in range (permutations 0 and 2)
+constexpr unsigned VALID_1 = 0x33u;     // middle side in range, no zero side (permutation 1)
 
 // Three-side codes: "at or above hist_max" in clean mode.
 constexpr uint32_t CODE3_CLEAN_FAR = 1u << 28;
@@ -61,6 +73,7 @@ struct TriParams {
     float t_thrB;                // slope of the c-dependent guard half-width
     float t2_off;                // (1 - 3 t_lo)/t_bw - 0.5 - 2*(-0.5) handled in code
     int theta_full;              // theta range covers (0,1): skip range checks
+    float lmax;                  // sides >= lmax cannot belong to a counted triangle
 };
 
 struct ThreeParams {
@@ -88,6 +101,7 @@ struct RecheckQueue {
     uint4* items;                // {slot | weight << 16, ia, ib, ic}
     unsigned int* count;
     unsigned int cap;
+    unsigned long long* evaluated;  // triangles of (i,j) pairs the fast kernel walked
 };
 
 struct LaunchStats {

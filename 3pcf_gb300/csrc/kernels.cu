@@ -190,7 +190,8 @@ constexpr int TRI_THREADS = TRI_WARPS * 32;
 constexpr size_t TRI_SMEM_FIXED = 3 * TILE * sizeof(float4) + TILE * TILE * sizeof(int2) +
                                   TRI_WARPS * TILE * sizeof(int2);
 
-// s-bin code of one side, monotone in the side length, multiplied by Q*T.
+// s-bin code of one side, monotone in the side length, multiplied by Q*T
+// (used by the plain FP64 kernel).
 template <bool FP64>
 __device__ __forceinline__ int tri_side_code(float d, const TriParams& p) {
     typedef FOps<FP64> F;
@@ -198,6 +199,27 @@ __device__ __forceinline__ int tri_side_code(float d, const TriParams& p) {
     if (d < p.s_lo) return CODE_BELOW;
     if (d >= p.s_hi) return CODE_ABOVE;
     return __float2int_rz(F::div(F::sub(d, p.s_lo), p.s_bw)) * (p.Q * p.T);
+}
+
+// Side word of the fast kernel: code * 128 + class weight (see engine.h).
+__device__ __forceinline__ int tri_side_word(float d, const TriParams& p) {
+    int code, w;
+    if (d == 0.f) {
+        code = CODE_ZERO;
+        w = CW_REJECT;
+    } else if (d < p.s_lo) {
+        code = CODE_BELOW;
+        w = CW_BELOW;
+    } else if (d >= p.s_hi) {
+        code = CODE_ABOVE;
+        w = CW_ABOVE;
+    } else {
+        int b = __float2int_rz(__fdiv_rn(__fsub_rn(d, p.s_lo), p.s_bw));
+        code = b * (p.Q * p.T);
+        w = b < p.S ? CW_IN : CW_ABOVE;  // b == S: rounding at the top edge, index past the array
+    }
+    if (d >= p.lmax) w = CW_REJECT;
+    return code * 128 + w;
 }
 
 // 1.5 * 2^23: adding it rounds a float in (-2^22, 2^22) to an integer held in
@@ -220,7 +242,7 @@ __device__ __forceinline__ GuardedBin magic_floor(float f_m) {
     return g;
 }
 
-// theta coordinate of a cosine (approximate), its guard threshold
+// theta coordinate of a cosine (approximate) and its guard threshold
 __device__ __forceinline__ void theta_fast(float c, const TriParams& p, float& f_m, float& thr) {
     float x = fabsf(c);
     float t = __fsub_rn(1.0f, x);
@@ -232,27 +254,30 @@ __device__ __forceinline__ void theta_fast(float c, const TriParams& p, float& f
     P = __fmaf_rn(P, x, p.t_coef[2]);
     P = __fmaf_rn(P, x, p.t_coef[1]);
     P = __fmaf_rn(P, x, p.t_coef[0]);
-    float a = __fmaf_rn(sq, P, -p.t_half);                         // K*acos(|c|) - K*pi/2
+    float a = __fmaf_rn(sq, P, -p.t_half);                                     // K*acos(|c|) - K*pi/2
     a = __int_as_float(__float_as_int(a) ^ (__float_as_int(c) & 0x80000000));  // acos(-x) = pi - acos(x)
     f_m = __fadd_rn(a, p.t_off0);
     thr = __fmaf_rn(-p.t_thrB, y, p.t_thrA);
 }
 
-template <int PRED>
-__device__ __forceinline__ void triangle_one(float a, int ca, float b, int cb, float c, int cc, unsigned w,
-                                             const TriParams& p, unsigned int* Hw, RecheckQueue& q,
-                                             uint32_t slot, uint32_t ia, uint32_t ib, uint32_t ic) {
-    const int SQT = p.len;  // S*Q*T: valid offsets are [0, SQT)
+__device__ __forceinline__ unsigned weight_index(int wa, int wb, int wc) { return (unsigned)(wa + wb + wc) & 127u; }
+__device__ __forceinline__ bool mask_bit(unsigned mask, unsigned idx) { return (__funnelshift_rc(mask, 0u, idx) & 1u) != 0; }
+
+// Full fast path of one triangle (sides a, b, c with their words) whose weight
+// index 'idx' says some permutation may count.  w: multiplicity (0 = none).
+// Returns true if the triangle must be recomputed exactly (guard band).
+template <bool THETA_FULL>
+__device__ __forceinline__ bool triangle_full(float a, int wa, float b, int wb, float c, int wc, unsigned idx,
+                                              unsigned w, const TriParams& p, unsigned int* Hw) {
+    const bool v02 = w && mask_bit(VALID_02, idx);
+    const bool v1 = w && mask_bit(VALID_1, idx);
     float lo_ab = fminf(a, b), hi_ab = fmaxf(a, b);
     float s = fminf(lo_ab, c);
     float l = fmaxf(hi_ab, c);
     float m = fmaxf(lo_ab, fminf(hi_ab, c));
-    int clo = min(ca, cb), chi = max(ca, cb);
-    int off_s = min(clo, cc);
-    int off_m = max(clo, min(chi, cc));
-    bool v02 = (unsigned)off_s < (unsigned)SQT && w;
-    bool v1 = (unsigned)off_m < (unsigned)SQT && off_s != CODE_ZERO && w;
-    if (!__any_sync(0xffffffffu, v02 || v1)) return;
+    int wlo = min(wa, wb), whi = max(wa, wb);
+    int off_s = min(wlo, wc) >> 7;
+    int off_m = max(wlo, min(whi, wc)) >> 7;
 
     float s2 = __fmul_rn(s, s), m2 = __fmul_rn(m, m), l2 = __fmul_rn(l, l);
     float rs = rcp_approx(s), rm = rcp_approx(m);
@@ -272,21 +297,29 @@ __device__ __forceinline__ void triangle_one(float a, int ca, float b, int cb, f
     float thr2 = __fadd_rn(__fadd_rn(thr0, thr1), -0.5f - 1e-6f);
     GuardedBin t0 = magic_floor(f0m), t1 = magic_floor(f1m), t2 = magic_floor(f2m);
 
-    // guard: any permutation that could count has a value near a bin edge
+    // guard: a permutation that could count has a value near a bin edge
     bool gq0 = !(fabsf(q0.err) <= p.q_thr), gq1 = !(fabsf(q1.err) <= p.q_thr), gq2 = !(fabsf(q2.err) <= p.q_thr);
     bool gt0 = !(fabsf(t0.err) <= thr0), gt1 = !(fabsf(t1.err) <= thr1), gt2 = !(fabsf(t2.err) <= thr2);
     bool guard = (v02 && (gq0 || gt0 || gq2 || gt2)) || (v1 && (gq1 || gt1));
 
-    bool ok0 = v02 && (unsigned)q0.bin < (unsigned)p.Q && (unsigned)t0.bin < (unsigned)p.T && !guard;
-    bool ok1 = v1 && (unsigned)q1.bin < (unsigned)p.Q && (unsigned)t1.bin < (unsigned)p.T && !guard;
-    bool ok2 = v02 && (unsigned)q2.bin < (unsigned)p.Q && (unsigned)t2.bin < (unsigned)p.T && !guard;
+    bool ok0 = v02 && !guard && (unsigned)q0.bin < (unsigned)p.Q;
+    bool ok1 = v1 && !guard && (unsigned)q1.bin < (unsigned)p.Q;
+    bool ok2 = v02 && !guard && (unsigned)q2.bin < (unsigned)p.Q;
+    if (!THETA_FULL) {
+        ok0 = ok0 && (unsigned)t0.bin < (unsigned)p.T;
+        ok1 = ok1 && (unsigned)t1.bin < (unsigned)p.T;
+        ok2 = ok2 && (unsigned)t2.bin < (unsigned)p.T;
+    }
     if (ok0) atomicAdd(Hw + off_s + q0.bin * p.T + t0.bin, w);
     if (ok1) atomicAdd(Hw + off_m + q1.bin * p.T + t1.bin, w);
     if (ok2) atomicAdd(Hw + off_s + q2.bin * p.T + t2.bin, w);
-    if (guard) {
-        unsigned int pos = atomicAdd(q.count, 1u);
-        if (pos < q.cap) q.items[pos] = make_uint4(slot | (w << 16), ia, ib, ic);
-    }
+    return guard;
+}
+
+__device__ __forceinline__ void push_recheck(RecheckQueue& q, uint32_t slot, unsigned w, uint32_t ia, uint32_t ib,
+                                             uint32_t ic) {
+    unsigned int pos = atomicAdd(q.count, 1u);
+    if (pos < q.cap) q.items[pos] = make_uint4(slot | (w << 16), ia, ib, ic);
 }
 
 struct TaskGeom {
@@ -315,7 +348,7 @@ __device__ __forceinline__ void load_points(float4* P, const DevJob& J, const Ta
 
 __device__ __forceinline__ int pkey(float4 p) { return __float_as_int(p.w); }
 
-template <int PRED>
+template <int PRED, bool THETA_FULL>
 __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams& p, float4* P, int2* JK,
                                    int2* IJ, unsigned int* Hw, RecheckQueue& q) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -328,52 +361,80 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
         int j = e / TILE, k = e % TILE;
         if (j < g.nB && k < g.nC) {
             float d = ref_dist<false>(P[TILE + j], P[2 * TILE + k]);
-            JK[e] = make_int2(__float_as_int(d), tri_side_code<false>(d, p));
+            JK[e] = make_int2(__float_as_int(d), tri_side_word(d, p));
         }
     }
     __syncthreads();
     int2* row = IJ + warp * TILE;
+    const int k0 = lane, k1 = lane + 32;
+    const int kk0 = k0 < g.nC ? k0 : 0, kk1 = k1 < g.nC ? k1 : 0;
+    const int key0 = pkey(P[2 * TILE + kk0]), key1 = pkey(P[2 * TILE + kk1]);
+    unsigned evaluated = 0;
     for (int i = warp; i < g.nA; i += TRI_WARPS) {
         const float4 pi = P[i];
-        float dik[2];
-        int cik[2];
-#pragma unroll
-        for (int r = 0; r < 2; r++) {
-            int k = lane + 32 * r;
-            float d = k < g.nC ? ref_dist<false>(pi, P[2 * TILE + k]) : 0.f;
-            dik[r] = d;
-            cik[r] = tri_side_code<false>(d, p);
-            int j = k;
-            if (j < g.nB) {
-                float dj = ref_dist<false>(pi, P[TILE + j]);
-                row[j] = make_int2(__float_as_int(dj), tri_side_code<false>(dj, p));
-            }
+        float dik0 = 0.f, dik1 = 0.f;
+        int wik0 = CW_REJECT, wik1 = CW_REJECT;
+        if (k0 < g.nC) {
+            dik0 = ref_dist<false>(pi, P[2 * TILE + k0]);
+            wik0 = tri_side_word(dik0, p);
+        }
+        if (k1 < g.nC) {
+            dik1 = ref_dist<false>(pi, P[2 * TILE + k1]);
+            wik1 = tri_side_word(dik1, p);
+        }
+        for (int j = lane; j < g.nB; j += 32) {
+            float dj = ref_dist<false>(pi, P[TILE + j]);
+            row[j] = make_int2(__float_as_int(dj), tri_side_word(dj, p));
         }
         __syncwarp();
         const int ki = pkey(pi);
         for (int j = diag_ij ? i + 1 : 0; j < g.nB; j++) {
             const int2 ij = row[j];
-            const float4 pj = P[TILE + j];
-            const int kj = pkey(pj);
-            if (PRED == PRED_SAME && !(ki <= kj)) continue;  // uniform over the warp
-#pragma unroll
-            for (int r = 0; r < 2; r++) {
-                const int k = lane + 32 * r;
-                const int kk = k < g.nC ? k : g.nC - 1 < 0 ? 0 : g.nC - 1;
-                const int2 jk = JK[j * TILE + kk];
-                unsigned w = (k < g.nC && (!diag_jk || k > j)) ? 1u : 0u;
-                const int kkey = pkey(P[2 * TILE + kk]);
-                if (PRED == PRED_DDR) w = w ? (unsigned)(kkey >= ki) + (unsigned)(kkey >= kj) : 0u;
-                if (PRED == PRED_SAME || PRED == PRED_ONE) w = (w && kj <= kkey) ? 1u : 0u;
-                triangle_one<PRED>(__int_as_float(ij.x), ij.y, dik[r], cik[r], __int_as_float(jk.x), jk.y, w, p, Hw,
-                                   q, slot, (uint32_t)(g.a0 + i), (uint32_t)(g.b0 + j), (uint32_t)(g.c0 + kk));
+            if ((ij.y & 127) >= CW_REJECT) continue;  // no counted triangle has this side (warp-uniform)
+            const int kj = pkey(P[TILE + j]);
+            if (PRED == PRED_SAME && !(ki <= kj)) continue;
+            evaluated += diag_jk ? (unsigned)max(g.nC - j - 1, 0) : (unsigned)g.nC;
+            const int2 jk0 = JK[j * TILE + kk0], jk1 = JK[j * TILE + kk1];
+            unsigned w0 = (k0 < g.nC && (!diag_jk || k0 > j)) ? 1u : 0u;
+            unsigned w1 = (k1 < g.nC && (!diag_jk || k1 > j)) ? 1u : 0u;
+            if (PRED == PRED_DDR) {
+                w0 = w0 ? (unsigned)(key0 >= ki) + (unsigned)(key0 >= kj) : 0u;
+                w1 = w1 ? (unsigned)(key1 >= ki) + (unsigned)(key1 >= kj) : 0u;
             }
+            if (PRED == PRED_SAME || PRED == PRED_ONE) {
+                w0 = (w0 && kj <= key0) ? 1u : 0u;
+                w1 = (w1 && kj <= key1) ? 1u : 0u;
+            }
+            const unsigned idx0 = weight_index(ij.y, wik0, jk0.y), idx1 = weight_index(ij.y, wik1, jk1.y);
+            const bool any0 = w0 && mask_bit(VALID_ANY, idx0), any1 = w1 && mask_bit(VALID_ANY, idx1);
+            if (!__any_sync(0xffffffffu, any0 || any1)) continue;
+            const float dij = __int_as_float(ij.x);
+            // both triangles of the lane in one basic block (two independent chains)
+            const bool g0 = triangle_full<THETA_FULL>(dij, ij.y, dik0, wik0, __int_as_float(jk0.x), jk0.y, idx0,
+                                                      any0 ? w0 : 0u, p, Hw);
+            const bool g1 = triangle_full<THETA_FULL>(dij, ij.y, dik1, wik1, __int_as_float(jk1.x), jk1.y, idx1,
+                                                      any1 ? w1 : 0u, p, Hw);
+            if (g0) push_recheck(q, slot, w0, (uint32_t)(g.a0 + i), (uint32_t)(g.b0 + j), (uint32_t)(g.c0 + kk0));
+            if (g1) push_recheck(q, slot, w1, (uint32_t)(g.a0 + i), (uint32_t)(g.b0 + j), (uint32_t)(g.c0 + kk1));
         }
         __syncwarp();
     }
+    if (lane == 0 && evaluated) atomicAdd(q.evaluated, (unsigned long long)evaluated);
 }
 
-__global__ void __launch_bounds__(TRI_THREADS, 1)
+template <bool THETA_FULL>
+__device__ __forceinline__ void triangle_dispatch(const DevJob& J, uint4 task, const TriParams& p, float4* P,
+                                                  int2* JK, int2* IJ, unsigned int* Hw, RecheckQueue& q) {
+    switch ((task.x >> TASK_PRED_SHIFT) & 0xFF) {
+        case PRED_NONE: triangle_task_fast<PRED_NONE, THETA_FULL>(J, task, p, P, JK, IJ, Hw, q); break;
+        case PRED_DDR: triangle_task_fast<PRED_DDR, THETA_FULL>(J, task, p, P, JK, IJ, Hw, q); break;
+        case PRED_SAME: triangle_task_fast<PRED_SAME, THETA_FULL>(J, task, p, P, JK, IJ, Hw, q); break;
+        default: triangle_task_fast<PRED_ONE, THETA_FULL>(J, task, p, P, JK, IJ, Hw, q); break;
+    }
+}
+
+template <bool THETA_FULL>
+__global__ void __launch_bounds__(TRI_THREADS, 2)
 triangle_fast_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ tasks, unsigned int ntasks,
                      unsigned int* task_counter, TriParams p, RecheckQueue q, int copies) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -402,13 +463,7 @@ triangle_fast_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ 
         cur = slot;
         if (slot < 0) break;
         since++;
-        const DevJob& J = jobs[slot];
-        switch ((task.x >> TASK_PRED_SHIFT) & 0xFF) {
-            case PRED_NONE: triangle_task_fast<PRED_NONE>(J, task, p, P, JK, IJ, Hw, q); break;
-            case PRED_DDR: triangle_task_fast<PRED_DDR>(J, task, p, P, JK, IJ, Hw, q); break;
-            case PRED_SAME: triangle_task_fast<PRED_SAME>(J, task, p, P, JK, IJ, Hw, q); break;
-            default: triangle_task_fast<PRED_ONE>(J, task, p, P, JK, IJ, Hw, q); break;
-        }
+        triangle_dispatch<THETA_FULL>(jobs[slot], task, p, P, JK, IJ, Hw, q);
     }
 }
 
@@ -710,9 +765,16 @@ cudaError_t launch_triangle_fast(const DevJob* jobs, const uint4* tasks, unsigne
                                  unsigned int* task_counter, const TriParams& p, RecheckQueue q, int grid,
                                  int copies, cudaStream_t st) {
     size_t smem = triangle_smem_bytes(p.len, copies);
-    cudaError_t e = cudaFuncSetAttribute(triangle_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    triangle_fast_kernel<<<grid, TRI_THREADS, smem, st>>>(jobs, tasks, ntasks, task_counter, p, q, copies);
+    cudaError_t e;
+    if (p.theta_full) {
+        e = cudaFuncSetAttribute(triangle_fast_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        triangle_fast_kernel<true><<<grid, TRI_THREADS, smem, st>>>(jobs, tasks, ntasks, task_counter, p, q, copies);
+    } else {
+        e = cudaFuncSetAttribute(triangle_fast_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        triangle_fast_kernel<false><<<grid, TRI_THREADS, smem, st>>>(jobs, tasks, ntasks, task_counter, p, q, copies);
+    }
     return cudaGetLastError();
 }
 
