@@ -50,9 +50,15 @@ def build(verbose=False):
     k_src = os.path.join(CSRC, "kernels.cu")
     k_obj = os.path.join(BUILD, "kernels.o")
     objs.append(k_obj)
-    if _newer(k_obj, [k_src] + hdr):
-        cmds.append([NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                                     "-Xptxas", "-v" if verbose else "-O3", "-c", k_src, "-o", k_obj])
+    # TPCF_NVCC_FLAGS: extra defines for kernel tuning sweeps (e.g. -DTRI_MIN_BLOCKS=2)
+    extra = os.environ.get("TPCF_NVCC_FLAGS", "").split()
+    stamp = os.path.join(BUILD, "kernels.flags")
+    if not os.path.exists(stamp) or open(stamp).read() != " ".join(extra):
+        with open(stamp, "w") as f:
+            f.write(" ".join(extra))
+    if _newer(k_obj, [k_src, stamp] + hdr):
+        cmds.append([NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"] + extra +
+                    ["-Xptxas", "-v" if verbose else "-O3", "-c", k_src, "-o", k_obj])
     for name in ("engine.cpp", "io.cpp"):
         src = os.path.join(CSRC, name)
         obj = os.path.join(BUILD, name.replace(".cpp", ".o"))

@@ -115,9 +115,9 @@ struct View {
 // Balanced k-d split: order[lo, hi) is split along the widest axis so that the
 // left part holds a multiple of TILE points, recursively, until parts hold at
 // most TILE points.  Leaves appear in order, giving spatially compact tiles.
-void kd_order(const float* xyz, std::vector<int32_t>& order, int64_t lo, int64_t hi) {
+void kd_order(const float* xyz, std::vector<int32_t>& order, int64_t lo, int64_t hi, int tile) {
     int64_t n = hi - lo;
-    if (n <= TILE) return;
+    if (n <= tile) return;
     float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (int64_t i = lo; i < hi; i++)
         for (int a = 0; a < 3; a++) {
@@ -128,16 +128,16 @@ void kd_order(const float* xyz, std::vector<int32_t>& order, int64_t lo, int64_t
     int ax = 0;
     for (int a = 1; a < 3; a++)
         if (mx[a] - mn[a] > mx[ax] - mn[ax]) ax = a;
-    int64_t ntile = (n + TILE - 1) / TILE;
-    int64_t left = ((ntile + 1) / 2) * TILE;
-    if (left >= n) left = n - TILE;
+    int64_t ntile = (n + tile - 1) / tile;
+    int64_t left = ((ntile + 1) / 2) * tile;
+    if (left >= n) left = n - tile;
     int64_t mid = lo + left;
     std::nth_element(order.begin() + lo, order.begin() + mid, order.begin() + hi, [&](int32_t p, int32_t q) {
         float vp = xyz[3 * (int64_t)p + ax], vq = xyz[3 * (int64_t)q + ax];
         return vp < vq || (vp == vq && p < q);
     });
-    kd_order(xyz, order, lo, mid);
-    kd_order(xyz, order, mid, hi);
+    kd_order(xyz, order, lo, mid, tile);
+    kd_order(xyz, order, mid, hi, tile);
 }
 
 // Lower bound on the reference's float side length between any point of box
@@ -406,8 +406,11 @@ Binning make_binning(const tpcf_spec& sp) {
         b.tri_prune = false;
     }
     // device copy of the bound, rounded up so that a float side >= it is >= lmax
-    if (sp.kind == TPCF_TRIANGLE)
+    if (sp.kind == TPCF_TRIANGLE) {
         b.tri.lmax = b.lmax < 3e38 ? nextafterf((float)b.lmax, INFINITY) : INFINITY;
+        double mid = (double)b.tri.s_hi * (double)b.tri.q_hi * (1 + 1e-5) + 1e-6;
+        b.tri.mid_hi = sp.prune && b.tri.q_hi > 0 ? nextafterf((float)mid, INFINITY) : INFINITY;
+    }
     return b;
 }
 
@@ -476,7 +479,8 @@ struct tpcf_ctx {
     uint64_t next_handle = 1;
     std::map<uint64_t, std::shared_ptr<Catalog>> catalogs;
     std::map<uint64_t, std::shared_ptr<DevBuf<float4>>> cat_dev;  // unsorted points (resident)
-    std::map<std::tuple<uint64_t, int64_t, int64_t>, std::shared_ptr<View>> views;
+    std::map<std::tuple<uint64_t, int64_t, int64_t, int>, std::shared_ptr<View>> views;
+    int tile_points = TILE;  // points per spatial tile (<= TILE)
     // acos table
     bool acos_ready = false;
     DevBuf<uint32_t> acos_keys, acos_vals, acos_bucket;
@@ -514,7 +518,8 @@ std::shared_ptr<View> get_view(tpcf_ctx* ctx, uint64_t handle, int64_t begin, in
     const Catalog& c = *it->second;
     if (end < 0) end = c.n;
     if (begin < 0 || begin > end || end > c.n) throw InvalidArg{"catalog range out of bounds"};
-    auto key = std::make_tuple(handle, begin, end);
+    const int tile = ctx->tile_points;
+    auto key = std::make_tuple(handle, begin, end, tile);
     auto vi = ctx->views.find(key);
     if (vi != ctx->views.end()) return vi->second;
     auto v = std::make_shared<View>();
@@ -528,8 +533,8 @@ std::shared_ptr<View> get_view(tpcf_ctx* ctx, uint64_t handle, int64_t begin, in
     }
     std::vector<int32_t> order(n);
     std::iota(order.begin(), order.end(), 0);
-    kd_order(xyz.data(), order, 0, n);
-    v->ntiles = (int)((n + TILE - 1) / TILE);
+    kd_order(xyz.data(), order, 0, n, tile);
+    v->ntiles = (int)((n + tile - 1) / tile);
     std::vector<float4> pts(std::max<int64_t>(n, 1));
     for (int64_t i = 0; i < n; i++) {
         int32_t o = order[i];
@@ -543,7 +548,7 @@ std::shared_ptr<View> get_view(tpcf_ctx* ctx, uint64_t handle, int64_t begin, in
     }
     v->h_tile_start.resize(v->ntiles + 1);
     v->boxes.resize(v->ntiles);
-    for (int t = 0; t <= v->ntiles; t++) v->h_tile_start[t] = (int32_t)std::min<int64_t>((int64_t)t * TILE, n);
+    for (int t = 0; t <= v->ntiles; t++) v->h_tile_start[t] = (int32_t)std::min<int64_t>((int64_t)t * tile, n);
     for (int t = 0; t < v->ntiles; t++) {
         Box b;
         for (int a = 0; a < 3; a++) {
@@ -731,7 +736,9 @@ int occupancy_grid(tpcf_ctx* ctx, int kind, size_t smem, int fp64, uint64_t ntas
     int per_sm = 1;
     int max_smem = 0;
     cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx->device);
-    if (smem > 0) per_sm = std::max(1, std::min(4, (int)(max_smem / (smem + 1024))));
+    const char* bps = getenv("TPCF_TRI_BLOCKS_PER_SM");
+    const int tri_per_sm = bps ? atoi(bps) : 3;
+    if (smem > 0) per_sm = std::max(1, std::min(kind == TPCF_TRIANGLE ? tri_per_sm : 4, (int)(max_smem / (smem + 1024))));
     else per_sm = 4;
     uint64_t g = (uint64_t)ctx->num_sms * per_sm;
     if (g > ntasks) g = std::max<uint64_t>(ntasks, 1);
@@ -778,7 +785,7 @@ void run_group(tpcf_ctx* ctx, const std::vector<GroupJob>& group) {
     for (size_t i = 0; i < tasks.size(); i++) h_tasks[i] = tasks[i].second;
     ctx->d_jobs.reserve(dj.size());
     ctx->d_tasks.reserve(std::max<size_t>(h_tasks.size(), 1));
-    ctx->d_counters.reserve(4);
+    ctx->d_counters.reserve(8);
     cudaStream_t st = ctx->stream;
     CK(cudaMemcpyAsync(ctx->d_jobs.p, dj.data(), dj.size() * sizeof(DevJob), cudaMemcpyHostToDevice, st));
     ctx->h2d += dj.size() * sizeof(DevJob) + h_tasks.size() * sizeof(uint4);
@@ -788,16 +795,19 @@ void run_group(tpcf_ctx* ctx, const std::vector<GroupJob>& group) {
     if (sp.kind == TPCF_TRIANGLE) ensure_acos(ctx);
     uint64_t launches = 0;
     unsigned int queue_cap = (unsigned int)std::max<size_t>(ctx->d_queue.n, (size_t)1 << 22);
-    uint64_t dev_evaluated = 0;
+    uint64_t dev_evaluated = 0, dev_binned = 0;
     for (int attempt = 0; attempt < 3; attempt++) {
         CK(cudaMemsetAsync(ctx->d_hist.p, 0, hist_total * sizeof(unsigned long long), st));
-        CK(cudaMemsetAsync(ctx->d_counters.p, 0, 4 * sizeof(unsigned int), st));
+        CK(cudaMemsetAsync(ctx->d_counters.p, 0, 8 * sizeof(unsigned int), st));
         CK(cudaEventRecord(ctx->ev0, st));
         unsigned int nt = (unsigned int)h_tasks.size();
         launches = 0;
         if (sp.kind == TPCF_TRIANGLE) {
+            // warp-private histogram copies, as many as still let three CTAs
+            // share an SM (the kernel is latency-bound and needs the warps)
             int copies = 8;
-            size_t smem_cap = 200 * 1024;
+            const char* cap_env = getenv("TPCF_TRI_SMEM_CAP_KB");
+            size_t smem_cap = (cap_env ? (size_t)atoi(cap_env) : (size_t)74) * 1024;
             while (copies > 1 && triangle_smem_bytes(bin.len, copies) > smem_cap) copies /= 2;
             if (triangle_smem_bytes(bin.len, copies) > 227 * 1024) throw InvalidArg{"triangle histogram too large for shared memory"};
             size_t smem = triangle_smem_bytes(bin.len, copies);
@@ -839,7 +849,7 @@ void run_group(tpcf_ctx* ctx, const std::vector<GroupJob>& group) {
             launches = 1;
         }
         CK(cudaEventRecord(ctx->ev1, st));
-        unsigned int counters[4];
+        unsigned int counters[8];
         CK(cudaMemcpyAsync(counters, ctx->d_counters.p, sizeof(counters), cudaMemcpyDeviceToHost, st));
         ctx->h_hist.resize(hist_total);
         CK(cudaMemcpyAsync(ctx->h_hist.data(), ctx->d_hist.p, hist_total * sizeof(unsigned long long),
@@ -848,6 +858,7 @@ void run_group(tpcf_ctx* ctx, const std::vector<GroupJob>& group) {
         ctx->d2h += sizeof(counters) + hist_total * sizeof(unsigned long long);
         ctx->stats.recheck_units = counters[1];
         memcpy(&dev_evaluated, &counters[2], sizeof(dev_evaluated));
+        memcpy(&dev_binned, &counters[4], sizeof(dev_binned));
         if (sp.kind == TPCF_TRIANGLE && !fp64 && counters[1] > queue_cap) {
             // the recheck queue overflowed: grow it and count again
             queue_cap = (unsigned int)std::min<uint64_t>((uint64_t)counters[1] + (counters[1] >> 2) + 1024, 0xF0000000ull);
@@ -867,6 +878,7 @@ void run_group(tpcf_ctx* ctx, const std::vector<GroupJob>& group) {
     // contain and counts the triangles it walks; other kernels walk every
     // triangle of their tasks
     ctx->stats.evaluated_units = (sp.kind == TPCF_TRIANGLE && !fp64) ? dev_evaluated : evaluated;
+    ctx->stats.binned_units = (sp.kind == TPCF_TRIANGLE && !fp64) ? dev_binned : evaluated;
     ctx->stats.tasks = h_tasks.size();
     ctx->stats.kernel_launches = launches;
     ctx->stats.total_ms =
@@ -1011,6 +1023,8 @@ tpcf_status tpcf_create(tpcf_ctx** out, int32_t device) {
         CK(cudaEventCreate(&ctx->ev0));
         CK(cudaEventCreate(&ctx->ev1));
         CK(cudaEventCreate(&ctx->ev_mid));
+        const char* tp = getenv("TPCF_TILE_POINTS");
+        if (tp) ctx->tile_points = std::max(8, std::min(TILE, atoi(tp)));
         const char* adm = getenv("TPCF_ADMIT_BYTES");
         if (adm) ctx->admit_bytes = atoll(adm);
     });
@@ -1156,6 +1170,7 @@ tpcf_status tpcf_count_batch(tpcf_ctx* ctx, const tpcf_spec* specs, const tpcf_j
             run_group(ctx, g);
             acc.kernel_ms += ctx->stats.kernel_ms;
             acc.main_kernel_ms += ctx->stats.main_kernel_ms;
+            acc.binned_units += ctx->stats.binned_units;
             acc.total_ms += ctx->stats.total_ms;
             acc.loop_units += ctx->stats.loop_units;
             acc.evaluated_units += ctx->stats.evaluated_units;

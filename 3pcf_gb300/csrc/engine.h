@@ -74,6 +74,8 @@ struct TriParams {
     float t2_off;                // (1 - 3 t_lo)/t_bw - 0.5 - 2*(-0.5) handled in code
     int theta_full;              // theta range covers (0,1): skip range checks
     float lmax;                  // sides >= lmax cannot belong to a counted triangle
+    float mid_hi;                // s_hi * q_hi (rounded up): permutation 0 needs two sides below it,
+                                 // permutation 1 needs all three below it
 };
 
 struct ThreeParams {

@@ -187,8 +187,16 @@ __device__ __forceinline__ float rsqrt_approx(float x) {
 
 constexpr int TRI_WARPS = 8;
 constexpr int TRI_THREADS = TRI_WARPS * 32;
+constexpr int TRI_QCAP = 128;  // per-warp candidate queue: up to 63 pending + 64 new
+// per j of role B: bit masks over k of the classes of side j-k (B, I, M, H)
+// and of key_k >= key_j
+struct JMasks {
+    unsigned long long c[4];
+    unsigned long long kge;
+};
 constexpr size_t TRI_SMEM_FIXED = 3 * TILE * sizeof(float4) + TILE * TILE * sizeof(int2) +
-                                  TRI_WARPS * TILE * sizeof(int2);
+                                  2 * TRI_WARPS * TILE * sizeof(int2) + TRI_WARPS * TRI_QCAP * sizeof(uint32_t) +
+                                  TRI_WARPS * TILE * sizeof(uint32_t) + TILE * sizeof(JMasks);
 
 // s-bin code of one side, monotone in the side length, multiplied by Q*T
 // (used by the plain FP64 kernel).
@@ -348,105 +356,239 @@ __device__ __forceinline__ void load_points(float4* P, const DevJob& J, const Ta
 
 __device__ __forceinline__ int pkey(float4 p) { return __float_as_int(p.w); }
 
+// Candidate triangle of the current i: j (6 bits), k (6 bits), weight (2 bits).
+__device__ __forceinline__ uint32_t pack_cand(int j, int k, unsigned w) { return (uint32_t)j | ((uint32_t)k << 6) | (w << 12); }
+
+// Runs the full binning path on n (<= 64) queued candidates, up to two per
+// lane (two independent dependency chains per lane).
+template <bool THETA_FULL>
+__device__ __forceinline__ void run_candidates(const uint32_t* cand, int n, const int2* row_ij, const int2* row_ik,
+                                               const int2* JK, const TriParams& p, unsigned int* Hw, RecheckQueue& q,
+                                               uint32_t slot, uint32_t ia, int b0, int c0) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t e0 = lane < n ? cand[lane] : 0u;
+    const uint32_t e1 = lane + 32 < n ? cand[lane + 32] : 0u;
+    const int j0 = e0 & 63, k0 = (e0 >> 6) & 63, j1 = e1 & 63, k1 = (e1 >> 6) & 63;
+    const unsigned w0 = e0 >> 12, w1 = e1 >> 12;
+    const int2 ij0 = row_ij[j0], ik0 = row_ik[k0], jk0 = JK[j0 * TILE + k0];
+    const int2 ij1 = row_ij[j1], ik1 = row_ik[k1], jk1 = JK[j1 * TILE + k1];
+    const bool g0 = triangle_full<THETA_FULL>(__int_as_float(ij0.x), ij0.y, __int_as_float(ik0.x), ik0.y,
+                                              __int_as_float(jk0.x), jk0.y, weight_index(ij0.y, ik0.y, jk0.y), w0,
+                                              p, Hw);
+    bool g1 = false;
+    if (n > 32)  // warp-uniform
+        g1 = triangle_full<THETA_FULL>(__int_as_float(ij1.x), ij1.y, __int_as_float(ik1.x), ik1.y,
+                                       __int_as_float(jk1.x), jk1.y, weight_index(ij1.y, ik1.y, jk1.y), w1, p, Hw);
+    if (g0) push_recheck(q, slot, w0, ia, (uint32_t)(b0 + j0), (uint32_t)(c0 + k0));
+    if (g1) push_recheck(q, slot, w1, ia, (uint32_t)(b0 + j1), (uint32_t)(c0 + k1));
+}
+
+// Side class for candidate filtering: 0 none (zero length or too long),
+// 1 below s_lo, 2 in the s range, 3 above s_hi but below s_hi*q_hi, 4 from
+// s_hi*q_hi up to the largest side a counted triangle can have.
+__device__ __forceinline__ int side_class(int word, float d, const TriParams& p) {
+    const int w = word & 127;
+    if (w >= CW_REJECT) return 0;
+    if (w == CW_BELOW) return 1;
+    if (w == CW_IN) return 2;
+    return d < p.mid_hi ? 3 : 4;
+}
+
+__device__ __forceinline__ unsigned long long ballot64(bool lo, bool hi) {
+    return (unsigned long long)__ballot_sync(0xffffffffu, lo) | ((unsigned long long)__ballot_sync(0xffffffffu, hi) << 32);
+}
+
+// Candidate k's of a pair (i, j) whose side i-j has class cij, from the class
+// masks of the sides i-k (n*) and j-k (m*).  A triangle can count only through
+// permutation 0/2 (no side below s_lo, one side in the s range, at most one
+// side at/above s_hi*q_hi) or permutation 1 (no side at/above s_hi*q_hi, at
+// most one below s_lo, at most one in [s_hi, s_hi*q_hi)); these are the
+// (class_ik, class_jk) combinations that leave one of the two possible.
+__device__ __forceinline__ unsigned long long candidate_mask(int cij, const unsigned long long n[4], const JMasks& m) {
+    const unsigned long long nB = n[0], nI = n[1], nM = n[2], nH = n[3];
+    const unsigned long long mB = m.c[0], mI = m.c[1], mM = m.c[2], mH = m.c[3];
+    if (cij == 2) return (nB | nI | nM | nH) & (mB | mI | mM | mH) & ~((nB | nH) & (mB | mH));
+    if (cij == 3) return (nI & (mB | mI | mM | mH)) | ((nB | nI | nM | nH) & mI);
+    return (nI & (mI | mM)) | (nM & mI);  // cij == 1 or 4
+}
+
 template <int PRED, bool THETA_FULL>
 __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams& p, float4* P, int2* JK,
-                                   int2* IJ, unsigned int* Hw, RecheckQueue& q) {
+                                   int2* IJ, int2* IK, uint32_t* Q, uint32_t* JL, JMasks* JM, unsigned int* Hw,
+                                   RecheckQueue& q, unsigned long long& evaluated, unsigned long long& binned,
+                                   int* next_i) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const TaskGeom g = task_geom(J, task);
     const uint32_t slot = task.x & TASK_SLOT_MASK;
     const bool diag_ij = task.x & TASK_DIAG_IJ, diag_jk = task.x & TASK_DIAG_JK;
     load_points(P, J, g);
+    if (threadIdx.x == 0) *next_i = 0;
     __syncthreads();
-    for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
-        int j = e / TILE, k = e % TILE;
-        if (j < g.nB && k < g.nC) {
-            float d = ref_dist<false>(P[TILE + j], P[2 * TILE + k]);
-            JK[e] = make_int2(__float_as_int(d), tri_side_word(d, p));
+    // rows j of the j-k side table and their class masks, one warp per row
+    const int key_k0 = pkey(P[2 * TILE + lane]), key_k1 = pkey(P[2 * TILE + lane + 32]);
+    for (int j = warp; j < g.nB; j += TRI_WARPS) {
+        const float4 pj = P[TILE + j];
+        int c0 = 0, c1 = 0;
+        if (lane < g.nC) {
+            float d = ref_dist<false>(pj, P[2 * TILE + lane]);
+            int w = tri_side_word(d, p);
+            JK[j * TILE + lane] = make_int2(__float_as_int(d), w);
+            c0 = side_class(w, d, p);
         }
+        if (lane + 32 < g.nC) {
+            float d = ref_dist<false>(pj, P[2 * TILE + lane + 32]);
+            int w = tri_side_word(d, p);
+            JK[j * TILE + lane + 32] = make_int2(__float_as_int(d), w);
+            c1 = side_class(w, d, p);
+        }
+        JMasks m;
+#pragma unroll
+        for (int c = 0; c < 4; c++) m.c[c] = ballot64(c0 == c + 1, c1 == c + 1);
+        const int kj = pkey(pj);
+        m.kge = ballot64(lane < g.nC && key_k0 >= kj, lane + 32 < g.nC && key_k1 >= kj);
+        if (lane == 0) JM[j] = m;
     }
     __syncthreads();
-    int2* row = IJ + warp * TILE;
-    const int k0 = lane, k1 = lane + 32;
-    const int kk0 = k0 < g.nC ? k0 : 0, kk1 = k1 < g.nC ? k1 : 0;
-    const int key0 = pkey(P[2 * TILE + kk0]), key1 = pkey(P[2 * TILE + kk1]);
-    unsigned evaluated = 0;
-    for (int i = warp; i < g.nA; i += TRI_WARPS) {
+    int2* row_ij = IJ + warp * TILE;
+    int2* row_ik = IK + warp * TILE;
+    uint32_t* cand = Q + warp * TRI_QCAP;
+    uint32_t* jlist = JL + warp * TILE;
+    const unsigned lt = (1u << lane) - 1u;
+    unsigned ev = 0, bn = 0;
+    for (;;) {
+        // points of role A are handed out to warps dynamically (balances the
+        // very uneven work per point)
+        int i = 0;
+        if (lane == 0) i = atomicAdd(next_i, 1);
+        i = __shfl_sync(0xffffffffu, i, 0);
+        if (i >= g.nA) break;
         const float4 pi = P[i];
-        float dik0 = 0.f, dik1 = 0.f;
-        int wik0 = CW_REJECT, wik1 = CW_REJECT;
-        if (k0 < g.nC) {
-            dik0 = ref_dist<false>(pi, P[2 * TILE + k0]);
-            wik0 = tri_side_word(dik0, p);
-        }
-        if (k1 < g.nC) {
-            dik1 = ref_dist<false>(pi, P[2 * TILE + k1]);
-            wik1 = tri_side_word(dik1, p);
-        }
-        for (int j = lane; j < g.nB; j += 32) {
-            float dj = ref_dist<false>(pi, P[TILE + j]);
-            row[j] = make_int2(__float_as_int(dj), tri_side_word(dj, p));
-        }
-        __syncwarp();
         const int ki = pkey(pi);
-        for (int j = diag_ij ? i + 1 : 0; j < g.nB; j++) {
-            const int2 ij = row[j];
-            if ((ij.y & 127) >= CW_REJECT) continue;  // no counted triangle has this side (warp-uniform)
-            const int kj = pkey(P[TILE + j]);
-            if (PRED == PRED_SAME && !(ki <= kj)) continue;
-            evaluated += diag_jk ? (unsigned)max(g.nC - j - 1, 0) : (unsigned)g.nC;
-            const int2 jk0 = JK[j * TILE + kk0], jk1 = JK[j * TILE + kk1];
-            unsigned w0 = (k0 < g.nC && (!diag_jk || k0 > j)) ? 1u : 0u;
-            unsigned w1 = (k1 < g.nC && (!diag_jk || k1 > j)) ? 1u : 0u;
+        // i-k sides: words for the binning path, class masks for the filter
+        int c0 = 0, c1 = 0;
+        if (lane < g.nC) {
+            float d = ref_dist<false>(pi, P[2 * TILE + lane]);
+            int w = tri_side_word(d, p);
+            row_ik[lane] = make_int2(__float_as_int(d), w);
+            c0 = side_class(w, d, p);
+        }
+        if (lane + 32 < g.nC) {
+            float d = ref_dist<false>(pi, P[2 * TILE + lane + 32]);
+            int w = tri_side_word(d, p);
+            row_ik[lane + 32] = make_int2(__float_as_int(d), w);
+            c1 = side_class(w, d, p);
+        }
+        unsigned long long n[4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) n[c] = ballot64(c0 == c + 1, c1 == c + 1);
+        const unsigned long long any_k = n[0] | n[1] | n[2] | n[3];
+        unsigned long long kge_i = 0;
+        if (PRED == PRED_DDR) kge_i = ballot64(lane < g.nC && key_k0 >= ki, lane + 32 < g.nC && key_k1 >= ki);
+        // i-j sides: words, and the list of j that can be in a counted triangle
+        bool ja = false, jb = false;
+        uint32_t ea = 0, eb = 0;
+        for (int h = 0; h < 2; h++) {
+            const int j = lane + 32 * h;
+            bool ok = false;
+            uint32_t e = 0;
+            if (j < g.nB) {
+                float d = ref_dist<false>(pi, P[TILE + j]);
+                int w = tri_side_word(d, p);
+                row_ij[j] = make_int2(__float_as_int(d), w);
+                int c = side_class(w, d, p);
+                ok = c != 0 && (!diag_ij || j > i);
+                if (PRED == PRED_SAME) ok = ok && ki <= pkey(P[TILE + j]);
+                e = (uint32_t)j | ((uint32_t)c << 8);
+            }
+            if (h == 0) { ja = ok; ea = e; } else { jb = ok; eb = e; }
+        }
+        const unsigned bja = __ballot_sync(0xffffffffu, ja), bjb = __ballot_sync(0xffffffffu, jb);
+        if (ja) jlist[__popc(bja & lt)] = ea;
+        if (jb) jlist[__popc(bja) + __popc(bjb & lt)] = eb;
+        const int nj = any_k ? __popc(bja) + __popc(bjb) : 0;
+        __syncwarp();
+        const uint32_t ia = (uint32_t)(g.a0 + i);
+        int qn = 0;  // queued candidates (warp-uniform)
+        for (int t = 0; t < nj; t++) {
+            const uint32_t e = jlist[t];
+            const int j = e & 63, cij = (int)(e >> 8);
+            const JMasks m = JM[j];
+            unsigned long long cm = candidate_mask(cij, n, m);
+            if (diag_jk) cm &= j >= 63 ? 0ull : (~0ull << (j + 1));
+            unsigned long long w2 = 0;
             if (PRED == PRED_DDR) {
-                w0 = w0 ? (unsigned)(key0 >= ki) + (unsigned)(key0 >= kj) : 0u;
-                w1 = w1 ? (unsigned)(key1 >= ki) + (unsigned)(key1 >= kj) : 0u;
+                w2 = cm & kge_i & m.kge;           // weight 2: k >= i and k >= j
+                cm &= kge_i | m.kge;               // weight 0 otherwise
+            } else if (PRED == PRED_SAME || PRED == PRED_ONE) {
+                cm &= m.kge;                       // key_j <= key_k
             }
-            if (PRED == PRED_SAME || PRED == PRED_ONE) {
-                w0 = (w0 && kj <= key0) ? 1u : 0u;
-                w1 = (w1 && kj <= key1) ? 1u : 0u;
+            ev += (unsigned)__popcll(any_k);
+            if (!cm) continue;
+            const unsigned lo = (unsigned)cm, hi = (unsigned)(cm >> 32);
+            const int nlo = __popc(lo);
+            if ((lo >> lane) & 1u) {
+                const unsigned w = PRED == PRED_DDR ? 1u + (unsigned)((w2 >> lane) & 1ull) : 1u;
+                cand[qn + __popc(lo & lt)] = pack_cand(j, lane, w);
             }
-            const unsigned idx0 = weight_index(ij.y, wik0, jk0.y), idx1 = weight_index(ij.y, wik1, jk1.y);
-            const bool any0 = w0 && mask_bit(VALID_ANY, idx0), any1 = w1 && mask_bit(VALID_ANY, idx1);
-            if (!__any_sync(0xffffffffu, any0 || any1)) continue;
-            const float dij = __int_as_float(ij.x);
-            // both triangles of the lane in one basic block (two independent chains)
-            const bool g0 = triangle_full<THETA_FULL>(dij, ij.y, dik0, wik0, __int_as_float(jk0.x), jk0.y, idx0,
-                                                      any0 ? w0 : 0u, p, Hw);
-            const bool g1 = triangle_full<THETA_FULL>(dij, ij.y, dik1, wik1, __int_as_float(jk1.x), jk1.y, idx1,
-                                                      any1 ? w1 : 0u, p, Hw);
-            if (g0) push_recheck(q, slot, w0, (uint32_t)(g.a0 + i), (uint32_t)(g.b0 + j), (uint32_t)(g.c0 + kk0));
-            if (g1) push_recheck(q, slot, w1, (uint32_t)(g.a0 + i), (uint32_t)(g.b0 + j), (uint32_t)(g.c0 + kk1));
+            if ((hi >> lane) & 1u) {
+                const unsigned w = PRED == PRED_DDR ? 1u + (unsigned)((w2 >> (lane + 32)) & 1ull) : 1u;
+                cand[qn + nlo + __popc(hi & lt)] = pack_cand(j, lane + 32, w);
+            }
+            qn += nlo + __popc(hi);
+            __syncwarp();
+            if (qn >= 64) {
+                qn -= 64;
+                run_candidates<THETA_FULL>(cand + qn, 64, row_ij, row_ik, JK, p, Hw, q, slot, ia, g.b0, g.c0);
+                bn += 64;
+                __syncwarp();
+            }
+        }
+        if (qn > 0) {
+            run_candidates<THETA_FULL>(cand, qn, row_ij, row_ik, JK, p, Hw, q, slot, ia, g.b0, g.c0);
+            bn += qn;
         }
         __syncwarp();
     }
-    if (lane == 0 && evaluated) atomicAdd(q.evaluated, (unsigned long long)evaluated);
+    evaluated += ev;
+    binned += bn;
 }
 
 template <bool THETA_FULL>
 __device__ __forceinline__ void triangle_dispatch(const DevJob& J, uint4 task, const TriParams& p, float4* P,
-                                                  int2* JK, int2* IJ, unsigned int* Hw, RecheckQueue& q) {
+                                                  int2* JK, int2* IJ, int2* IK, uint32_t* Q, uint32_t* KL,
+                                                  JMasks* JM, unsigned int* Hw, RecheckQueue& q,
+                                                  unsigned long long& ev, unsigned long long& bn, int* next_i) {
     switch ((task.x >> TASK_PRED_SHIFT) & 0xFF) {
-        case PRED_NONE: triangle_task_fast<PRED_NONE, THETA_FULL>(J, task, p, P, JK, IJ, Hw, q); break;
-        case PRED_DDR: triangle_task_fast<PRED_DDR, THETA_FULL>(J, task, p, P, JK, IJ, Hw, q); break;
-        case PRED_SAME: triangle_task_fast<PRED_SAME, THETA_FULL>(J, task, p, P, JK, IJ, Hw, q); break;
-        default: triangle_task_fast<PRED_ONE, THETA_FULL>(J, task, p, P, JK, IJ, Hw, q); break;
+        case PRED_NONE: triangle_task_fast<PRED_NONE, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, KL, JM, Hw, q, ev, bn, next_i); break;
+        case PRED_DDR: triangle_task_fast<PRED_DDR, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, KL, JM, Hw, q, ev, bn, next_i); break;
+        case PRED_SAME: triangle_task_fast<PRED_SAME, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, KL, JM, Hw, q, ev, bn, next_i); break;
+        default: triangle_task_fast<PRED_ONE, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, KL, JM, Hw, q, ev, bn, next_i); break;
     }
 }
 
+#ifndef TRI_MIN_BLOCKS
+#define TRI_MIN_BLOCKS 3
+#endif
 template <bool THETA_FULL>
-__global__ void __launch_bounds__(TRI_THREADS, 2)
+__global__ void __launch_bounds__(TRI_THREADS, TRI_MIN_BLOCKS)
 triangle_fast_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ tasks, unsigned int ntasks,
                      unsigned int* task_counter, TriParams p, RecheckQueue q, int copies) {
     extern __shared__ __align__(16) unsigned char smem[];
     float4* P = reinterpret_cast<float4*>(smem);
     int2* JK = reinterpret_cast<int2*>(smem + 3 * TILE * sizeof(float4));
     int2* IJ = JK + TILE * TILE;
-    unsigned int* H = reinterpret_cast<unsigned int*>(IJ + TRI_WARPS * TILE);
+    int2* IK = IJ + TRI_WARPS * TILE;
+    uint32_t* Q = reinterpret_cast<uint32_t*>(IK + TRI_WARPS * TILE);
+    uint32_t* KL = Q + TRI_WARPS * TRI_QCAP;
+    JMasks* JM = reinterpret_cast<JMasks*>(KL + TRI_WARPS * TILE);
+    unsigned int* H = reinterpret_cast<unsigned int*>(JM + TILE);
     __shared__ uint4 s_task;
+    __shared__ int s_next_i;
     for (int b = threadIdx.x; b < copies * p.len; b += blockDim.x) H[b] = 0;
     unsigned int* Hw = H + ((threadIdx.x >> 5) % copies) * p.len;
     int cur = -1;
     unsigned int since = 0;
+    unsigned long long ev = 0, bn = 0;
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -463,7 +605,11 @@ triangle_fast_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ 
         cur = slot;
         if (slot < 0) break;
         since++;
-        triangle_dispatch<THETA_FULL>(jobs[slot], task, p, P, JK, IJ, Hw, q);
+        triangle_dispatch<THETA_FULL>(jobs[slot], task, p, P, JK, IJ, IK, Q, KL, JM, Hw, q, ev, bn, &s_next_i);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (ev) atomicAdd(q.evaluated, ev);
+        if (bn) atomicAdd(q.evaluated + 1, bn);
     }
 }
 

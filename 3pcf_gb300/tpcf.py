@@ -10,7 +10,7 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_build", "libtpcf.so")
+LIB_PATH = os.environ.get("TPCF_LIB") or os.path.join(HERE, "_build", "libtpcf.so")
 BIN_DIR = os.path.join(HERE, "bin")
 
 THREE_SIDE, TRIANGLE, PAIR = 0, 1, 2
@@ -52,7 +52,8 @@ class Stats(ctypes.Structure):
     _fields_ = [("kernel_ms", ctypes.c_double), ("total_ms", ctypes.c_double), ("loop_units", ctypes.c_uint64),
                 ("evaluated_units", ctypes.c_uint64), ("recheck_units", ctypes.c_uint64),
                 ("tasks", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64),
-                ("main_kernel_ms", ctypes.c_double), ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64)]
+                ("main_kernel_ms", ctypes.c_double), ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
+                ("binned_units", ctypes.c_uint64)]
 
 
 _LIB = None

@@ -123,6 +123,7 @@ typedef struct {
     double main_kernel_ms;       /* device time of the counting kernel alone (no recheck) */
     uint64_t h2d_bytes;          /* host-to-device bytes copied since the previous tpcf_last_stats */
     uint64_t d2h_bytes;          /* device-to-host bytes copied since the previous tpcf_last_stats */
+    uint64_t binned_units;       /* triangles (pairs) that reached the full binning arithmetic */
 } tpcf_stats;
 
 typedef struct tpcf_ctx tpcf_ctx;
