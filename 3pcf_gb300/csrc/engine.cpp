@@ -103,6 +103,7 @@ struct Catalog {
 };
 
 struct View {
+    uint64_t id = 0;  // unique per view object (plan cache key)
     int64_t n = 0;
     int ntiles = 0;
     DevBuf<float4> pts;          // sorted points, .w = loop index (int bits)
@@ -481,6 +482,11 @@ struct tpcf_ctx {
     std::map<uint64_t, std::shared_ptr<DevBuf<float4>>> cat_dev;  // unsorted points (resident)
     std::map<std::tuple<uint64_t, int64_t, int64_t, int>, std::shared_ptr<View>> views;
     int tile_points = TILE;  // points per spatial tile (<= TILE)
+    uint64_t next_view_id = 0;
+    // last planned batch (see run_group)
+    std::vector<uint64_t> plan_sig;
+    size_t plan_ntasks = 0;
+    uint64_t plan_evaluated = 0;
     // acos table
     bool acos_ready = false;
     DevBuf<uint32_t> acos_keys, acos_vals, acos_bucket;
@@ -523,6 +529,7 @@ std::shared_ptr<View> get_view(tpcf_ctx* ctx, uint64_t handle, int64_t begin, in
     auto vi = ctx->views.find(key);
     if (vi != ctx->views.end()) return vi->second;
     auto v = std::make_shared<View>();
+    v->id = ++ctx->next_view_id;
     int64_t n = end - begin;
     v->n = n;
     std::vector<float> xyz(3 * (size_t)n);
@@ -609,14 +616,6 @@ inline bool close_enough(const View& a, int ta, const View& b, int tb, double lm
     return box_lower_bound(a.boxes[ta], b.boxes[tb]) < lmax;
 }
 
-std::vector<std::vector<int>> neighbours(const View& a, const View& b, double lmax) {
-    std::vector<std::vector<int>> nb(a.ntiles);
-    for (int i = 0; i < a.ntiles; i++)
-        for (int j = 0; j < b.ntiles; j++)
-            if (close_enough(a, i, b, j, lmax)) nb[i].push_back(j);
-    return nb;
-}
-
 uint64_t task_units3(const View& A, int a, const View& B, int b, const View& C, int c, uint32_t flags) {
     uint64_t na = A.h_tile_start[a + 1] - A.h_tile_start[a];
     uint64_t nb = B.h_tile_start[b + 1] - B.h_tile_start[b];
@@ -629,16 +628,48 @@ uint64_t task_units3(const View& A, int a, const View& B, int b, const View& C, 
 }
 
 // Tile tasks of one triangle/three-side job.
+// Lower/upper side bounds of every tile pair of two views, held densely when
+// small enough (else computed on demand).
+struct PairBounds {
+    const View* a = nullptr;
+    const View* b = nullptr;
+    bool dense = false;
+    std::vector<float> lb, ub;
+    void build(const View& A, const View& B) {
+        a = &A;
+        b = &B;
+        dense = (int64_t)A.ntiles * B.ntiles <= ((int64_t)1 << 24);
+        if (!dense) return;
+        lb.resize((size_t)A.ntiles * B.ntiles);
+        ub.resize(lb.size());
+        for (int i = 0; i < A.ntiles; i++)
+            for (int j = 0; j < B.ntiles; j++) {
+                // float copies rounded outwards so they stay conservative
+                lb[(size_t)i * B.ntiles + j] = nextafterf((float)box_lower_bound(A.boxes[i], B.boxes[j]), 0.f);
+                ub[(size_t)i * B.ntiles + j] = nextafterf((float)box_upper_bound(A.boxes[i], B.boxes[j]), INFINITY);
+            }
+    }
+    double L(int i, int j) const {
+        return dense ? (double)lb[(size_t)i * b->ntiles + j] : box_lower_bound(a->boxes[i], b->boxes[j]);
+    }
+    double U(int i, int j) const {
+        return dense ? (double)ub[(size_t)i * b->ntiles + j] : box_upper_bound(a->boxes[i], b->boxes[j]);
+    }
+};
+
 // Whether a tile triple can hold a counted triangle-parametrization triangle:
 // with the three pair bounds sorted (L1<=L2<=L3 lower, U1<=U2<=U3 upper) the
 // shortest side lies in [L1,U1], the middle in [L2,U2], the longest in [L3,U3];
 // permutations 0/2 need s_lo <= shortest < s_hi and middle < q_hi*shortest,
 // permutation 1 needs s_lo <= middle < s_hi and longest < q_hi*middle.
-bool tri_triple_possible(const Binning& bin, const Box& a, const Box& b, const Box& c) {
-    double L[3] = {box_lower_bound(a, b), box_lower_bound(a, c), box_lower_bound(b, c)};
-    double U[3] = {box_upper_bound(a, b), box_upper_bound(a, c), box_upper_bound(b, c)};
-    std::sort(L, L + 3);
-    std::sort(U, U + 3);
+bool tri_triple_possible(const Binning& bin, double l0, double l1, double l2, double u0, double u1, double u2) {
+    double L[3] = {l0, l1, l2}, U[3] = {u0, u1, u2};
+    if (L[0] > L[1]) std::swap(L[0], L[1]);
+    if (L[1] > L[2]) std::swap(L[1], L[2]);
+    if (L[0] > L[1]) std::swap(L[0], L[1]);
+    if (U[0] > U[1]) std::swap(U[0], U[1]);
+    if (U[1] > U[2]) std::swap(U[1], U[2]);
+    if (U[0] > U[1]) std::swap(U[0], U[1]);
     bool p0 = L[0] < bin.s_hi && U[0] >= bin.s_lo && L[1] < bin.q_hi * U[0];
     bool p1 = L[1] < bin.s_hi && U[1] >= bin.s_lo && L[2] < bin.q_hi * U[1];
     return p0 || p1;
@@ -649,32 +680,45 @@ void plan_triplets(const tpcf_spec& sp, const PlannedJob& pj, uint32_t slot, con
     const double lmax = bin.lmax;
     const View &A = *pj.v[0], &B = *pj.v[1], &C = *pj.v[2];
     const bool sameAB = pj.v[0] == pj.v[1], sameBC = pj.v[1] == pj.v[2];
+    if (A.ntiles == 0 || B.ntiles == 0 || C.ntiles == 0) return;
+    const bool prune = lmax < INFINITY;
+    PairBounds bAB, bAC, bBC;
+    if (prune) {
+        bAB.build(A, B);
+        bAC.build(A, C);
+        bBC.build(B, C);
+    }
     auto add = [&](int a, int b, int c, uint32_t pred, uint32_t flags) {
-        if (bin.tri_prune && !tri_triple_possible(bin, A.boxes[a], B.boxes[b], C.boxes[c])) return;
+        if (prune) {
+            double lab = bAB.L(a, b), lac = bAC.L(a, c), lbc = bBC.L(b, c);
+            if (!(lbc < lmax)) return;
+            if (bin.tri_prune &&
+                !tri_triple_possible(bin, lab, lac, lbc, bAB.U(a, b), bAC.U(a, c), bBC.U(b, c)))
+                return;
+        }
         uint64_t u = task_units3(A, a, B, b, C, c, flags);
         if (u == 0) return;
         evaluated += u;
         tasks.push_back({u, make_uint4(slot | (pred << TASK_PRED_SHIFT) | flags, (uint32_t)a, (uint32_t)b,
                                        (uint32_t)c)});
     };
-    if (A.ntiles == 0 || B.ntiles == 0 || C.ntiles == 0) return;
-    auto nAB = neighbours(A, B, lmax);
-    auto nAC = neighbours(A, C, lmax);
-    std::vector<std::vector<char>> okBC;
-    const bool prune = lmax < INFINITY;
-    if (prune) {
-        okBC.assign(B.ntiles, std::vector<char>(C.ntiles, 0));
-        for (int b = 0; b < B.ntiles; b++)
-            for (int c = 0; c < C.ntiles; c++) okBC[b][c] = close_enough(B, b, C, c, lmax);
-    }
-    auto bc_ok = [&](int b, int c) { return !prune || okBC[b][c]; };
+    // neighbour lists (tile pairs whose lower bound is below lmax)
+    auto nbrs = [&](const View& X, const View& Y, const PairBounds& pb) {
+        std::vector<std::vector<int>> nb(X.ntiles);
+        for (int i = 0; i < X.ntiles; i++)
+            for (int j = 0; j < Y.ntiles; j++)
+                if (!prune || pb.L(i, j) < lmax) nb[i].push_back(j);
+        return nb;
+    };
+    auto nAB = nbrs(A, B, bAB);
+    auto nAC = nbrs(A, C, bAC);
     if (sp.kind == TPCF_TRIANGLE && sp.loop == TPCF_LOOP_SAME && sameAB && sameBC) {
         // i <= j <= k over one array: unordered distinct triples
         for (int a = 0; a < A.ntiles; a++)
             for (int b : nAB[a]) {
                 if (b < a) continue;
                 for (int c : nAC[a]) {
-                    if (c < b || !bc_ok(b, c)) continue;
+                    if (c < b) continue;
                     uint32_t f = (a == b ? TASK_DIAG_IJ : 0) | (b == c ? TASK_DIAG_JK : 0);
                     add(a, b, c, PRED_NONE, f);
                 }
@@ -684,7 +728,7 @@ void plan_triplets(const tpcf_spec& sp, const PlannedJob& pj, uint32_t slot, con
         for (int a = 0; a < A.ntiles; a++)
             for (int b : nAB[a])
                 for (int c : nAC[a]) {
-                    if (c < b || !bc_ok(b, c)) continue;
+                    if (c < b) continue;
                     add(a, b, c, PRED_NONE, b == c ? TASK_DIAG_JK : 0);
                 }
     } else if (sp.kind == TPCF_TRIANGLE && sp.loop == TPCF_LOOP_ONE && sameAB) {
@@ -693,18 +737,14 @@ void plan_triplets(const tpcf_spec& sp, const PlannedJob& pj, uint32_t slot, con
         for (int a = 0; a < A.ntiles; a++)
             for (int b : nAB[a]) {
                 if (b < a) continue;
-                for (int c : nAC[a]) {
-                    if (!bc_ok(b, c)) continue;
-                    add(a, b, c, PRED_DDR, a == b ? TASK_DIAG_IJ : 0);
-                }
+                for (int c : nAC[a]) add(a, b, c, PRED_DDR, a == b ? TASK_DIAG_IJ : 0);
             }
     } else {
         uint32_t pred = PRED_NONE;
         if (sp.kind == TPCF_TRIANGLE) pred = sp.loop == TPCF_LOOP_SAME ? PRED_SAME : sp.loop == TPCF_LOOP_ONE ? PRED_ONE : PRED_NONE;
         for (int a = 0; a < A.ntiles; a++)
             for (int b : nAB[a])
-                for (int c : nAC[a])
-                    if (bc_ok(b, c)) add(a, b, c, pred, 0);
+                for (int c : nAC[a]) add(a, b, c, pred, 0);
     }
 }
 
@@ -755,42 +795,88 @@ void run_group(tpcf_ctx* ctx, const std::vector<GroupJob>& group) {
     if (group.size() > 0xFFFF) throw InvalidArg{"too many jobs in one batch"};
     std::vector<PlannedJob> pj(group.size());
     std::vector<DevJob> dj(group.size());
-    std::vector<std::pair<uint64_t, uint4>> tasks;
     uint64_t evaluated = 0, units = 0;
     size_t hist_total = (size_t)bin.len * group.size();
     ctx->d_hist.reserve(hist_total);
+    // signature of the batch: a repeated batch over the same resident views
+    // reuses its task list and device upload
+    std::vector<uint64_t> sig;
+    sig.push_back((uint64_t)(uintptr_t)ctx->d_hist.p);
     for (size_t g = 0; g < group.size(); g++) {
         const tpcf_job& job = *group[g].job;
+        const tpcf_spec& jsp = *group[g].spec;  // same binning as sp; the loop nest may differ
         int64_t n[3] = {0, 0, 0};
         for (int r = 0; r < ncat; r++) {
             pj[g].v[r] = get_view(ctx, job.catalog[r], job.begin[r], job.end[r]);
             n[r] = pj[g].v[r]->n;
         }
         if (ncat == 2) pj[g].v[2] = pj[g].v[1];
-        const tpcf_spec& jsp = *group[g].spec;  // same binning as sp; the loop nest may differ
         pj[g].loop_units = loop_units(jsp.kind, jsp.loop, n);
         units += pj[g].loop_units;
         for (int r = 0; r < 3; r++) {
             dj[g].pts[r] = pj[g].v[r]->pts.p;
             dj[g].tile_start[r] = pj[g].v[r]->tile_start.p;
+            sig.push_back(pj[g].v[r]->id);
         }
         dj[g].hist = ctx->d_hist.p + (size_t)bin.len * g;
-        if (jsp.kind == TPCF_PAIR) plan_pairs(jsp, pj[g], (uint32_t)g, bin.lmax, tasks, evaluated);
-        else plan_triplets(jsp, pj[g], (uint32_t)g, bin, tasks, evaluated);
+        uint64_t f[6] = {(uint64_t)jsp.kind, (uint64_t)jsp.loop, (uint64_t)jsp.prune, (uint64_t)jsp.precision,
+                         (uint64_t)jsp.nan_policy, (uint64_t)jsp.overflow};
+        sig.insert(sig.end(), f, f + 6);
+        for (int a = 0; a < 3; a++) {
+            sig.push_back((uint64_t)fbits(jsp.axis[a].lo) << 32 | fbits(jsp.axis[a].hi));
+            sig.push_back((uint64_t)(uint32_t)jsp.axis[a].nbins);
+        }
     }
-    // largest tasks first (dynamic fetch then balances the tail)
-    std::stable_sort(tasks.begin(), tasks.end(),
-                     [](const std::pair<uint64_t, uint4>& a, const std::pair<uint64_t, uint4>& b) { return a.first > b.first; });
-    std::vector<uint4> h_tasks(tasks.size());
-    for (size_t i = 0; i < tasks.size(); i++) h_tasks[i] = tasks[i].second;
-    ctx->d_jobs.reserve(dj.size());
-    ctx->d_tasks.reserve(std::max<size_t>(h_tasks.size(), 1));
-    ctx->d_counters.reserve(8);
     cudaStream_t st = ctx->stream;
-    CK(cudaMemcpyAsync(ctx->d_jobs.p, dj.data(), dj.size() * sizeof(DevJob), cudaMemcpyHostToDevice, st));
-    ctx->h2d += dj.size() * sizeof(DevJob) + h_tasks.size() * sizeof(uint4);
-    if (!h_tasks.empty())
-        CK(cudaMemcpyAsync(ctx->d_tasks.p, h_tasks.data(), h_tasks.size() * sizeof(uint4), cudaMemcpyHostToDevice, st));
+    ctx->d_counters.reserve(8);
+    size_t ntasks = 0;
+    if (sig == ctx->plan_sig) {
+        ntasks = ctx->plan_ntasks;
+        evaluated = ctx->plan_evaluated;
+    } else {
+        // plan the jobs in parallel (one host thread per job, bounded)
+        std::vector<std::vector<std::pair<uint64_t, uint4>>> part(group.size());
+        std::vector<uint64_t> part_eval(group.size(), 0);
+        std::atomic<size_t> next(0);
+        auto worker = [&]() {
+            for (;;) {
+                size_t g = next.fetch_add(1);
+                if (g >= group.size()) break;
+                const tpcf_spec& jsp = *group[g].spec;
+                if (jsp.kind == TPCF_PAIR) plan_pairs(jsp, pj[g], (uint32_t)g, bin.lmax, part[g], part_eval[g]);
+                else plan_triplets(jsp, pj[g], (uint32_t)g, bin, part[g], part_eval[g]);
+            }
+        };
+        size_t nth = std::min<size_t>(group.size(), std::max(1u, std::thread::hardware_concurrency()));
+        if (nth <= 1) {
+            worker();
+        } else {
+            std::vector<std::thread> th;
+            for (size_t t = 0; t < nth; t++) th.emplace_back(worker);
+            for (auto& t : th) t.join();
+        }
+        std::vector<std::pair<uint64_t, uint4>> tasks;
+        for (size_t g = 0; g < group.size(); g++) {
+            evaluated += part_eval[g];
+            tasks.insert(tasks.end(), part[g].begin(), part[g].end());
+        }
+        // largest tasks first (dynamic fetch then balances the tail)
+        std::stable_sort(tasks.begin(), tasks.end(),
+                         [](const std::pair<uint64_t, uint4>& a, const std::pair<uint64_t, uint4>& b) { return a.first > b.first; });
+        std::vector<uint4> h_tasks(tasks.size());
+        for (size_t i = 0; i < tasks.size(); i++) h_tasks[i] = tasks[i].second;
+        ntasks = h_tasks.size();
+        ctx->d_jobs.reserve(dj.size());
+        ctx->d_tasks.reserve(std::max<size_t>(h_tasks.size(), 1));
+        CK(cudaMemcpyAsync(ctx->d_jobs.p, dj.data(), dj.size() * sizeof(DevJob), cudaMemcpyHostToDevice, st));
+        ctx->h2d += dj.size() * sizeof(DevJob) + h_tasks.size() * sizeof(uint4);
+        if (!h_tasks.empty())
+            CK(cudaMemcpyAsync(ctx->d_tasks.p, h_tasks.data(), h_tasks.size() * sizeof(uint4), cudaMemcpyHostToDevice, st));
+        CK(cudaStreamSynchronize(st));
+        ctx->plan_sig = sig;
+        ctx->plan_ntasks = ntasks;
+        ctx->plan_evaluated = evaluated;
+    }
     const bool fp64 = sp.precision == TPCF_PLAIN_FP64;
     if (sp.kind == TPCF_TRIANGLE) ensure_acos(ctx);
     uint64_t launches = 0;
@@ -800,7 +886,7 @@ void run_group(tpcf_ctx* ctx, const std::vector<GroupJob>& group) {
         CK(cudaMemsetAsync(ctx->d_hist.p, 0, hist_total * sizeof(unsigned long long), st));
         CK(cudaMemsetAsync(ctx->d_counters.p, 0, 8 * sizeof(unsigned int), st));
         CK(cudaEventRecord(ctx->ev0, st));
-        unsigned int nt = (unsigned int)h_tasks.size();
+        unsigned int nt = (unsigned int)ntasks;
         launches = 0;
         if (sp.kind == TPCF_TRIANGLE) {
             // warp-private histogram copies, as many as still let three CTAs
@@ -879,7 +965,7 @@ void run_group(tpcf_ctx* ctx, const std::vector<GroupJob>& group) {
     // triangle of their tasks
     ctx->stats.evaluated_units = (sp.kind == TPCF_TRIANGLE && !fp64) ? dev_evaluated : evaluated;
     ctx->stats.binned_units = (sp.kind == TPCF_TRIANGLE && !fp64) ? dev_binned : evaluated;
-    ctx->stats.tasks = h_tasks.size();
+    ctx->stats.tasks = ntasks;
     ctx->stats.kernel_launches = launches;
     ctx->stats.total_ms =
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_wall0).count();
