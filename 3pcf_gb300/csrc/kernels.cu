@@ -20,6 +20,9 @@
 #include <limits.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
+#include "../../include/tpcf.h"
 #include "engine.h"
 #include "exact_acos.h"
 
@@ -982,3 +985,151 @@ cudaError_t launch_acos_check(AcosTable t, uint32_t key_begin, uint32_t count, u
 }
 
 }  // namespace tpcf
+
+// ===========================================================================
+// Pair counts without any device allocation.
+//
+// For callers that cannot call cudaMalloc -- code running inside a framework
+// that owns all device memory through its own pool, or a library that must not
+// grow the process's footprint behind its host application's back.  They pass
+// device pointers to their catalogs and to the output histogram; every other
+// buffer the count needs (packed points, tile table, job descriptor, task
+// counter) is the file-scope array below, which exists on every device that
+// loads this library until the process exits.
+//
+// Limits and sharing: at most NOALLOC_MAX_POINTS points per catalog; all calls
+// on a device share the array, so calls whose work overlaps on the GPU (two
+// streams, or two host threads) race and must be serialised by the caller.
+// The array keeps the previous call's contents; everything that must start
+// from zero (task counter, output histogram) is cleared by the call itself.
+// ===========================================================================
+
+namespace tpcf {
+
+constexpr int64_t NOALLOC_MAX_POINTS = 1 << 18;             // per catalog
+constexpr int NOALLOC_MAX_TILES = (int)(NOALLOC_MAX_POINTS / TILE);
+
+struct NoAllocScratch {
+    float4 pts[2][NOALLOC_MAX_POINTS];        // 2 x 4 MiB
+    int32_t tile_start[2][NOALLOC_MAX_TILES + 1];
+    DevJob job;
+    unsigned int task_counter;
+};
+static __device__ __align__(256) NoAllocScratch g_noalloc;  // 8 MiB per device
+
+// packs SoA catalogs into the scratch points (.w = loop index), fills the tile
+// table, resets the task counter
+__global__ void noalloc_prepare(const float* x0, const float* y0, const float* z0, int n0, const float* x1,
+                                const float* y1, const float* z1, int n1, unsigned long long* hist) {
+    NoAllocScratch* S = &g_noalloc;
+    const int stride = gridDim.x * blockDim.x;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int i = tid; i < n0; i += stride) S->pts[0][i] = make_float4(x0[i], y0[i], z0[i], __int_as_float(i));
+    for (int i = tid; i < n1; i += stride) S->pts[1][i] = make_float4(x1[i], y1[i], z1[i], __int_as_float(i));
+    const int t0 = (n0 + TILE - 1) / TILE, t1 = (n1 + TILE - 1) / TILE;
+    for (int t = tid; t <= t0; t += stride) S->tile_start[0][t] = min(t * TILE, n0);
+    for (int t = tid; t <= t1; t += stride) S->tile_start[1][t] = min(t * TILE, n1);
+    if (tid == 0) {
+        S->job.pts[0] = S->pts[0];
+        S->job.pts[1] = S->pts[1];
+        S->job.pts[2] = S->pts[1];
+        S->job.tile_start[0] = S->tile_start[0];
+        S->job.tile_start[1] = S->tile_start[1];
+        S->job.tile_start[2] = S->tile_start[1];
+        S->job.hist = hist;
+        S->task_counter = 0u;
+    }
+}
+
+// pair_kernel with tile-pair tasks computed from the counter value (no task
+// list): task t is tile pair (t / ntB, t % ntB); 'same' enumerates only a <= b
+// of one catalog with j >= i inside the diagonal tile
+template <bool FP64>
+__global__ void __launch_bounds__(PR_THREADS)
+pair_kernel_noalloc(unsigned int* task_counter, int ntA, int ntB, int same, int pred_same, PairParams p, int copies) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    float4* P = reinterpret_cast<float4*>(smem);
+    unsigned int* H = reinterpret_cast<unsigned int*>(smem + PR_SMEM_FIXED);
+    __shared__ unsigned int s_t;
+    const DevJob& J = g_noalloc.job;
+    for (int b = threadIdx.x; b < copies * p.n; b += blockDim.x) H[b] = 0;
+    unsigned int* Hw = H + ((threadIdx.x >> 5) % copies) * p.n;
+    const unsigned int ntasks = (unsigned int)ntA * (unsigned int)ntB;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_t = atomicAdd(task_counter, 1u);
+        __syncthreads();
+        const unsigned int t = s_t;
+        if (t >= ntasks) break;
+        const unsigned int a = t / (unsigned int)ntB, b = t % (unsigned int)ntB;
+        if (same && b < a) continue;
+        uint4 task = make_uint4((same && a == b ? TASK_DIAG_IJ : 0u), a, b, 0u);
+        if (pred_same) pair_task<FP64, PRED_SAME>(J, task, p, P, Hw);
+        else pair_task<FP64, PRED_NONE>(J, task, p, P, Hw);
+    }
+    flush_hist(H, copies, p.n, J.hist);
+}
+
+}  // namespace tpcf
+
+namespace {
+struct NoAllocDevice {
+    bool ready = false;
+    void* scratch = nullptr;
+};
+NoAllocDevice g_noalloc_dev[64];
+}  // namespace
+
+// Declared in include/tpcf.h.  The first call on a device resolves the device
+// address of the scratch array (cudaGetSymbolAddress) with that device
+// current; make that first call outside any stream capture.
+extern "C" int32_t tpcf_pair_count_noalloc(const float* x0, const float* y0, const float* z0, int64_t n0,
+                                           const float* x1, const float* y1, const float* z1, int64_t n1,
+                                           int32_t loop, float lo, float hi, int32_t nbins, uint64_t* hist_out,
+                                           void* stream) {
+    using namespace tpcf;
+    unsigned long long* hist = reinterpret_cast<unsigned long long*>(hist_out);
+    if (n0 < 0 || n1 < 0 || n0 > NOALLOC_MAX_POINTS || n1 > NOALLOC_MAX_POINTS) return TPCF_ERR_INVALID;
+    if (!hist || nbins <= 0 || !(hi > lo)) return TPCF_ERR_INVALID;
+    if ((n0 > 0 && (!x0 || !y0 || !z0)) || (n1 > 0 && (!x1 || !y1 || !z1))) return TPCF_ERR_INVALID;
+    if (loop != TPCF_LOOP_ALL && loop != TPCF_LOOP_SAME && loop != TPCF_LOOP_ONE) return TPCF_ERR_INVALID;
+    int copies = 8;
+    while (copies > 1 && pair_smem_bytes(nbins, copies) > 200 * 1024) copies /= 2;
+    if (pair_smem_bytes(nbins, copies) > 227 * 1024) return TPCF_ERR_INVALID;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return TPCF_ERR_NO_DEVICE;
+    NoAllocDevice& D = g_noalloc_dev[dev];
+    if (!D.ready) {
+        if (cudaGetSymbolAddress(&D.scratch, g_noalloc) != cudaSuccess || !D.scratch) {
+            cudaGetLastError();
+            return TPCF_ERR_CUDA;
+        }
+        D.ready = true;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    NoAllocScratch* S = (NoAllocScratch*)D.scratch;
+    unsigned int* counter = &S->task_counter;
+    if (cudaMemsetAsync(hist, 0, sizeof(unsigned long long) * (size_t)nbins, st) != cudaSuccess) return TPCF_ERR_CUDA;
+    noalloc_prepare<<<256, 256, 0, st>>>(x0, y0, z0, (int)n0, x1, y1, z1, (int)n1, hist);
+    const bool same = loop == TPCF_LOOP_SAME && x0 == x1 && y0 == y1 && z0 == z1 && n0 == n1;
+    const int pred_same = loop == TPCF_LOOP_SAME && !same;
+    const int ntA = (int)((n0 + TILE - 1) / TILE), ntB = (int)((n1 + TILE - 1) / TILE);
+    if (ntA > 0 && ntB > 0) {
+        PairParams p;
+        p.n = nbins;
+        p.lo = lo;
+        p.hi = hi;
+        volatile float span = hi - lo;
+        p.bw = span / (float)nbins;
+        size_t smem = pair_smem_bytes(nbins, copies);
+        if (cudaFuncSetAttribute(pair_kernel_noalloc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+            return TPCF_ERR_CUDA;
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        long long tasks = (long long)ntA * ntB;
+        int grid = (int)std::min<long long>(tasks, (long long)sms * 4);
+        pair_kernel_noalloc<false><<<grid, PR_THREADS, smem, st>>>(counter, ntA, ntB, same ? 1 : 0, pred_same, p, copies);
+    }
+    return cudaGetLastError() == cudaSuccess ? TPCF_OK : TPCF_ERR_CUDA;
+}

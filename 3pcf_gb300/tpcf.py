@@ -24,7 +24,7 @@ ABI_SYMBOLS = [
     "tpcf_create", "tpcf_destroy", "tpcf_last_error", "tpcf_status_string", "tpcf_abi_version",
     "tpcf_catalog_create", "tpcf_catalog_release", "tpcf_resident_bytes", "tpcf_hist_len", "tpcf_count",
     "tpcf_count_batch", "tpcf_submit", "tpcf_wait", "tpcf_cancel", "tpcf_last_stats", "tpcf_loop_units",
-    "tpcf_read_catalog",
+    "tpcf_read_catalog", "tpcf_pair_count_noalloc",
 ]
 
 
@@ -84,6 +84,9 @@ def lib():
         L.tpcf_loop_units.argtypes = [P, ctypes.POINTER(Spec), ctypes.POINTER(Job), ctypes.POINTER(ctypes.c_uint64)]
         L.tpcf_read_catalog.argtypes = [ctypes.c_char_p, ctypes.c_int32, ctypes.c_float, P, P, P,
                                         ctypes.POINTER(ctypes.c_int64)]
+        L.tpcf_pair_count_noalloc.restype = ctypes.c_int32
+        L.tpcf_pair_count_noalloc.argtypes = [P, P, P, ctypes.c_int64, P, P, P, ctypes.c_int64, ctypes.c_int32,
+                                              ctypes.c_float, ctypes.c_float, ctypes.c_int32, P, P]
         L.tpcf_debug_acos_selfcheck.restype = ctypes.c_int64
         L.tpcf_debug_acos_selfcheck.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
         _LIB = L

@@ -176,6 +176,29 @@ tpcf_status tpcf_last_stats(tpcf_ctx* ctx, tpcf_stats* stats);
  * reference's numcalc / fake_tot counter (:520, src/3pcf_C_version.cc:429). */
 tpcf_status tpcf_loop_units(tpcf_ctx* ctx, const tpcf_spec* spec, const tpcf_job* job, uint64_t* units);
 
+/* ---- pair counts without device allocation -------------------------------- */
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory themselves or let a library do so -- e.g. code inside a framework
+ * whose memory pool owns the whole device, or a plugin that must not change its
+ * host application's device footprint.  It counts the same pair histogram as
+ * tpcf_count with TPCF_PAIR (same loop nests, bit-identical counts) from device
+ * arrays x0/y0/z0 (n0 points) and x1/y1/z1 (n1 points), writing nbins counts to
+ * the device array hist, and calls no cudaMalloc or cudaFree: its working
+ * buffers are one 8 MiB array per device, reserved when the library is loaded
+ * and held until the process exits.
+ *   - at most 262144 points per catalog (TPCF_ERR_INVALID beyond);
+ *   - loop TPCF_LOOP_SAME with identical pointers and sizes counts j >= i of
+ *     one catalog; with different arrays it compares loop indices;
+ *   - the first call on a device looks up that array's device address, with
+ *     the device current; make that first call before any stream capture;
+ *   - calls share the array: calls that overlap on the GPU (other streams or
+ *     host threads) race; the call clears the counter and hist it needs;
+ *   - asynchronous on 'stream' (a cudaStream_t, or NULL for the default stream). */
+tpcf_status tpcf_pair_count_noalloc(const float* x0, const float* y0, const float* z0, int64_t n0,
+                                    const float* x1, const float* y1, const float* z1, int64_t n1,
+                                    int32_t loop, float lo, float hi, int32_t nbins, uint64_t* hist,
+                                    void* stream);
+
 /* ---- reference catalog files ---------------------------------------------- */
 /* Read a catalog file exactly as the reference's fscanf loops do.
  * format 0: header-count "N" then "x y z" lines, divided by scale_factor in
