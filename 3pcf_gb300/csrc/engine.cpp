@@ -1369,3 +1369,66 @@ int64_t tpcf_debug_acos_selfcheck(tpcf_ctx* ctx, int64_t* table_size) {
 }
 
 }  // extern "C"
+
+// test hook (not in the public header): size and FNV-1a hash of this host's
+// exact-acosf exception table (built or loaded from the cache; no GPU needed)
+extern "C" int32_t tpcf_debug_acos_table_hash(uint64_t* n, uint64_t* hash) {
+    AcosHost h = load_or_build_acos_table();
+    uint64_t x = 1469598103934665603ull;
+    for (size_t i = 0; i < h.keys.size(); i++) {
+        x = (x ^ h.keys[i]) * 1099511628211ull;
+        x = (x ^ h.vals[i]) * 1099511628211ull;
+    }
+    if (n) *n = h.keys.size();
+    if (hash) *hash = x;
+    return TPCF_OK;
+}
+
+// test hook (not in the public header): this host's exact-acosf exceptions as
+// keys (float bits of c, sorted) and the direction (+1/-1 ulp) of glibc's value
+// relative to (float)tpcf_acos_d(c).  Call with keys == NULL for the count.
+extern "C" int32_t tpcf_debug_acos_exceptions(uint32_t* keys, int8_t* dir, uint64_t cap, uint64_t* n) {
+    AcosHost h = load_or_build_acos_table();
+    if (n) *n = h.keys.size();
+    if (!keys || !dir) return TPCF_OK;
+    for (size_t i = 0; i < h.keys.size() && i < cap; i++) {
+        keys[i] = h.keys[i];
+        int64_t d = (int64_t)h.vals[i] - (int64_t)fbits((float)tpcf_acos_d((double)ffrom(h.keys[i])));
+        dir[i] = (int8_t)(d > 0 ? 1 : (d < 0 ? -1 : 0));
+    }
+    return TPCF_OK;
+}
+
+// test hook (not in the public header): replaces the context's exception table
+// by the given one (e.g. another machine's glibc, to compare with files that
+// machine produced).  dir: +1/-1 ulp relative to (float)tpcf_acos_d(c).
+extern "C" int32_t tpcf_debug_set_acos_exceptions(tpcf_ctx* ctx, const uint32_t* keys, const int8_t* dir, uint64_t n) {
+    if (!ctx || (n && (!keys || !dir))) return TPCF_ERR_INVALID;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    return guarded(ctx, [&] {
+        CK(cudaSetDevice(ctx->device));
+        AcosHost h;
+        h.keys.assign(keys, keys + n);
+        h.vals.resize(n);
+        for (uint64_t i = 0; i < n; i++) {
+            if (i && keys[i] <= keys[i - 1]) throw InvalidArg{"exception keys must be strictly increasing"};
+            h.vals[i] = fbits((float)tpcf_acos_d((double)ffrom(keys[i]))) + (uint32_t)(int32_t)dir[i];
+        }
+        h.bucket.assign(65537, 0);
+        size_t j = 0;
+        for (uint32_t b = 0; b <= 65536; b++) {
+            while (j < h.keys.size() && (h.keys[j] >> 16) < b) j++;
+            h.bucket[b] = (uint32_t)j;
+        }
+        ctx->acos_n = (uint32_t)n;
+        ctx->acos_keys.reserve(std::max<size_t>(n, 1));
+        ctx->acos_vals.reserve(std::max<size_t>(n, 1));
+        ctx->acos_bucket.reserve(65537);
+        if (n) {
+            CK(cudaMemcpy(ctx->acos_keys.p, h.keys.data(), n * 4, cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(ctx->acos_vals.p, h.vals.data(), n * 4, cudaMemcpyHostToDevice));
+        }
+        CK(cudaMemcpy(ctx->acos_bucket.p, h.bucket.data(), 65537 * 4, cudaMemcpyHostToDevice));
+        ctx->acos_ready = true;
+    });
+}

@@ -87,6 +87,8 @@ def lib():
         L.tpcf_pair_count_noalloc.restype = ctypes.c_int32
         L.tpcf_pair_count_noalloc.argtypes = [P, P, P, ctypes.c_int64, P, P, P, ctypes.c_int64, ctypes.c_int32,
                                               ctypes.c_float, ctypes.c_float, ctypes.c_int32, P, P]
+        L.tpcf_debug_set_acos_exceptions.restype = ctypes.c_int32
+        L.tpcf_debug_set_acos_exceptions.argtypes = [P, P, P, ctypes.c_uint64]
         L.tpcf_debug_acos_selfcheck.restype = ctypes.c_int64
         L.tpcf_debug_acos_selfcheck.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
         _LIB = L
@@ -218,6 +220,14 @@ class Engine:
         b = ctypes.c_int64()
         self._check(lib().tpcf_resident_bytes(self._ctx, ctypes.byref(b)), "resident_bytes")
         return b.value
+
+    def set_acos_exceptions(self, keys, up):
+        """Test hook: use another machine's glibc acosf (exception keys sorted,
+        up[i] True when glibc rounds one ulp above (float)tpcf_acos_d)."""
+        keys = np.ascontiguousarray(keys, dtype=np.uint32)
+        dirs = np.where(np.asarray(up, dtype=bool), 1, -1).astype(np.int8)
+        self._check(lib().tpcf_debug_set_acos_exceptions(self._ctx, keys.ctypes.data, dirs.ctypes.data, len(keys)),
+                    "set_acos_exceptions")
 
     def acos_selfcheck(self):
         n = ctypes.c_int64()

@@ -149,3 +149,13 @@ def flags_scale(flags):
     if "-m" in flags:
         return 3437.74677
     return 1.0
+
+
+def x86_acos_exceptions():
+    """The x86-64 glibc 2.39 acosf exception table (keys, up flags) the
+    reference's golden files were made with (tests/golden/make_acos_fixture.py)."""
+    z = np.load(os.path.join(GOLDEN, "acosf_exceptions_x86_64_glibc2.39.npz"))
+    n = int(z["n"])
+    keys = np.cumsum(z["key_deltas"].astype(np.int64)).astype(np.uint32)
+    up = np.unpackbits(z["up_bits"])[:n].astype(bool)
+    return keys, up

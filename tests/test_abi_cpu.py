@@ -104,3 +104,24 @@ def test_cli_without_gpu_fails_loudly(tmp_path):
     assert r.returncode == 2
     assert "no CUDA device" in r.stderr
     assert not (tmp_path / "o.dat").exists()
+
+
+def test_x86_acos_fixture_matches_this_host():
+    """The committed x86-64 glibc acosf table equals an exhaustive scan of this
+    machine's libm when this machine is x86-64 with glibc 2.39."""
+    import platform
+    libc = ctypes.CDLL("libc.so.6")
+    libc.gnu_get_libc_version.restype = ctypes.c_char_p
+    if platform.machine() != "x86_64" or libc.gnu_get_libc_version().decode() != "2.39":
+        pytest.skip("fixture is for x86-64 glibc 2.39")
+    L = tpcf.lib()
+    n = ctypes.c_uint64()
+    L.tpcf_debug_acos_exceptions(None, None, ctypes.c_uint64(0), ctypes.byref(n))
+    keys = np.zeros(n.value, dtype=np.uint32)
+    dirs = np.zeros(n.value, dtype=np.int8)
+    L.tpcf_debug_acos_exceptions(keys.ctypes.data_as(ctypes.c_void_p), dirs.ctypes.data_as(ctypes.c_void_p),
+                                 ctypes.c_uint64(n.value), ctypes.byref(n))
+    fk, fu = rf.x86_acos_exceptions()
+    assert np.array_equal(keys, fk)
+    assert np.array_equal(dirs > 0, fu)
+    assert np.all(np.abs(dirs) == 1)
