@@ -452,8 +452,42 @@ uint64_t loop_units(int kind, int loop, const int64_t n[3]) {
 // ---------------------------------------------------------------------------
 // context
 
+// One lane = one stream with its own scratch buffers.  The synchronous API uses
+// lane 0; every serving worker owns one further lane, so batches of different
+// workers run concurrently on the device.
+struct Lane {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_mid = nullptr;
+    uint64_t h2d = 0, d2h = 0;  // bytes copied since the last stats read
+    DevBuf<DevJob> d_jobs;
+    DevBuf<uint4> d_tasks;
+    DevBuf<unsigned int> d_counters;  // [0] task counter, [1] recheck count, [2..5] evaluated/binned
+    DevBuf<uint4> d_queue;
+    DevBuf<unsigned long long> d_hist;
+    std::vector<unsigned long long> h_hist;
+    // last planned batch (see run_group)
+    std::vector<uint64_t> plan_sig;
+    size_t plan_ntasks = 0;
+    uint64_t plan_evaluated = 0;
+    tpcf_stats stats{};
+    void release() {
+        d_jobs.release();
+        d_tasks.release();
+        d_counters.release();
+        d_queue.release();
+        d_hist.release();
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (ev_mid) cudaEventDestroy(ev_mid);
+        if (stream) cudaStreamDestroy(stream);
+        ev0 = ev1 = ev_mid = nullptr;
+        stream = nullptr;
+    }
+};
+
 struct Pending {
     uint64_t ticket;
+    double t_submit = 0, t_start = 0, t_done = 0;  // steady-clock ms
     tpcf_spec spec;
     tpcf_job job;
     std::vector<uint64_t> result;
@@ -472,10 +506,9 @@ struct GroupJob {
 struct tpcf_ctx {
     int device = 0;
     int num_sms = 0;
-    cudaStream_t stream = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_mid = nullptr;
-    uint64_t h2d = 0, d2h = 0;  // bytes copied since the last stats reset
-    std::recursive_mutex mu;  // serialises device work on this context
+    std::recursive_mutex mu;      // serialises the synchronous API (lane 0)
+    std::recursive_mutex view_mu; // catalogs and spatial views
+    std::mutex acos_mu;
     std::string last_error;
     uint64_t next_handle = 1;
     std::map<uint64_t, std::shared_ptr<Catalog>> catalogs;
@@ -483,31 +516,21 @@ struct tpcf_ctx {
     std::map<std::tuple<uint64_t, int64_t, int64_t, int>, std::shared_ptr<View>> views;
     int tile_points = TILE;  // points per spatial tile (<= TILE)
     uint64_t next_view_id = 0;
-    // last planned batch (see run_group)
-    std::vector<uint64_t> plan_sig;
-    size_t plan_ntasks = 0;
-    uint64_t plan_evaluated = 0;
     // acos table
     bool acos_ready = false;
     DevBuf<uint32_t> acos_keys, acos_vals, acos_bucket;
     uint32_t acos_n = 0;
-    // scratch
-    DevBuf<DevJob> d_jobs;
-    DevBuf<uint4> d_tasks;
-    DevBuf<unsigned int> d_counters;  // [0] task counter, [1] recheck count
-    DevBuf<uint4> d_queue;
-    DevBuf<unsigned long long> d_hist;
-    std::vector<unsigned long long> h_hist;
-    tpcf_stats stats{};
+    std::vector<std::unique_ptr<Lane>> lanes;
     // serving
     std::mutex qmu;
     std::condition_variable qcv;
     std::deque<std::shared_ptr<Pending>> queue;
     std::map<uint64_t, std::shared_ptr<Pending>> tickets;
     uint64_t next_ticket = 1;
-    std::thread worker;
+    std::vector<std::thread> workers;
     bool stop = false;
     int64_t admit_bytes = (int64_t)8 << 30;
+    int64_t inflight_bytes = 0;  // device bytes of batches running on serving lanes
 };
 
 namespace {
@@ -518,7 +541,8 @@ tpcf_status fail(tpcf_ctx* ctx, tpcf_status s, const std::string& msg) {
     return s;
 }
 
-std::shared_ptr<View> get_view(tpcf_ctx* ctx, uint64_t handle, int64_t begin, int64_t end) {
+std::shared_ptr<View> get_view(tpcf_ctx* ctx, Lane& L, uint64_t handle, int64_t begin, int64_t end) {
+    std::lock_guard<std::recursive_mutex> vlk(ctx->view_mu);
     auto it = ctx->catalogs.find(handle);
     if (it == ctx->catalogs.end()) throw InvalidArg{"unknown catalog handle"};
     const Catalog& c = *it->second;
@@ -572,17 +596,18 @@ std::shared_ptr<View> get_view(tpcf_ctx* ctx, uint64_t handle, int64_t begin, in
         v->boxes[t] = b;
     }
     v->pts.reserve(pts.size());
-    CK(cudaMemcpyAsync(v->pts.p, pts.data(), pts.size() * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
-    ctx->h2d += pts.size() * sizeof(float4) + (v->ntiles + 1) * sizeof(int32_t);
+    CK(cudaMemcpyAsync(v->pts.p, pts.data(), pts.size() * sizeof(float4), cudaMemcpyHostToDevice, L.stream));
+    L.h2d += pts.size() * sizeof(float4) + (v->ntiles + 1) * sizeof(int32_t);
     v->tile_start.reserve(v->ntiles + 1);
     CK(cudaMemcpyAsync(v->tile_start.p, v->h_tile_start.data(), (v->ntiles + 1) * sizeof(int32_t),
-                       cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
+                       cudaMemcpyHostToDevice, L.stream));
+    CK(cudaStreamSynchronize(L.stream));
     ctx->views[key] = v;
     return v;
 }
 
 void ensure_acos(tpcf_ctx* ctx) {
+    std::lock_guard<std::mutex> alk(ctx->acos_mu);
     if (ctx->acos_ready) return;
     AcosHost h = load_or_build_acos_table();
     ctx->acos_n = (uint32_t)h.keys.size();
@@ -787,7 +812,7 @@ int occupancy_grid(tpcf_ctx* ctx, int kind, size_t smem, int fp64, uint64_t ntas
 
 // Runs one group of jobs that share kind, binning and precision in a single
 // persistent launch.  outs[i] receives hist_len counts.
-void run_group(tpcf_ctx* ctx, const std::vector<GroupJob>& group) {
+void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
     auto t_wall0 = std::chrono::steady_clock::now();
     const tpcf_spec& sp = *group[0].spec;
     Binning bin = make_binning(sp);
@@ -797,17 +822,17 @@ void run_group(tpcf_ctx* ctx, const std::vector<GroupJob>& group) {
     std::vector<DevJob> dj(group.size());
     uint64_t evaluated = 0, units = 0;
     size_t hist_total = (size_t)bin.len * group.size();
-    ctx->d_hist.reserve(hist_total);
+    L.d_hist.reserve(hist_total);
     // signature of the batch: a repeated batch over the same resident views
     // reuses its task list and device upload
     std::vector<uint64_t> sig;
-    sig.push_back((uint64_t)(uintptr_t)ctx->d_hist.p);
+    sig.push_back((uint64_t)(uintptr_t)L.d_hist.p);
     for (size_t g = 0; g < group.size(); g++) {
         const tpcf_job& job = *group[g].job;
         const tpcf_spec& jsp = *group[g].spec;  // same binning as sp; the loop nest may differ
         int64_t n[3] = {0, 0, 0};
         for (int r = 0; r < ncat; r++) {
-            pj[g].v[r] = get_view(ctx, job.catalog[r], job.begin[r], job.end[r]);
+            pj[g].v[r] = get_view(ctx, L, job.catalog[r], job.begin[r], job.end[r]);
             n[r] = pj[g].v[r]->n;
         }
         if (ncat == 2) pj[g].v[2] = pj[g].v[1];
@@ -818,7 +843,7 @@ void run_group(tpcf_ctx* ctx, const std::vector<GroupJob>& group) {
             dj[g].tile_start[r] = pj[g].v[r]->tile_start.p;
             sig.push_back(pj[g].v[r]->id);
         }
-        dj[g].hist = ctx->d_hist.p + (size_t)bin.len * g;
+        dj[g].hist = L.d_hist.p + (size_t)bin.len * g;
         uint64_t f[6] = {(uint64_t)jsp.kind, (uint64_t)jsp.loop, (uint64_t)jsp.prune, (uint64_t)jsp.precision,
                          (uint64_t)jsp.nan_policy, (uint64_t)jsp.overflow};
         sig.insert(sig.end(), f, f + 6);
@@ -827,12 +852,12 @@ void run_group(tpcf_ctx* ctx, const std::vector<GroupJob>& group) {
             sig.push_back((uint64_t)(uint32_t)jsp.axis[a].nbins);
         }
     }
-    cudaStream_t st = ctx->stream;
-    ctx->d_counters.reserve(8);
+    cudaStream_t st = L.stream;
+    L.d_counters.reserve(8);
     size_t ntasks = 0;
-    if (sig == ctx->plan_sig) {
-        ntasks = ctx->plan_ntasks;
-        evaluated = ctx->plan_evaluated;
+    if (sig == L.plan_sig) {
+        ntasks = L.plan_ntasks;
+        evaluated = L.plan_evaluated;
     } else {
         // plan the jobs in parallel (one host thread per job, bounded)
         std::vector<std::vector<std::pair<uint64_t, uint4>>> part(group.size());
@@ -866,26 +891,26 @@ void run_group(tpcf_ctx* ctx, const std::vector<GroupJob>& group) {
         std::vector<uint4> h_tasks(tasks.size());
         for (size_t i = 0; i < tasks.size(); i++) h_tasks[i] = tasks[i].second;
         ntasks = h_tasks.size();
-        ctx->d_jobs.reserve(dj.size());
-        ctx->d_tasks.reserve(std::max<size_t>(h_tasks.size(), 1));
-        CK(cudaMemcpyAsync(ctx->d_jobs.p, dj.data(), dj.size() * sizeof(DevJob), cudaMemcpyHostToDevice, st));
-        ctx->h2d += dj.size() * sizeof(DevJob) + h_tasks.size() * sizeof(uint4);
+        L.d_jobs.reserve(dj.size());
+        L.d_tasks.reserve(std::max<size_t>(h_tasks.size(), 1));
+        CK(cudaMemcpyAsync(L.d_jobs.p, dj.data(), dj.size() * sizeof(DevJob), cudaMemcpyHostToDevice, st));
+        L.h2d += dj.size() * sizeof(DevJob) + h_tasks.size() * sizeof(uint4);
         if (!h_tasks.empty())
-            CK(cudaMemcpyAsync(ctx->d_tasks.p, h_tasks.data(), h_tasks.size() * sizeof(uint4), cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(L.d_tasks.p, h_tasks.data(), h_tasks.size() * sizeof(uint4), cudaMemcpyHostToDevice, st));
         CK(cudaStreamSynchronize(st));
-        ctx->plan_sig = sig;
-        ctx->plan_ntasks = ntasks;
-        ctx->plan_evaluated = evaluated;
+        L.plan_sig = sig;
+        L.plan_ntasks = ntasks;
+        L.plan_evaluated = evaluated;
     }
     const bool fp64 = sp.precision == TPCF_PLAIN_FP64;
     if (sp.kind == TPCF_TRIANGLE) ensure_acos(ctx);
     uint64_t launches = 0;
-    unsigned int queue_cap = (unsigned int)std::max<size_t>(ctx->d_queue.n, (size_t)1 << 22);
+    unsigned int queue_cap = (unsigned int)std::max<size_t>(L.d_queue.n, (size_t)1 << 22);
     uint64_t dev_evaluated = 0, dev_binned = 0;
     for (int attempt = 0; attempt < 3; attempt++) {
-        CK(cudaMemsetAsync(ctx->d_hist.p, 0, hist_total * sizeof(unsigned long long), st));
-        CK(cudaMemsetAsync(ctx->d_counters.p, 0, 8 * sizeof(unsigned int), st));
-        CK(cudaEventRecord(ctx->ev0, st));
+        CK(cudaMemsetAsync(L.d_hist.p, 0, hist_total * sizeof(unsigned long long), st));
+        CK(cudaMemsetAsync(L.d_counters.p, 0, 8 * sizeof(unsigned int), st));
+        CK(cudaEventRecord(L.ev0, st));
         unsigned int nt = (unsigned int)ntasks;
         launches = 0;
         if (sp.kind == TPCF_TRIANGLE) {
@@ -899,20 +924,20 @@ void run_group(tpcf_ctx* ctx, const std::vector<GroupJob>& group) {
             size_t smem = triangle_smem_bytes(bin.len, copies);
             int grid = occupancy_grid(ctx, sp.kind, smem, fp64, nt);
             if (fp64) {
-                CK(launch_triangle_fp64(ctx->d_jobs.p, ctx->d_tasks.p, nt, ctx->d_counters.p, bin.tri, acos_table(ctx),
+                CK(launch_triangle_fp64(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.tri, acos_table(ctx),
                                         grid, copies, st));
-                CK(cudaEventRecord(ctx->ev_mid, st));
+                CK(cudaEventRecord(L.ev_mid, st));
                 launches = 1;
             } else {
-                ctx->d_queue.reserve(queue_cap);
+                L.d_queue.reserve(queue_cap);
                 RecheckQueue q;
-                q.items = ctx->d_queue.p;
-                q.count = ctx->d_counters.p + 1;
+                q.items = L.d_queue.p;
+                q.count = L.d_counters.p + 1;
                 q.cap = queue_cap;
-                q.evaluated = reinterpret_cast<unsigned long long*>(ctx->d_counters.p + 2);
-                CK(launch_triangle_fast(ctx->d_jobs.p, ctx->d_tasks.p, nt, ctx->d_counters.p, bin.tri, q, grid, copies, st));
-                CK(cudaEventRecord(ctx->ev_mid, st));
-                CK(launch_triangle_recheck(ctx->d_jobs.p, q, bin.tri, acos_table(ctx), ctx->num_sms * 8, st));
+                q.evaluated = reinterpret_cast<unsigned long long*>(L.d_counters.p + 2);
+                CK(launch_triangle_fast(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.tri, q, grid, copies, st));
+                CK(cudaEventRecord(L.ev_mid, st));
+                CK(launch_triangle_recheck(L.d_jobs.p, q, bin.tri, acos_table(ctx), ctx->num_sms * 8, st));
                 launches = 2;
             }
         } else if (sp.kind == TPCF_THREE_SIDE) {
@@ -921,8 +946,8 @@ void run_group(tpcf_ctx* ctx, const std::vector<GroupJob>& group) {
             while (copies > 0 && three_side_smem_bytes(bin.len, copies) > smem_cap) copies /= 2;
             size_t smem = three_side_smem_bytes(copies ? bin.len : 0, copies);
             int grid = occupancy_grid(ctx, sp.kind, smem, fp64, nt);
-            CK(launch_three_side(ctx->d_jobs.p, ctx->d_tasks.p, nt, ctx->d_counters.p, bin.three, fp64, grid, copies, st));
-            CK(cudaEventRecord(ctx->ev_mid, st));
+            CK(launch_three_side(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.three, fp64, grid, copies, st));
+            CK(cudaEventRecord(L.ev_mid, st));
             launches = 1;
         } else {
             int copies = 8;
@@ -930,19 +955,19 @@ void run_group(tpcf_ctx* ctx, const std::vector<GroupJob>& group) {
             if (pair_smem_bytes(bin.len, copies) > 227 * 1024) throw InvalidArg{"pair histogram too large"};
             size_t smem = pair_smem_bytes(bin.len, copies);
             int grid = occupancy_grid(ctx, sp.kind, smem, fp64, nt);
-            CK(launch_pairs(ctx->d_jobs.p, ctx->d_tasks.p, nt, ctx->d_counters.p, bin.pair, fp64, grid, copies, st));
-            CK(cudaEventRecord(ctx->ev_mid, st));
+            CK(launch_pairs(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.pair, fp64, grid, copies, st));
+            CK(cudaEventRecord(L.ev_mid, st));
             launches = 1;
         }
-        CK(cudaEventRecord(ctx->ev1, st));
+        CK(cudaEventRecord(L.ev1, st));
         unsigned int counters[8];
-        CK(cudaMemcpyAsync(counters, ctx->d_counters.p, sizeof(counters), cudaMemcpyDeviceToHost, st));
-        ctx->h_hist.resize(hist_total);
-        CK(cudaMemcpyAsync(ctx->h_hist.data(), ctx->d_hist.p, hist_total * sizeof(unsigned long long),
+        CK(cudaMemcpyAsync(counters, L.d_counters.p, sizeof(counters), cudaMemcpyDeviceToHost, st));
+        L.h_hist.resize(hist_total);
+        CK(cudaMemcpyAsync(L.h_hist.data(), L.d_hist.p, hist_total * sizeof(unsigned long long),
                            cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
-        ctx->d2h += sizeof(counters) + hist_total * sizeof(unsigned long long);
-        ctx->stats.recheck_units = counters[1];
+        L.d2h += sizeof(counters) + hist_total * sizeof(unsigned long long);
+        L.stats.recheck_units = counters[1];
         memcpy(&dev_evaluated, &counters[2], sizeof(dev_evaluated));
         memcpy(&dev_binned, &counters[4], sizeof(dev_binned));
         if (sp.kind == TPCF_TRIANGLE && !fp64 && counters[1] > queue_cap) {
@@ -953,21 +978,21 @@ void run_group(tpcf_ctx* ctx, const std::vector<GroupJob>& group) {
         break;
     }
     float ms = 0, ms_main = 0;
-    CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
-    CK(cudaEventElapsedTime(&ms_main, ctx->ev0, ctx->ev_mid));
-    ctx->stats.main_kernel_ms = ms_main;
+    CK(cudaEventElapsedTime(&ms, L.ev0, L.ev1));
+    CK(cudaEventElapsedTime(&ms_main, L.ev0, L.ev_mid));
+    L.stats.main_kernel_ms = ms_main;
     for (size_t g = 0; g < group.size(); g++)
-        memcpy(group[g].out, ctx->h_hist.data() + (size_t)bin.len * g, (size_t)bin.len * sizeof(uint64_t));
-    ctx->stats.kernel_ms = ms;
-    ctx->stats.loop_units = units;
+        memcpy(group[g].out, L.h_hist.data() + (size_t)bin.len * g, (size_t)bin.len * sizeof(uint64_t));
+    L.stats.kernel_ms = ms;
+    L.stats.loop_units = units;
     // the fast triangle kernel skips (i,j) pairs that no counted triangle can
     // contain and counts the triangles it walks; other kernels walk every
     // triangle of their tasks
-    ctx->stats.evaluated_units = (sp.kind == TPCF_TRIANGLE && !fp64) ? dev_evaluated : evaluated;
-    ctx->stats.binned_units = (sp.kind == TPCF_TRIANGLE && !fp64) ? dev_binned : evaluated;
-    ctx->stats.tasks = ntasks;
-    ctx->stats.kernel_launches = launches;
-    ctx->stats.total_ms =
+    L.stats.evaluated_units = (sp.kind == TPCF_TRIANGLE && !fp64) ? dev_evaluated : evaluated;
+    L.stats.binned_units = (sp.kind == TPCF_TRIANGLE && !fp64) ? dev_binned : evaluated;
+    L.stats.tasks = ntasks;
+    L.stats.kernel_launches = launches;
+    L.stats.total_ms =
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_wall0).count();
 }
 
@@ -1012,53 +1037,82 @@ int64_t job_bytes(tpcf_ctx* ctx, const tpcf_spec& sp, const tpcf_job& job) {
     return b + len * 8;
 }
 
-void worker_loop(tpcf_ctx* ctx) {
+double now_ms() {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// Serving worker on lane 'lane'.  It takes the oldest pending job plus every
+// pending job of the same binning that fits the admission budget (device
+// bytes of all batches in flight on the serving lanes), counts them in one
+// persistent launch on its own stream and completes their tickets.  Jobs that
+// arrive meanwhile are taken by the next free worker, so batches overlap on
+// the device.
+void worker_loop(tpcf_ctx* ctx, int lane) {
+    Lane& L = *ctx->lanes[lane];
+    cudaSetDevice(ctx->device);
     for (;;) {
         std::vector<std::shared_ptr<Pending>> batch;
+        int64_t used = 0;
         {
             std::unique_lock<std::mutex> lk(ctx->qmu);
-            ctx->qcv.wait(lk, [&] { return ctx->stop || !ctx->queue.empty(); });
-            if (ctx->stop && ctx->queue.empty()) return;
-            // admit the oldest job and every compatible pending job while the
-            // device-memory footprint stays within the admission budget
-            auto first = ctx->queue.front();
-            int64_t budget = ctx->admit_bytes, used = 0;
-            for (auto it = ctx->queue.begin(); it != ctx->queue.end();) {
-                auto& p = *it;
-                if (p->cancelled) {
-                    p->status = TPCF_ERR_CANCELLED;
+            for (;;) {
+                ctx->qcv.wait(lk, [&] { return ctx->stop || !ctx->queue.empty(); });
+                if (ctx->stop && ctx->queue.empty()) return;
+                // drop cancelled jobs
+                for (auto it = ctx->queue.begin(); it != ctx->queue.end();) {
+                    if ((*it)->cancelled) {
+                        (*it)->status = TPCF_ERR_CANCELLED;
+                        (*it)->t_done = now_ms();
+                        it = ctx->queue.erase(it);
+                    } else {
+                        ++it;
+                    }
+                }
+                if (ctx->queue.empty()) continue;
+                auto first = ctx->queue.front();
+                int64_t room = ctx->admit_bytes - ctx->inflight_bytes;
+                int64_t fb = job_bytes(ctx, first->spec, first->job);
+                // the oldest job waits for memory unless nothing else is in flight
+                if (fb > room && ctx->inflight_bytes > 0) {
+                    ctx->qcv.wait(lk);
+                    continue;
+                }
+                for (auto it = ctx->queue.begin(); it != ctx->queue.end();) {
+                    auto& p = *it;
+                    if (!same_binning(p->spec, first->spec) || p->spec.prune != first->spec.prune) {
+                        ++it;
+                        continue;
+                    }
+                    int64_t jb = job_bytes(ctx, p->spec, p->job);
+                    if (!batch.empty() && used + jb > room) break;
+                    used += jb;
+                    batch.push_back(p);
                     it = ctx->queue.erase(it);
-                    continue;
+                    if (batch.size() >= 4096) break;
                 }
-                if (!same_binning(p->spec, first->spec) || p->spec.prune != first->spec.prune) {
-                    ++it;
-                    continue;
-                }
-                int64_t jb = job_bytes(ctx, p->spec, p->job);
-                if (!batch.empty() && used + jb > budget) break;
-                used += jb;
-                batch.push_back(p);
-                it = ctx->queue.erase(it);
-                if (batch.size() >= 4096) break;
+                ctx->inflight_bytes += used;
+                break;
             }
         }
         ctx->qcv.notify_all();
-        if (batch.empty()) continue;
         std::vector<GroupJob> group;
         int64_t len = 0;
         tpcf_hist_len(&batch[0]->spec, &len);
+        double t_start = now_ms();
         for (auto& p : batch) {
             p->result.assign((size_t)len, 0);
+            p->t_start = t_start;
             group.push_back({&p->spec, &p->job, p->result.data()});
         }
-        tpcf_status st;
-        {
-            std::lock_guard<std::recursive_mutex> lk(ctx->mu);
-            st = guarded(ctx, [&] { run_group(ctx, group); });
-        }
+        tpcf_status st = guarded(ctx, [&] { run_group(ctx, L, group); });
+        double t_done = now_ms();
         {
             std::lock_guard<std::mutex> lk(ctx->qmu);
-            for (auto& p : batch) p->status = st;
+            ctx->inflight_bytes -= used;
+            for (auto& p : batch) {
+                p->status = st;
+                p->t_done = t_done;
+            }
         }
         ctx->qcv.notify_all();
     }
@@ -1105,21 +1159,28 @@ tpcf_status tpcf_create(tpcf_ctx** out, int32_t device) {
         ctx->device = device;
         CK(cudaSetDevice(device));
         CK(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device));
-        CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
-        CK(cudaEventCreate(&ctx->ev0));
-        CK(cudaEventCreate(&ctx->ev1));
-        CK(cudaEventCreate(&ctx->ev_mid));
         const char* tp = getenv("TPCF_TILE_POINTS");
         if (tp) ctx->tile_points = std::max(8, std::min(TILE, atoi(tp)));
         const char* adm = getenv("TPCF_ADMIT_BYTES");
         if (adm) ctx->admit_bytes = atoll(adm);
+        const char* nw = getenv("TPCF_SERVING_LANES");
+        int workers = nw ? std::max(1, std::min(8, atoi(nw))) : 2;
+        for (int i = 0; i <= workers; i++) {
+            auto L = std::make_unique<Lane>();
+            CK(cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking));
+            CK(cudaEventCreate(&L->ev0));
+            CK(cudaEventCreate(&L->ev1));
+            CK(cudaEventCreate(&L->ev_mid));
+            ctx->lanes.push_back(std::move(L));
+        }
     });
     if (s != TPCF_OK) {
         g_tls_error = ctx->last_error;
+        for (auto& L : ctx->lanes) L->release();
         delete ctx;
         return s;
     }
-    ctx->worker = std::thread(worker_loop, ctx);
+    for (size_t i = 1; i < ctx->lanes.size(); i++) ctx->workers.emplace_back(worker_loop, ctx, (int)i);
     *out = ctx;
     return TPCF_OK;
 }
@@ -1131,24 +1192,18 @@ tpcf_status tpcf_destroy(tpcf_ctx* ctx) {
         ctx->stop = true;
     }
     ctx->qcv.notify_all();
-    if (ctx->worker.joinable()) ctx->worker.join();
+    for (auto& t : ctx->workers)
+        if (t.joinable()) t.join();
     {
         std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+        std::lock_guard<std::recursive_mutex> vlk(ctx->view_mu);
         cudaSetDevice(ctx->device);
         ctx->views.clear();
         ctx->cat_dev.clear();
-        ctx->d_jobs.release();
-        ctx->d_tasks.release();
-        ctx->d_counters.release();
-        ctx->d_queue.release();
-        ctx->d_hist.release();
+        for (auto& L : ctx->lanes) L->release();
         ctx->acos_keys.release();
         ctx->acos_vals.release();
         ctx->acos_bucket.release();
-        if (ctx->ev0) cudaEventDestroy(ctx->ev0);
-        if (ctx->ev1) cudaEventDestroy(ctx->ev1);
-        if (ctx->ev_mid) cudaEventDestroy(ctx->ev_mid);
-        if (ctx->stream) cudaStreamDestroy(ctx->stream);
     }
     delete ctx;
     return TPCF_OK;
@@ -1166,28 +1221,24 @@ tpcf_status tpcf_catalog_create(tpcf_ctx* ctx, const float* x, const float* y, c
         c->x.assign(x, x + n);
         c->y.assign(y, y + n);
         c->z.assign(z, z + n);
-        auto d = std::make_shared<DevBuf<float4>>();
-        d->reserve(std::max<int64_t>(n, 1));
-        std::vector<float4> p(std::max<int64_t>(n, 1));
-        for (int64_t i = 0; i < n; i++) {
-            p[i].x = x[i];
-            p[i].y = y[i];
-            p[i].z = z[i];
-            int32_t k = (int32_t)i;
-            memcpy(&p[i].w, &k, 4);
-        }
-        CK(cudaMemcpy(d->p, p.data(), p.size() * sizeof(float4), cudaMemcpyHostToDevice));
-        ctx->h2d += p.size() * sizeof(float4);
+        std::lock_guard<std::recursive_mutex> vlk(ctx->view_mu);
         uint64_t h = ctx->next_handle++;
         ctx->catalogs[h] = c;
-        ctx->cat_dev[h] = d;
+        // the resident form of a catalog is its spatial view (sorted points,
+        // tiles); sub-range views are made on demand from the host copy
+        try {
+            get_view(ctx, *ctx->lanes[0], h, 0, n);
+        } catch (...) {
+            ctx->catalogs.erase(h);
+            throw;
+        }
         *handle = h;
     });
 }
 
 tpcf_status tpcf_catalog_release(tpcf_ctx* ctx, uint64_t handle) {
     if (!ctx) return TPCF_ERR_INVALID;
-    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    std::lock_guard<std::recursive_mutex> vlk(ctx->view_mu);
     if (!ctx->catalogs.count(handle)) return fail(ctx, TPCF_ERR_NOT_FOUND, "unknown catalog handle");
     ctx->catalogs.erase(handle);
     ctx->cat_dev.erase(handle);
@@ -1200,9 +1251,8 @@ tpcf_status tpcf_catalog_release(tpcf_ctx* ctx, uint64_t handle) {
 
 tpcf_status tpcf_resident_bytes(tpcf_ctx* ctx, int64_t* bytes) {
     if (!ctx || !bytes) return TPCF_ERR_INVALID;
-    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    std::lock_guard<std::recursive_mutex> lk(ctx->view_mu);
     int64_t b = 0;
-    for (auto& kv : ctx->cat_dev) b += (int64_t)kv.second->bytes();
     for (auto& kv : ctx->views) b += (int64_t)kv.second->bytes();
     *bytes = b;
     return TPCF_OK;
@@ -1219,7 +1269,7 @@ tpcf_status tpcf_hist_len(const tpcf_spec* sp, int64_t* len) {
 
 tpcf_status tpcf_loop_units(tpcf_ctx* ctx, const tpcf_spec* sp, const tpcf_job* job, uint64_t* units) {
     if (!ctx || !sp || !job || !units) return TPCF_ERR_INVALID;
-    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    std::lock_guard<std::recursive_mutex> lk(ctx->view_mu);
     int64_t n[3] = {0, 0, 0};
     int nc = sp->kind == TPCF_PAIR ? 2 : 3;
     for (int r = 0; r < nc; r++) {
@@ -1253,18 +1303,19 @@ tpcf_status tpcf_count_batch(tpcf_ctx* ctx, const tpcf_spec* specs, const tpcf_j
                     g.push_back({&specs[k], &jobs[k], hists[k]});
                     done[k] = 1;
                 }
-            run_group(ctx, g);
-            acc.kernel_ms += ctx->stats.kernel_ms;
-            acc.main_kernel_ms += ctx->stats.main_kernel_ms;
-            acc.binned_units += ctx->stats.binned_units;
-            acc.total_ms += ctx->stats.total_ms;
-            acc.loop_units += ctx->stats.loop_units;
-            acc.evaluated_units += ctx->stats.evaluated_units;
-            acc.recheck_units += ctx->stats.recheck_units;
-            acc.tasks += ctx->stats.tasks;
-            acc.kernel_launches += ctx->stats.kernel_launches;
+            Lane& L = *ctx->lanes[0];
+            run_group(ctx, L, g);
+            acc.kernel_ms += L.stats.kernel_ms;
+            acc.main_kernel_ms += L.stats.main_kernel_ms;
+            acc.binned_units += L.stats.binned_units;
+            acc.total_ms += L.stats.total_ms;
+            acc.loop_units += L.stats.loop_units;
+            acc.evaluated_units += L.stats.evaluated_units;
+            acc.recheck_units += L.stats.recheck_units;
+            acc.tasks += L.stats.tasks;
+            acc.kernel_launches += L.stats.kernel_launches;
         }
-        ctx->stats = acc;
+        ctx->lanes[0]->stats = acc;
     });
 }
 
@@ -1289,6 +1340,7 @@ tpcf_status tpcf_submit(tpcf_ctx* ctx, const tpcf_spec* spec, const tpcf_job* jo
     auto p = std::make_shared<Pending>();
     p->spec = *spec;
     p->job = *job;
+    p->t_submit = now_ms();
     {
         std::lock_guard<std::mutex> lk(ctx->qmu);
         p->ticket = ctx->next_ticket++;
@@ -1300,7 +1352,8 @@ tpcf_status tpcf_submit(tpcf_ctx* ctx, const tpcf_spec* spec, const tpcf_job* jo
     return TPCF_OK;
 }
 
-tpcf_status tpcf_wait(tpcf_ctx* ctx, uint64_t ticket, uint64_t* hist, int64_t hist_len, int64_t timeout_ms) {
+tpcf_status tpcf_wait_timed(tpcf_ctx* ctx, uint64_t ticket, uint64_t* hist, int64_t hist_len, int64_t timeout_ms,
+                            double* latency_ms, double* run_ms) {
     if (!ctx) return TPCF_ERR_INVALID;
     std::unique_lock<std::mutex> lk(ctx->qmu);
     auto it = ctx->tickets.find(ticket);
@@ -1310,12 +1363,18 @@ tpcf_status tpcf_wait(tpcf_ctx* ctx, uint64_t ticket, uint64_t* hist, int64_t hi
     if (timeout_ms < 0) ctx->qcv.wait(lk, ready);
     else if (!ctx->qcv.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready)) return TPCF_ERR_TIMEOUT;
     ctx->tickets.erase(ticket);
+    if (latency_ms) *latency_ms = p->t_done - p->t_submit;
+    if (run_ms) *run_ms = p->t_start > 0 ? p->t_done - p->t_start : 0.0;
     if (p->status != TPCF_OK) return p->status;
     if (hist) {
         if ((int64_t)p->result.size() != hist_len) return fail(ctx, TPCF_ERR_INVALID, "hist_len mismatch");
         memcpy(hist, p->result.data(), p->result.size() * sizeof(uint64_t));
     }
     return TPCF_OK;
+}
+
+tpcf_status tpcf_wait(tpcf_ctx* ctx, uint64_t ticket, uint64_t* hist, int64_t hist_len, int64_t timeout_ms) {
+    return tpcf_wait_timed(ctx, ticket, hist, hist_len, timeout_ms, nullptr, nullptr);
 }
 
 tpcf_status tpcf_cancel(tpcf_ctx* ctx, uint64_t ticket) {
@@ -1338,11 +1397,12 @@ tpcf_status tpcf_cancel(tpcf_ctx* ctx, uint64_t ticket) {
 tpcf_status tpcf_last_stats(tpcf_ctx* ctx, tpcf_stats* stats) {
     if (!ctx || !stats) return TPCF_ERR_INVALID;
     std::lock_guard<std::recursive_mutex> lk(ctx->mu);
-    *stats = ctx->stats;
+    Lane& L = *ctx->lanes[0];
+    *stats = L.stats;
     // byte counters cover everything copied since the previous stats read
-    stats->h2d_bytes = ctx->h2d;
-    stats->d2h_bytes = ctx->d2h;
-    ctx->h2d = ctx->d2h = 0;
+    stats->h2d_bytes = L.h2d;
+    stats->d2h_bytes = L.d2h;
+    L.h2d = L.d2h = 0;
     return TPCF_OK;
 }
 
@@ -1358,10 +1418,11 @@ int64_t tpcf_debug_acos_selfcheck(tpcf_ctx* ctx, int64_t* table_size) {
         DevBuf<unsigned int> mm;
         mm.reserve(1);
         CK(cudaMemset(mm.p, 0, 4));
-        CK(launch_acos_check(acos_table(ctx), 0, ctx->acos_n, mm.p, ctx->stream));
+        cudaStream_t st = ctx->lanes[0]->stream;
+        CK(launch_acos_check(acos_table(ctx), 0, ctx->acos_n, mm.p, st));
         unsigned int h = 0;
-        CK(cudaMemcpyAsync(&h, mm.p, 4, cudaMemcpyDeviceToHost, ctx->stream));
-        CK(cudaStreamSynchronize(ctx->stream));
+        CK(cudaMemcpyAsync(&h, mm.p, 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
         r = h;
         if (table_size) *table_size = ctx->acos_n;
     });

@@ -24,7 +24,7 @@ ABI_SYMBOLS = [
     "tpcf_create", "tpcf_destroy", "tpcf_last_error", "tpcf_status_string", "tpcf_abi_version",
     "tpcf_catalog_create", "tpcf_catalog_release", "tpcf_resident_bytes", "tpcf_hist_len", "tpcf_count",
     "tpcf_count_batch", "tpcf_submit", "tpcf_wait", "tpcf_cancel", "tpcf_last_stats", "tpcf_loop_units",
-    "tpcf_read_catalog", "tpcf_pair_count_noalloc",
+    "tpcf_read_catalog", "tpcf_pair_count_noalloc", "tpcf_wait_timed",
 ]
 
 
@@ -80,6 +80,8 @@ def lib():
         L.tpcf_submit.argtypes = [P, ctypes.POINTER(Spec), ctypes.POINTER(Job), ctypes.POINTER(ctypes.c_uint64)]
         L.tpcf_wait.argtypes = [P, ctypes.c_uint64, P, ctypes.c_int64, ctypes.c_int64]
         L.tpcf_cancel.argtypes = [P, ctypes.c_uint64]
+        L.tpcf_wait_timed.argtypes = [P, ctypes.c_uint64, P, ctypes.c_int64, ctypes.c_int64,
+                                      ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
         L.tpcf_last_stats.argtypes = [P, ctypes.POINTER(Stats)]
         L.tpcf_loop_units.argtypes = [P, ctypes.POINTER(Spec), ctypes.POINTER(Job), ctypes.POINTER(ctypes.c_uint64)]
         L.tpcf_read_catalog.argtypes = [ctypes.c_char_p, ctypes.c_int32, ctypes.c_float, P, P, P,
@@ -201,6 +203,15 @@ class Engine:
         h = np.zeros(n, dtype=np.uint64)
         self._check(lib().tpcf_wait(self._ctx, ticket, h.ctypes.data, n, timeout_ms), "wait")
         return h
+
+    def wait_timed(self, ticket, spec, timeout_ms=-1):
+        """(histogram, latency ms from submit to completion, ms of its batch)."""
+        n = hist_len(spec)
+        h = np.zeros(n, dtype=np.uint64)
+        lat, run = ctypes.c_double(), ctypes.c_double()
+        self._check(lib().tpcf_wait_timed(self._ctx, ticket, h.ctypes.data, n, timeout_ms, ctypes.byref(lat),
+                                          ctypes.byref(run)), "wait")
+        return h, lat.value, run.value
 
     def cancel(self, ticket):
         return lib().tpcf_cancel(self._ctx, ticket)

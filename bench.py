@@ -415,6 +415,232 @@ def impl_ours(args):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# Other workloads (python bench.py --config NAME); the default is configs[1].
+
+def _line(metric, value, unit, args, config, **kw):
+    d = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+         "config": config}
+    d.update(kw)
+    print(json.dumps(d))
+
+
+def run_three_side(args):
+    """configs[0]: three-side DDD + RRR, 1000 clustered + 1000 uniform points in a
+    100^3 cube, 16 bins on [0,40) (reference overflow aliasing), 2e9 triangles."""
+    import tpcf
+    import synth
+    d = synth.blobs(1000, n_blobs=20, sigma=5.0, box=100.0, seed=1)
+    r = synth.uniform(1000, box=100.0, seed=0)
+    eng = tpcf.Engine(0)
+    hd, hr = eng.catalog(d), eng.catalog(r)
+    sp = [tpcf.make_spec(tpcf.THREE_SIDE, tpcf.LOOP_ALL, [(16, 0.0, 40.0)])] * 2
+    jobs = [eng.job([hd, hd, hd]), eng.job([hr, hr, hr])]
+    for _ in range(args.warmup):
+        eng.count_batch(sp, jobs)
+    ms = []
+    for _ in range(args.steps):
+        eng.count_batch(sp, jobs)
+        ms.append(eng.stats()["kernel_ms"])
+    units = eng.stats()["loop_units"]
+    h64 = eng.count_batch([tpcf.make_spec(tpcf.THREE_SIDE, tpcf.LOOP_ALL, [(16, 0.0, 40.0)],
+                                          precision=tpcf.PLAIN_FP64)] * 2, jobs)
+    fp64_ms = eng.stats()["kernel_ms"]
+    h32 = eng.count_batch(sp, jobs)
+    same = all(np.array_equal(a, b) for a, b in zip(h32, h64))
+    cpu = None
+    import ref_build
+    exe = ref_build.binary("3side_n16_0_40")
+    if exe and not args.no_cpu_baseline:
+        with tempfile.TemporaryDirectory() as tmp:
+            path = os.path.join(tmp, "D400.dat")
+            synth.write_header_catalog(path, d[:400])
+            t0 = time.perf_counter()
+            subprocess.run([exe, path, path, path, "-o", os.path.join(tmp, "o.dat")], stdout=subprocess.DEVNULL,
+                           check=True)
+            dt = time.perf_counter() - t0
+            cpu = {"value": 400 ** 3 / dt, "unit": "triangles/s", "cores": 1, "kind": "reference",
+                   "sample": "reference three-side program (16 bins on [0,40)), DDD of 400 clustered points, "
+                             "6.4e7 triangles in %.1f s, as built (lock diagnostic included)" % dt}
+    mean = statistics.mean(ms) / 1e3
+    _line("triangles/s (bit-exact histos)", units / mean, "triangles/s", args,
+          {"workload": "three-side DDD+RRR, 1000 clustered + 1000 uniform, 16 bins on [0,40)",
+           "triangles_per_step": units},
+          ms_per_step=mean * 1e3, p50_ms=statistics.median(ms), p99_ms=float(np.percentile(ms, 99)),
+          plain_fp64={"value": units / (fp64_ms / 1e3), "ms_per_step": fp64_ms, "identical": same},
+          roofline={"bound": "issue", "achieved": 10 * units / mean / 1e12, "unit": "Tinst/s",
+                    "per_unit": "10 lane-instructions per triangle"},
+          cpu_baseline=cpu)
+    eng.close()
+    return 0
+
+
+def _jackknife_region(xyz):
+    """4 x 4 cells of the flat-sky angles (x/z, y/z) over [-10, 10] degrees."""
+    a = np.deg2rad(10.0)
+    tx = np.clip(((xyz[:, 0] / xyz[:, 2] + a) / (2 * a) * 4).astype(int), 0, 3)
+    ty = np.clip(((xyz[:, 1] / xyz[:, 2] + a) / (2 * a) * 4).astype(int), 0, 3)
+    return tx * 4 + ty
+
+
+def run_voxel(args):
+    """configs[2]: 100k clustered + 100k uniform points in a 20x20 degree light-cone
+    slab (depth 500-1500), triangle parametrization DDD/DDR/DRR/RRR of the full
+    catalogs and of the 16 jackknife subsamples (one 4x4 angular cell left out
+    each): 68 jobs of uneven size in one persistent launch."""
+    import tpcf
+    import synth
+    d = synth.lightcone(100000, clustered=True, seed=11)
+    r = synth.lightcone(100000, seed=12)
+    rd, rr = _jackknife_region(d), _jackknife_region(r)
+    nan = tpcf.NAN_ZERO if platform.machine() == "aarch64" else tpcf.NAN_INT_MIN
+    eng = tpcf.Engine(0)
+    cats = [(eng.catalog(d), eng.catalog(r))]
+    for reg in range(16):
+        cats.append((eng.catalog(d[rd != reg]), eng.catalog(r[rr != reg])))
+    specs, jobs = [], []
+    for hd, hr in cats:
+        for hs, loop in (([hd, hd, hd], tpcf.LOOP_SAME), ([hd, hd, hr], tpcf.LOOP_ONE),
+                         ([hd, hr, hr], tpcf.LOOP_ONE), ([hr, hr, hr], tpcf.LOOP_SAME)):
+            specs.append(tpcf.make_spec(tpcf.TRIANGLE, loop, SPEC_AXES, nan_policy=nan))
+            jobs.append(eng.job(hs))
+    for _ in range(args.warmup):
+        eng.count_batch(specs, jobs)
+    ms, st = [], None
+    for _ in range(args.steps):
+        eng.count_batch(specs, jobs)
+        st = eng.stats()
+        ms.append(st["kernel_ms"])
+    mean = statistics.mean(ms) / 1e3
+    _line("triangles/s (bit-exact histos)", st["loop_units"] / mean, "triangles/s", args,
+          {"workload": "light cone 100k clustered + 100k uniform, TP s8 q8 t16, full + 16 jackknife subsamples "
+                       "x DDD/DDR/DRR/RRR = 68 jobs, one launch", "jobs": len(jobs),
+           "triangles_per_step": st["loop_units"], "evaluated_triangles_per_step": st["evaluated_units"],
+           "binned_triangles_per_step": st["binned_units"], "tasks": st["tasks"]},
+          ms_per_step=mean * 1e3, wall_ms_per_step=st["total_ms"], p50_ms=statistics.median(ms),
+          p99_ms=float(np.percentile(ms, 99)),
+          roofline={"bound": "issue", "achieved": W_TP * st["binned_units"] / (st["main_kernel_ms"] / 1e3) / 1e12,
+                    "unit": "Tinst/s", "per_unit": "58 lane-instructions per binned triangle"})
+    eng.close()
+    return 0
+
+
+def run_lattice(args):
+    """configs[3]: 500k points uniform in a 500^3 box with 30 % on the integer
+    lattice; three-side 32 bins on [0,32) restricted to triples whose sides are
+    all below 32; FP32 path vs all-FP64 kernel, counts identical."""
+    import tpcf
+    import synth
+    pts = synth.lattice_mix(500000, box=500.0, frac=0.3, seed=3)
+    eng = tpcf.Engine(0)
+    h = eng.catalog(pts)
+    job = eng.job([h, h, h])
+    s32 = tpcf.make_spec(tpcf.THREE_SIDE, tpcf.LOOP_ALL, [(32, 0.0, 32.0)], overflow=tpcf.OVERFLOW_CLEAN)
+    s64 = tpcf.make_spec(tpcf.THREE_SIDE, tpcf.LOOP_ALL, [(32, 0.0, 32.0)], overflow=tpcf.OVERFLOW_CLEAN,
+                         precision=tpcf.PLAIN_FP64)
+    for _ in range(args.warmup):
+        eng.count(s32, job)
+    ms = []
+    for _ in range(args.steps):
+        h32 = eng.count(s32, job)
+        st = eng.stats()
+        ms.append(st["kernel_ms"])
+    # FP64 comparison on the slab x < 100 (a fifth of the box), or everything
+    sub = pts if args.fp64_full else pts[pts[:, 0] < 100.0]
+    hs = h if args.fp64_full else eng.catalog(sub)
+    js = eng.job([hs, hs, hs])
+    h64 = eng.count(s64, js)
+    st64 = eng.stats()
+    h32s = h32 if args.fp64_full else eng.count(s32, js)
+    mean = statistics.mean(ms) / 1e3
+    _line("triangles/s (bit-exact histos)", st["loop_units"] / mean, "triangles/s", args,
+          {"workload": "500k points, 500^3 box, 30 % on the integer lattice, three-side 32 bins on [0,32), "
+                       "sides < 32 only", "triangles_per_step": st["loop_units"],
+           "evaluated_triangles_per_step": st["evaluated_units"], "tasks": st["tasks"],
+           "counted": int(h32.sum())},
+          ms_per_step=mean * 1e3, wall_ms_per_step=st["total_ms"],
+          plain_fp64={"ms_per_step": st64["kernel_ms"], "points": int(len(sub)),
+                      "sample": "all points" if args.fp64_full else "slab x < 100",
+                      "identical": bool(np.array_equal(h32s, h64))})
+    eng.close()
+    return 0
+
+
+def run_serving(args):
+    """configs[4]: 2000 jobs with Poisson arrivals (rate --rate per second, seed
+    2) on resident catalogs whose sizes are log-uniform in [500, 50000], drawn
+    from the clustered-cube (configs[0]) and light-cone (configs[2]) generators;
+    70 % triangle jobs (DDD/DDR/DRR/RRR), 30 % pair jobs (DD/DR/RR, 700 bins on
+    [0,70)); p50/p99 latency from arrival to histogram and throughput."""
+    import tpcf
+    import synth
+    rng = np.random.Generator(np.random.PCG64(2))
+    nan = tpcf.NAN_ZERO if platform.machine() == "aarch64" else tpcf.NAN_INT_MIN
+    eng = tpcf.Engine(0)
+    pool = {"cube": [], "cone": []}
+    sizes = np.exp(rng.uniform(np.log(500), np.log(50000), size=24)).astype(int)
+    for i, n in enumerate(sizes):
+        fam = "cube" if i % 2 == 0 else "cone"
+        if fam == "cube":
+            # 500 points per blob, as in the 10k-point cube workload
+            dd = synth.blobs(n, n_blobs=max(1, n // 500), seed=1000 + i)
+            rr = synth.uniform(n, box=100.0, seed=2000 + i)
+        else:
+            dd, rr = synth.lightcone(n, clustered=True, seed=3000 + i), synth.lightcone(n, seed=4000 + i)
+        pool[fam].append((eng.catalog(dd), eng.catalog(rr), n))
+    tp = lambda loop: tpcf.make_spec(tpcf.TRIANGLE, loop, SPEC_AXES, nan_policy=nan)
+    pr = lambda loop: tpcf.make_spec(tpcf.PAIR, loop, [(700, 0.0, 70.0)])
+    jobs = []
+    for k in range(args.jobs):
+        fam = "cube" if rng.random() < 0.5 else "cone"
+        a = pool[fam][int(rng.integers(len(pool[fam])))]
+        b = pool[fam][int(rng.integers(len(pool[fam])))]
+        hd, hr = a[0], b[1]
+        if rng.random() < 0.7:
+            kind = int(rng.integers(4))
+            hs, loop = [([hd, hd, hd], tpcf.LOOP_SAME), ([hd, hd, hr], tpcf.LOOP_ONE),
+                        ([hd, hr, hr], tpcf.LOOP_ONE), ([hr, hr, hr], tpcf.LOOP_SAME)][kind]
+            jobs.append((tp(loop), eng.job(hs)))
+        else:
+            kind = int(rng.integers(3))
+            hs, loop = [([hd, hd], tpcf.LOOP_SAME), ([hd, hr], tpcf.LOOP_ONE), ([hr, hr], tpcf.LOOP_SAME)][kind]
+            jobs.append((pr(loop), eng.job(hs)))
+    units = sum(eng.loop_units(s, j) for s, j in jobs)
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, size=len(jobs)))
+    for s, j in jobs[:20]:  # warm the kernels and the acos table
+        eng.count(s, j)
+    tickets = [None] * len(jobs)
+    t0 = time.perf_counter()
+
+    def submitter():
+        for i, (s, j) in enumerate(jobs):
+            dt = arrivals[i] - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            tickets[i] = eng.submit(s, j)
+
+    th = threading.Thread(target=submitter)
+    th.start()
+    lat, run = [], []
+    for i, (s, j) in enumerate(jobs):
+        while tickets[i] is None:
+            time.sleep(0.0005)
+        _, l_ms, r_ms = eng.wait_timed(tickets[i], s)
+        lat.append(l_ms)
+        run.append(r_ms)
+    makespan = time.perf_counter() - t0
+    th.join()
+    _line("jobs/s with p50/p99 latency (bit-exact histos)", len(jobs) / makespan, "jobs/s", args,
+          {"workload": "%d Poisson-arrival jobs at %.0f/s, catalogs 500-50000 points (log-uniform), 70 %% triangle "
+                       "(s8 q8 t16) / 30 %% pair (700 bins) jobs, resident catalogs" % (len(jobs), args.rate),
+           "jobs": len(jobs), "triangles_and_pairs": units},
+          p50_ms=float(np.percentile(lat, 50)), p99_ms=float(np.percentile(lat, 99)),
+          mean_batch_ms=float(np.mean(run)), makespan_s=makespan, units_per_s=units / makespan)
+    eng.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -423,11 +649,18 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--config", default="tp10k", choices=["tp10k", "three1k", "voxel100k", "lattice500k", "serving"])
+    ap.add_argument("--jobs", type=int, default=2000, help="serving: number of jobs")
+    ap.add_argument("--rate", type=float, default=50.0, help="serving: Poisson arrival rate (jobs/s)")
+    ap.add_argument("--fp64-full", action="store_true", help="lattice500k: FP64 comparison on all points")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return impl_reference(args)
+    if args.config != "tp10k":
+        return {"three1k": run_three_side, "voxel100k": run_voxel, "lattice500k": run_lattice,
+                "serving": run_serving}[args.config](args)
     return impl_ours(args)
 
 

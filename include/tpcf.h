@@ -164,10 +164,19 @@ tpcf_status tpcf_count(tpcf_ctx* ctx, const tpcf_spec* spec, const tpcf_job* job
 tpcf_status tpcf_count_batch(tpcf_ctx* ctx, const tpcf_spec* specs, const tpcf_job* jobs, int32_t n,
                              uint64_t* const* hists);
 
-/* Asynchronous submit / wait (serving).  Jobs submitted while others run are
- * admitted into the next launch; tpcf_wait blocks up to timeout_ms (<0: forever). */
+/* Asynchronous submit / wait (serving).  Serving workers (TPCF_SERVING_LANES,
+ * default 2), each with its own stream, take the oldest pending job together
+ * with every pending job of the same binning, while the device bytes of all
+ * running batches stay within the admission budget (TPCF_ADMIT_BYTES, default
+ * 8 GiB), and count them in one launch; jobs submitted meanwhile go to the next
+ * free worker, so batches overlap on the device.  tpcf_wait blocks up to
+ * timeout_ms (<0: forever); tpcf_cancel drops a job that has not started. */
 tpcf_status tpcf_submit(tpcf_ctx* ctx, const tpcf_spec* spec, const tpcf_job* job, uint64_t* ticket);
 tpcf_status tpcf_wait(tpcf_ctx* ctx, uint64_t ticket, uint64_t* hist, int64_t hist_len, int64_t timeout_ms);
+/* As tpcf_wait; also returns the job's milliseconds from submission to
+ * completion (latency_ms) and of the device batch it ran in (run_ms). */
+tpcf_status tpcf_wait_timed(tpcf_ctx* ctx, uint64_t ticket, uint64_t* hist, int64_t hist_len, int64_t timeout_ms,
+                            double* latency_ms, double* run_ms);
 tpcf_status tpcf_cancel(tpcf_ctx* ctx, uint64_t ticket);
 
 tpcf_status tpcf_last_stats(tpcf_ctx* ctx, tpcf_stats* stats);

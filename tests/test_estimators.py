@@ -1,0 +1,64 @@
+"""Estimators (3pcf_gb300/estimators.py) against the element-by-element
+restatement of the reference scripts (oracle/estimators_ref.py)."""
+import numpy as np
+
+import estimators
+import estimators_ref
+import oracle
+import synth
+
+
+def _hists(seed):
+    d = synth.blobs(140, n_blobs=3, sigma=4.0, box=40.0, seed=seed)
+    r = synth.uniform(150, box=30.0, seed=seed + 1)
+    spec = ((8, 2.0, 10.0), (8, 1.0, 3.0), (16, 0.0, 1.0))
+    h = {k: oracle.triangle(c, w, spec)[0] for k, c, w in (("DDD", [d, d, d], 0), ("DDR", [d, d, r], 1),
+                                                          ("DRR", [d, r, r], 1), ("RRR", [r, r, r], 0))}
+    n = {"DDD": (140, 140, 140), "DDR": (140, 140, 150), "DRR": (140, 150, 150), "RRR": (150, 150, 150)}
+    return h, n, spec, d, r
+
+
+def test_zeta_matches_reference_restatement():
+    h, n, spec, _, _ = _hists(5)
+    z = estimators.zeta(h["DDD"], h["DDR"], h["DRR"], h["RRR"], n["DDD"], n["DDR"], n["DRR"], n["RRR"])
+    want = estimators_ref.zeta(h["DDD"], h["DDR"], h["DRR"], h["RRR"], n["DDD"], n["DDR"], n["DRR"], n["RRR"])
+    assert np.array_equal(z, np.array(want))
+    assert np.count_nonzero(z) > 0
+
+
+def test_zeta_of_identical_catalogs_is_zero():
+    """D = R: every term cancels exactly where RRR is populated."""
+    d = synth.uniform(120, box=25.0, seed=9)
+    spec = ((8, 2.0, 10.0), (8, 1.0, 3.0), (16, 0.0, 1.0))
+    ddd, _ = oracle.triangle([d, d, d], 0, spec)
+    ddr, _ = oracle.triangle([d, d, d], 1, spec)
+    n = (120, 120, 120)
+    z = estimators.zeta(ddd, ddr, ddr, ddd, n, n, n, n)
+    nd = estimators.norms_3pcf(n, n, n, n)
+    expect = (ddd / nd[0] - 3 * ddr / nd[1] + 3 * ddr / nd[2] - ddd / nd[3]) / (ddd / nd[3])
+    expect[~np.isfinite(expect)] = 0
+    assert np.allclose(z, expect, rtol=0, atol=1e-12)
+
+
+def test_xi_matches_reference_restatement():
+    d = synth.blobs(800, n_blobs=6, sigma=5.0, box=80.0, seed=3)
+    r = synth.uniform(700, box=80.0, seed=4)
+    dd, _ = oracle.pair([d, d], 0, 0.0, 70.0, 700)
+    dr, _ = oracle.pair([d, r], 1, 0.0, 70.0, 700)
+    rr, _ = oracle.pair([r, r], 0, 0.0, 70.0, 700)
+    x = estimators.xi(dd, dr, rr, (800, 800), (800, 700), (700, 700))
+    want = estimators_ref.xi(dd, dr, rr, (800, 800), (800, 700), (700, 700))
+    assert np.array_equal(x, np.array(want))
+    tab = estimators.xi_table(x, 0.0, 70.0, 700)
+    text = estimators.format_xi_table(tab)
+    assert text.splitlines()[0] == "%f %f" % (0.1, x[0])
+    assert len(text.splitlines()) == 700
+
+
+def test_reduced_zeta_shape_and_finite_denominator():
+    h, n, spec, d, r = _hists(11)
+    z = estimators.zeta(h["DDD"], h["DDR"], h["DRR"], h["RRR"], n["DDD"], n["DDR"], n["DRR"], n["RRR"])
+    tab = np.stack([np.linspace(0.5, 70, 140), np.linspace(2.0, 0.01, 140)], axis=1)
+    q = estimators.reduced_zeta(z, spec, 3, [0, 1, 2], tab)
+    assert q.shape == (3, 16)
+    assert np.all(np.isfinite(q))
