@@ -93,6 +93,28 @@ struct DevBuf {
     size_t bytes() const { return n * sizeof(T); }
 };
 
+// Page-locked host buffer (device-to-host copies inside captured graphs need one).
+template <typename T>
+struct PinnedBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    PinnedBuf() = default;
+    PinnedBuf(const PinnedBuf&) = delete;
+    PinnedBuf& operator=(const PinnedBuf&) = delete;
+    ~PinnedBuf() { release(); }
+    void release() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+    }
+    void reserve(size_t m) {
+        if (m <= n) return;
+        release();
+        CK(cudaMallocHost((void**)&p, std::max<size_t>(m, 1) * sizeof(T)));
+        n = m;
+    }
+};
+
 struct Box {
     float lo[3], hi[3];
 };
@@ -464,13 +486,27 @@ struct Lane {
     DevBuf<unsigned int> d_counters;  // [0] task counter, [1] recheck count, [2..5] evaluated/binned
     DevBuf<uint4> d_queue;
     DevBuf<unsigned long long> d_hist;
-    std::vector<unsigned long long> h_hist;
+    PinnedBuf<unsigned long long> h_hist;
+    PinnedBuf<unsigned int> h_counters;
     // last planned batch (see run_group)
     std::vector<uint64_t> plan_sig;
     size_t plan_ntasks = 0;
     uint64_t plan_evaluated = 0;
+    // the launch sequence of the last batch, captured as a CUDA graph and
+    // replayed while the batch and every buffer it touches stay the same
+    cudaGraphExec_t graph = nullptr;
+    std::vector<uint64_t> graph_sig;
+    bool graphs_ok = true;
     tpcf_stats stats{};
+    void drop_graph() {
+        if (graph) cudaGraphExecDestroy(graph);
+        graph = nullptr;
+        graph_sig.clear();
+    }
     void release() {
+        drop_graph();
+        h_hist.release();
+        h_counters.release();
         d_jobs.release();
         d_tasks.release();
         d_counters.release();
@@ -902,71 +938,121 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
         L.plan_ntasks = ntasks;
         L.plan_evaluated = evaluated;
     }
-    const bool fp64 = sp.precision == TPCF_PLAIN_FP64;
+    const bool fp64 = sp.precision != TPCF_GUARDED_FP32;
     if (sp.kind == TPCF_TRIANGLE) ensure_acos(ctx);
-    uint64_t launches = 0;
+    const AcosTable acos_t = sp.kind == TPCF_TRIANGLE ? acos_table(ctx) : AcosTable{};
+    // launch shape: warp-private histogram copies in shared memory
+    int copies = 8;
+    size_t smem = 0;
+    if (sp.kind == TPCF_TRIANGLE) {
+        // as many copies as still let three CTAs share an SM (the kernel is
+        // latency-bound and needs the warps)
+        const char* cap_env = getenv("TPCF_TRI_SMEM_CAP_KB");
+        size_t smem_cap = (cap_env ? (size_t)atoi(cap_env) : (size_t)74) * 1024;
+        while (copies > 1 && triangle_smem_bytes(bin.len, copies) > smem_cap) copies /= 2;
+        if (triangle_smem_bytes(bin.len, copies) > 227 * 1024) throw InvalidArg{"triangle histogram too large for shared memory"};
+        smem = triangle_smem_bytes(bin.len, copies);
+    } else if (sp.kind == TPCF_THREE_SIDE) {
+        while (copies > 0 && three_side_smem_bytes(bin.len, copies) > 200 * 1024) copies /= 2;
+        smem = three_side_smem_bytes(copies ? bin.len : 0, copies);
+    } else {
+        while (copies > 1 && pair_smem_bytes(bin.len, copies) > 200 * 1024) copies /= 2;
+        if (pair_smem_bytes(bin.len, copies) > 227 * 1024) throw InvalidArg{"pair histogram too large"};
+        smem = pair_smem_bytes(bin.len, copies);
+    }
+    const unsigned int nt = (unsigned int)ntasks;
+    const int grid = occupancy_grid(ctx, sp.kind, smem, fp64, nt);
+    const uint64_t launches = (sp.kind == TPCF_TRIANGLE && !fp64) ? 2 : 1;
+    const char* genv = getenv("TPCF_GRAPHS");
+    const bool graphs = L.graphs_ok && !(genv && genv[0] == '0');
+    L.h_hist.reserve(hist_total);
+    L.h_counters.reserve(8);
     unsigned int queue_cap = (unsigned int)std::max<size_t>(L.d_queue.n, (size_t)1 << 22);
-    uint64_t dev_evaluated = 0, dev_binned = 0;
+    uint64_t dev_evaluated = 0, dev_binned = 0, replays = 0;
     for (int attempt = 0; attempt < 3; attempt++) {
-        CK(cudaMemsetAsync(L.d_hist.p, 0, hist_total * sizeof(unsigned long long), st));
-        CK(cudaMemsetAsync(L.d_counters.p, 0, 8 * sizeof(unsigned int), st));
-        CK(cudaEventRecord(L.ev0, st));
-        unsigned int nt = (unsigned int)ntasks;
-        launches = 0;
-        if (sp.kind == TPCF_TRIANGLE) {
-            // warp-private histogram copies, as many as still let three CTAs
-            // share an SM (the kernel is latency-bound and needs the warps)
-            int copies = 8;
-            const char* cap_env = getenv("TPCF_TRI_SMEM_CAP_KB");
-            size_t smem_cap = (cap_env ? (size_t)atoi(cap_env) : (size_t)74) * 1024;
-            while (copies > 1 && triangle_smem_bytes(bin.len, copies) > smem_cap) copies /= 2;
-            if (triangle_smem_bytes(bin.len, copies) > 227 * 1024) throw InvalidArg{"triangle histogram too large for shared memory"};
-            size_t smem = triangle_smem_bytes(bin.len, copies);
-            int grid = occupancy_grid(ctx, sp.kind, smem, fp64, nt);
-            if (fp64) {
-                CK(launch_triangle_fp64(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.tri, acos_table(ctx),
-                                        grid, copies, st));
-                CK(cudaEventRecord(L.ev_mid, st));
-                launches = 1;
-            } else {
-                L.d_queue.reserve(queue_cap);
-                RecheckQueue q;
-                q.items = L.d_queue.p;
-                q.count = L.d_counters.p + 1;
-                q.cap = queue_cap;
-                q.evaluated = reinterpret_cast<unsigned long long*>(L.d_counters.p + 2);
-                CK(launch_triangle_fast(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.tri, q, grid, copies, st));
-                CK(cudaEventRecord(L.ev_mid, st));
-                CK(launch_triangle_recheck(L.d_jobs.p, q, bin.tri, acos_table(ctx), ctx->num_sms * 8, st));
-                launches = 2;
-            }
-        } else if (sp.kind == TPCF_THREE_SIDE) {
-            int copies = 8;
-            size_t smem_cap = 200 * 1024;
-            while (copies > 0 && three_side_smem_bytes(bin.len, copies) > smem_cap) copies /= 2;
-            size_t smem = three_side_smem_bytes(copies ? bin.len : 0, copies);
-            int grid = occupancy_grid(ctx, sp.kind, smem, fp64, nt);
-            CK(launch_three_side(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.three, fp64, grid, copies, st));
-            CK(cudaEventRecord(L.ev_mid, st));
-            launches = 1;
-        } else {
-            int copies = 8;
-            while (copies > 1 && pair_smem_bytes(bin.len, copies) > 200 * 1024) copies /= 2;
-            if (pair_smem_bytes(bin.len, copies) > 227 * 1024) throw InvalidArg{"pair histogram too large"};
-            size_t smem = pair_smem_bytes(bin.len, copies);
-            int grid = occupancy_grid(ctx, sp.kind, smem, fp64, nt);
-            CK(launch_pairs(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.pair, fp64, grid, copies, st));
-            CK(cudaEventRecord(L.ev_mid, st));
-            launches = 1;
+        RecheckQueue q{};
+        if (sp.kind == TPCF_TRIANGLE && !fp64) {
+            if (L.d_queue.n < queue_cap) L.drop_graph();
+            L.d_queue.reserve(queue_cap);
+            q.items = L.d_queue.p;
+            q.count = L.d_counters.p + 1;
+            q.cap = queue_cap;
+            q.evaluated = reinterpret_cast<unsigned long long*>(L.d_counters.p + 2);
         }
-        CK(cudaEventRecord(L.ev1, st));
-        unsigned int counters[8];
-        CK(cudaMemcpyAsync(counters, L.d_counters.p, sizeof(counters), cudaMemcpyDeviceToHost, st));
-        L.h_hist.resize(hist_total);
-        CK(cudaMemcpyAsync(L.h_hist.data(), L.d_hist.p, hist_total * sizeof(unsigned long long),
-                           cudaMemcpyDeviceToHost, st));
+        // the whole step as stream work: zero, count, recheck, copy back
+        auto enqueue = [&](bool capturing) -> cudaError_t {
+            const unsigned int ev_flags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+            cudaError_t e;
+#define EQ(x)                                 \
+    do {                                      \
+        if ((e = (x)) != cudaSuccess) return e; \
+    } while (0)
+            EQ(cudaMemsetAsync(L.d_hist.p, 0, hist_total * sizeof(unsigned long long), st));
+            EQ(cudaMemsetAsync(L.d_counters.p, 0, 8 * sizeof(unsigned int), st));
+            EQ(cudaEventRecordWithFlags(L.ev0, st, ev_flags));
+            if (sp.kind == TPCF_TRIANGLE && fp64) {
+                EQ(launch_triangle_fp64(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.tri, acos_t, grid, copies,
+                                        sp.precision == TPCF_GEOMETRY_FP64, st));
+                EQ(cudaEventRecordWithFlags(L.ev_mid, st, ev_flags));
+            } else if (sp.kind == TPCF_TRIANGLE) {
+                EQ(launch_triangle_fast(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.tri, q, grid, copies, st));
+                EQ(cudaEventRecordWithFlags(L.ev_mid, st, ev_flags));
+                EQ(launch_triangle_recheck(L.d_jobs.p, q, bin.tri, acos_t, ctx->num_sms * 8, st));
+            } else if (sp.kind == TPCF_THREE_SIDE) {
+                EQ(launch_three_side(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.three, fp64, grid, copies, st));
+                EQ(cudaEventRecordWithFlags(L.ev_mid, st, ev_flags));
+            } else {
+                EQ(launch_pairs(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.pair, fp64, grid, copies, st));
+                EQ(cudaEventRecordWithFlags(L.ev_mid, st, ev_flags));
+            }
+            EQ(cudaEventRecordWithFlags(L.ev1, st, ev_flags));
+            EQ(cudaMemcpyAsync(L.h_counters.p, L.d_counters.p, 8 * sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
+            EQ(cudaMemcpyAsync(L.h_hist.p, L.d_hist.p, hist_total * sizeof(unsigned long long),
+                               cudaMemcpyDeviceToHost, st));
+#undef EQ
+            return cudaSuccess;
+        };
+        bool replayed = false;
+        if (graphs) {
+            // everything the captured launches read: the batch, its buffers, the shape
+            std::vector<uint64_t> gsig = sig;
+            const uint64_t extra[] = {(uint64_t)(uintptr_t)L.d_jobs.p, (uint64_t)(uintptr_t)L.d_tasks.p,
+                                      (uint64_t)(uintptr_t)L.d_counters.p, (uint64_t)(uintptr_t)L.d_queue.p,
+                                      (uint64_t)(uintptr_t)L.h_hist.p, (uint64_t)(uintptr_t)L.h_counters.p,
+                                      (uint64_t)(uintptr_t)acos_t.keys, (uint64_t)(uintptr_t)acos_t.vals,
+                                      (uint64_t)(uintptr_t)acos_t.bucket, (uint64_t)acos_t.n, queue_cap, (uint64_t)grid,
+                                      (uint64_t)copies, hist_total, ntasks};
+            gsig.insert(gsig.end(), extra, extra + sizeof(extra) / sizeof(extra[0]));
+            if (!L.graph || gsig != L.graph_sig) {
+                L.drop_graph();
+                cudaGraph_t g = nullptr;
+                cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+                if (e == cudaSuccess) {
+                    cudaError_t e1 = enqueue(true);
+                    cudaError_t e2 = cudaStreamEndCapture(st, &g);
+                    e = e1 != cudaSuccess ? e1 : e2;
+                }
+                if (e == cudaSuccess) e = cudaGraphInstantiate(&L.graph, g, 0);
+                if (g) cudaGraphDestroy(g);
+                if (e == cudaSuccess) {
+                    L.graph_sig = gsig;
+                } else {
+                    // capture unavailable here: issue the launches one by one from now on
+                    (void)cudaGetLastError();
+                    L.graph = nullptr;
+                    L.graphs_ok = false;
+                }
+            }
+            if (L.graph) {
+                CK(cudaGraphLaunch(L.graph, st));
+                replayed = true;
+            }
+        }
+        if (!replayed) CK(enqueue(false));
         CK(cudaStreamSynchronize(st));
-        L.d2h += sizeof(counters) + hist_total * sizeof(unsigned long long);
+        replays = replayed ? 1 : 0;
+        const unsigned int* counters = L.h_counters.p;
+        L.d2h += 8 * sizeof(unsigned int) + hist_total * sizeof(unsigned long long);
         L.stats.recheck_units = counters[1];
         memcpy(&dev_evaluated, &counters[2], sizeof(dev_evaluated));
         memcpy(&dev_binned, &counters[4], sizeof(dev_binned));
@@ -982,7 +1068,8 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
     CK(cudaEventElapsedTime(&ms_main, L.ev0, L.ev_mid));
     L.stats.main_kernel_ms = ms_main;
     for (size_t g = 0; g < group.size(); g++)
-        memcpy(group[g].out, L.h_hist.data() + (size_t)bin.len * g, (size_t)bin.len * sizeof(uint64_t));
+        memcpy(group[g].out, L.h_hist.p + (size_t)bin.len * g, (size_t)bin.len * sizeof(uint64_t));
+    L.stats.graph_replays = replays;
     L.stats.kernel_ms = ms;
     L.stats.loop_units = units;
     // the fast triangle kernel skips (i,j) pairs that no counted triangle can
@@ -1000,7 +1087,10 @@ void validate(const tpcf_spec* sp, const tpcf_job* job) {
     if (!sp || !job) throw InvalidArg{"null spec or job"};
     if (sp->kind != TPCF_THREE_SIDE && sp->kind != TPCF_TRIANGLE && sp->kind != TPCF_PAIR) throw InvalidArg{"bad kind"};
     if (sp->loop < TPCF_LOOP_ALL || sp->loop > TPCF_LOOP_ONE) throw InvalidArg{"bad loop"};
-    if (sp->precision != TPCF_GUARDED_FP32 && sp->precision != TPCF_PLAIN_FP64) throw InvalidArg{"bad precision"};
+    if (sp->precision != TPCF_GUARDED_FP32 && sp->precision != TPCF_PLAIN_FP64 && sp->precision != TPCF_GEOMETRY_FP64)
+        throw InvalidArg{"bad precision"};
+    if (sp->precision == TPCF_GEOMETRY_FP64 && sp->kind != TPCF_TRIANGLE)
+        throw InvalidArg{"TPCF_GEOMETRY_FP64 is implemented for the triangle parametrization only"};
     (void)make_binning(*sp);
 }
 
@@ -1314,6 +1404,7 @@ tpcf_status tpcf_count_batch(tpcf_ctx* ctx, const tpcf_spec* specs, const tpcf_j
             acc.recheck_units += L.stats.recheck_units;
             acc.tasks += L.stats.tasks;
             acc.kernel_launches += L.stats.kernel_launches;
+            acc.graph_replays += L.stats.graph_replays;
         }
         ctx->lanes[0]->stats = acc;
     });

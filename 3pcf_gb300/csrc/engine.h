@@ -118,7 +118,7 @@ cudaError_t launch_triangle_recheck(const DevJob* jobs, RecheckQueue q, const Tr
                                     int grid, cudaStream_t st);
 cudaError_t launch_triangle_fp64(const DevJob* jobs, const uint4* tasks, unsigned int ntasks,
                                  unsigned int* task_counter, const TriParams& p, AcosTable t, int grid,
-                                 int hist_copies, cudaStream_t st);
+                                 int hist_copies, bool geometry, cudaStream_t st);
 cudaError_t launch_three_side(const DevJob* jobs, const uint4* tasks, unsigned int ntasks,
                               unsigned int* task_counter, const ThreeParams& p, int fp64, int grid,
                               int hist_copies, cudaStream_t st);

@@ -156,6 +156,77 @@ __device__ void tp_exact(float dist0, float dist1, float dist2, const TriParams&
 }
 
 // ---------------------------------------------------------------------------
+// The same triangle formulas evaluated in double from the float coordinates,
+// acos in double: not the reference's float arithmetic, but the FP64 truth
+// the derived correlation function's error is quoted against.  Every
+// operation is an explicit round-to-nearest double op (no contraction), so a
+// host restatement compiled without FMA contraction agrees except where the
+// two acos implementations differ.
+
+__device__ __forceinline__ double geo_dist(float4 a, float4 b) {
+    double dx = __dsub_rn((double)a.x, (double)b.x);
+    double dy = __dsub_rn((double)a.y, (double)b.y);
+    double dz = __dsub_rn((double)a.z, (double)b.z);
+    double s = __dmul_rn(dx, dx);
+    s = __dadd_rn(s, __dmul_rn(dy, dy));
+    s = __dadd_rn(s, __dmul_rn(dz, dz));
+    return __dsqrt_rn(s);
+}
+
+__device__ __forceinline__ int geo_bin(double v, float lo, float hi, int n, int nan_zero) {
+    double bw = __ddiv_rn(__dsub_rn((double)hi, (double)lo), (double)n);
+    if (v < (double)lo) return -999;
+    if (v >= (double)hi) return -999;
+    if (v != v) return nan_zero ? 0 : INT_MIN;
+    return __double2int_rz(__ddiv_rn(__dsub_rn(v, (double)lo), bw));
+}
+
+__device__ void tp_geom(double d0, double d1, double d2, const TriParams& p, int out[3]) {
+    // shortest <= middle <= longest with the reference's tie handling
+    double shortest, middle, longest;
+    if (d0 > d1) {
+        if (d0 > d2) {
+            longest = d0;
+            if (d1 > d2) { middle = d1; shortest = d2; }
+            else { middle = d2; shortest = d1; }
+        } else {
+            middle = d0;
+            if (d1 > d2) { longest = d1; shortest = d2; }
+            else { longest = d2; shortest = d1; }
+        }
+    } else {
+        if (d1 > d2) {
+            longest = d1;
+            if (d0 > d2) { middle = d0; shortest = d2; }
+            else { middle = d2; shortest = d0; }
+        } else {
+            middle = d1; longest = d2; shortest = d0;
+        }
+    }
+    const double s2 = __dmul_rn(shortest, shortest), m2 = __dmul_rn(middle, middle), l2 = __dmul_rn(longest, longest);
+    const bool zero = d0 == 0.0 || d1 == 0.0 || d2 == 0.0;
+    double c0 = __ddiv_rn(__dsub_rn(__dadd_rn(s2, m2), l2), __dmul_rn(__dmul_rn(2.0, shortest), middle));
+    double c1 = __ddiv_rn(__dsub_rn(__dadd_rn(m2, l2), s2), __dmul_rn(__dmul_rn(2.0, middle), longest));
+    double th0 = __ddiv_rn(acos(c0), 3.14159), th1 = __ddiv_rn(acos(c1), 3.14159);
+    double th2 = __dsub_rn(__dsub_rn(1.0, th0), th1);
+    const double sv[3] = {shortest, middle, shortest};
+    const double qv[3] = {__ddiv_rn(middle, shortest), __ddiv_rn(longest, middle), __ddiv_rn(longest, shortest)};
+    const double tv[3] = {th0, th1, th2};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        int i0 = geo_bin(sv[k], p.s_lo, p.s_hi, p.S, p.nan_zero);
+        int i1 = geo_bin(qv[k], p.q_lo, p.q_hi, p.Q, p.nan_zero);
+        int i2 = geo_bin(tv[k], p.t_lo, p.t_hi, p.T, p.nan_zero);
+        int tot = -1;
+        if (!(i0 < 0 || i1 < 0 || i2 < 0) && !zero) {
+            long long idx = (long long)p.Q * p.T * i0 + (long long)p.T * i1 + i2;
+            if (idx < p.len) tot = (int)idx;
+        }
+        out[k] = tot;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Persistent-task plumbing.
 
 constexpr unsigned int FLUSH_EVERY = 256;  // tasks between histogram flushes (u32 safety)
@@ -192,14 +263,17 @@ constexpr int TRI_WARPS = 8;
 constexpr int TRI_THREADS = TRI_WARPS * 32;
 constexpr int TRI_QCAP = 128;  // per-warp candidate queue: up to 63 pending + 64 new
 // per j of role B: bit masks over k of the classes of side j-k (B, I, M, H)
-// and of key_k >= key_j
+// and of key_k >= key_j; held in shared memory as five 64-entry arrays
+// (JM_WORDS x TILE, word-major) so that lanes reading different j's do not
+// share banks
 struct JMasks {
     unsigned long long c[4];
     unsigned long long kge;
 };
+constexpr int JM_WORDS = 5;
 constexpr size_t TRI_SMEM_FIXED = 3 * TILE * sizeof(float4) + TILE * TILE * sizeof(int2) +
                                   2 * TRI_WARPS * TILE * sizeof(int2) + TRI_WARPS * TRI_QCAP * sizeof(uint32_t) +
-                                  TRI_WARPS * TILE * sizeof(uint32_t) + TILE * sizeof(JMasks);
+                                  JM_WORDS * TILE * sizeof(unsigned long long);
 
 // s-bin code of one side, monotone in the side length, multiplied by Q*T
 // (used by the plain FP64 kernel).
@@ -407,9 +481,10 @@ __device__ __forceinline__ unsigned long long ballot64(bool lo, bool hi) {
 // side at/above s_hi*q_hi) or permutation 1 (no side at/above s_hi*q_hi, at
 // most one below s_lo, at most one in [s_hi, s_hi*q_hi)); these are the
 // (class_ik, class_jk) combinations that leave one of the two possible.
-__device__ __forceinline__ unsigned long long candidate_mask(int cij, const unsigned long long n[4], const JMasks& m) {
-    const unsigned long long nB = n[0], nI = n[1], nM = n[2], nH = n[3];
-    const unsigned long long mB = m.c[0], mI = m.c[1], mM = m.c[2], mH = m.c[3];
+__device__ __forceinline__ unsigned long long candidate_mask(int cij, unsigned long long nB, unsigned long long nI,
+                                                             unsigned long long nM, unsigned long long nH,
+                                                             unsigned long long mB, unsigned long long mI,
+                                                             unsigned long long mM, unsigned long long mH) {
     if (cij == 2) return (nB | nI | nM | nH) & (mB | mI | mM | mH) & ~((nB | nH) & (mB | mH));
     if (cij == 3) return (nI & (mB | mI | mM | mH)) | ((nB | nI | nM | nH) & mI);
     return (nI & (mI | mM)) | (nM & mI);  // cij == 1 or 4
@@ -417,7 +492,7 @@ __device__ __forceinline__ unsigned long long candidate_mask(int cij, const unsi
 
 template <int PRED, bool THETA_FULL>
 __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams& p, float4* P, int2* JK,
-                                   int2* IJ, int2* IK, uint32_t* Q, uint32_t* JL, JMasks* JM, unsigned int* Hw,
+                                   int2* IJ, int2* IK, uint32_t* Q, unsigned long long* JM, unsigned int* Hw,
                                    RecheckQueue& q, unsigned long long& evaluated, unsigned long long& binned,
                                    int* next_i) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -449,13 +524,13 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
         for (int c = 0; c < 4; c++) m.c[c] = ballot64(c0 == c + 1, c1 == c + 1);
         const int kj = pkey(pj);
         m.kge = ballot64(lane < g.nC && key_k0 >= kj, lane + 32 < g.nC && key_k1 >= kj);
-        if (lane == 0) JM[j] = m;
+        if (lane < 4) JM[lane * TILE + j] = m.c[lane];
+        if (lane == 4) JM[4 * TILE + j] = m.kge;
     }
     __syncthreads();
     int2* row_ij = IJ + warp * TILE;
     int2* row_ik = IK + warp * TILE;
     uint32_t* cand = Q + warp * TRI_QCAP;
-    uint32_t* jlist = JL + warp * TILE;
     const unsigned lt = (1u << lane) - 1u;
     unsigned ev = 0, bn = 0;
     for (;;) {
@@ -481,71 +556,82 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
             row_ik[lane + 32] = make_int2(__float_as_int(d), w);
             c1 = side_class(w, d, p);
         }
-        unsigned long long n[4];
-#pragma unroll
-        for (int c = 0; c < 4; c++) n[c] = ballot64(c0 == c + 1, c1 == c + 1);
-        const unsigned long long any_k = n[0] | n[1] | n[2] | n[3];
+        const unsigned long long nB = ballot64(c0 == 1, c1 == 1), nI = ballot64(c0 == 2, c1 == 2);
+        const unsigned long long nM = ballot64(c0 == 3, c1 == 3), nH = ballot64(c0 == 4, c1 == 4);
+        const unsigned long long any_k = nB | nI | nM | nH;
         unsigned long long kge_i = 0;
         if (PRED == PRED_DDR) kge_i = ballot64(lane < g.nC && key_k0 >= ki, lane + 32 < g.nC && key_k1 >= ki);
-        // i-j sides: words, and the list of j that can be in a counted triangle
-        bool ja = false, jb = false;
-        uint32_t ea = 0, eb = 0;
-        for (int h = 0; h < 2; h++) {
-            const int j = lane + 32 * h;
-            bool ok = false;
-            uint32_t e = 0;
-            if (j < g.nB) {
-                float d = ref_dist<false>(pi, P[TILE + j]);
-                int w = tri_side_word(d, p);
-                row_ij[j] = make_int2(__float_as_int(d), w);
-                int c = side_class(w, d, p);
-                ok = c != 0 && (!diag_ij || j > i);
-                if (PRED == PRED_SAME) ok = ok && ki <= pkey(P[TILE + j]);
-                e = (uint32_t)j | ((uint32_t)c << 8);
+        // i-j sides: words for the binning path; each lane then forms the
+        // candidate-k mask of its own two j's (the scan over j is lane-parallel)
+        // mask of candidate k's (and of weight-2 k's) of the pair (i, j)
+        auto scan_j = [&](int j, unsigned long long& cm, unsigned long long& w2) -> bool {
+            cm = 0;
+            w2 = 0;
+            if (j >= g.nB) return false;
+            float d = ref_dist<false>(pi, P[TILE + j]);
+            int w = tri_side_word(d, p);
+            row_ij[j] = make_int2(__float_as_int(d), w);
+            const int c = side_class(w, d, p);
+            bool ok = c != 0 && any_k && (!diag_ij || j > i);
+            if (PRED == PRED_SAME) ok = ok && ki <= pkey(P[TILE + j]);
+            if (!ok) return false;
+            cm = candidate_mask(c, nB, nI, nM, nH, JM[j], JM[TILE + j], JM[2 * TILE + j], JM[3 * TILE + j]);
+            if (diag_jk) cm &= j >= 63 ? 0ull : (~0ull << (j + 1));
+            if (PRED != PRED_NONE) {
+                const unsigned long long kge_j = JM[4 * TILE + j];
+                if (PRED == PRED_DDR) {
+                    w2 = cm & kge_i & kge_j;  // weight 2: k >= i and k >= j
+                    cm &= kge_i | kge_j;      // weight 0 otherwise
+                } else {
+                    cm &= kge_j;              // key_j <= key_k
+                }
             }
-            if (h == 0) { ja = ok; ea = e; } else { jb = ok; eb = e; }
-        }
-        const unsigned bja = __ballot_sync(0xffffffffu, ja), bjb = __ballot_sync(0xffffffffu, jb);
-        if (ja) jlist[__popc(bja & lt)] = ea;
-        if (jb) jlist[__popc(bja) + __popc(bjb & lt)] = eb;
-        const int nj = any_k ? __popc(bja) + __popc(bjb) : 0;
+            return true;
+        };
+        unsigned long long cm0, w20, cm1, w21;
+        const bool ok0 = scan_j(lane, cm0, w20);
+        const bool ok1 = scan_j(lane + 32, cm1, w21);
+        // walked (i, j, k): every k with a usable i-k side, for every usable j
+        ev += (unsigned)__popcll(any_k) *
+              (unsigned)(__popc(__ballot_sync(0xffffffffu, ok0)) + __popc(__ballot_sync(0xffffffffu, ok1)));
         __syncwarp();
         const uint32_t ia = (uint32_t)(g.a0 + i);
         int qn = 0;  // queued candidates (warp-uniform)
-        for (int t = 0; t < nj; t++) {
-            const uint32_t e = jlist[t];
-            const int j = e & 63, cij = (int)(e >> 8);
-            const JMasks m = JM[j];
-            unsigned long long cm = candidate_mask(cij, n, m);
-            if (diag_jk) cm &= j >= 63 ? 0ull : (~0ull << (j + 1));
-            unsigned long long w2 = 0;
-            if (PRED == PRED_DDR) {
-                w2 = cm & kge_i & m.kge;           // weight 2: k >= i and k >= j
-                cm &= kge_i | m.kge;               // weight 0 otherwise
-            } else if (PRED == PRED_SAME || PRED == PRED_ONE) {
-                cm &= m.kge;                       // key_j <= key_k
-            }
-            ev += (unsigned)__popcll(any_k);
-            if (!cm) continue;
-            const unsigned lo = (unsigned)cm, hi = (unsigned)(cm >> 32);
-            const int nlo = __popc(lo);
-            if ((lo >> lane) & 1u) {
-                const unsigned w = PRED == PRED_DDR ? 1u + (unsigned)((w2 >> lane) & 1ull) : 1u;
-                cand[qn + __popc(lo & lt)] = pack_cand(j, lane, w);
-            }
-            if ((hi >> lane) & 1u) {
-                const unsigned w = PRED == PRED_DDR ? 1u + (unsigned)((w2 >> (lane + 32)) & 1ull) : 1u;
-                cand[qn + nlo + __popc(hi & lt)] = pack_cand(j, lane + 32, w);
-            }
-            qn += nlo + __popc(hi);
-            __syncwarp();
-            if (qn >= 64) {
-                qn -= 64;
-                run_candidates<THETA_FULL>(cand + qn, 64, row_ij, row_ik, JK, p, Hw, q, slot, ia, g.b0, g.c0);
-                bn += 64;
+        // queue the candidates of every j whose mask is not empty, in turn
+        auto emit = [&](unsigned long long cmv, unsigned long long w2v, int jbase) {
+            unsigned live = __ballot_sync(0xffffffffu, cmv != 0ull);
+            while (live) {
+                const int src = __ffs(live) - 1;
+                live &= live - 1u;
+                const int j = src + jbase;
+                const unsigned lo = __shfl_sync(0xffffffffu, (unsigned)cmv, src);
+                const unsigned hi = __shfl_sync(0xffffffffu, (unsigned)(cmv >> 32), src);
+                unsigned w2lo = 0, w2hi = 0;
+                if (PRED == PRED_DDR) {
+                    w2lo = __shfl_sync(0xffffffffu, (unsigned)w2v, src);
+                    w2hi = __shfl_sync(0xffffffffu, (unsigned)(w2v >> 32), src);
+                }
+                const int nlo = __popc(lo);
+                if ((lo >> lane) & 1u) {
+                    const unsigned w = PRED == PRED_DDR ? 1u + ((w2lo >> lane) & 1u) : 1u;
+                    cand[qn + __popc(lo & lt)] = pack_cand(j, lane, w);
+                }
+                if ((hi >> lane) & 1u) {
+                    const unsigned w = PRED == PRED_DDR ? 1u + ((w2hi >> lane) & 1u) : 1u;
+                    cand[qn + nlo + __popc(hi & lt)] = pack_cand(j, lane + 32, w);
+                }
+                qn += nlo + __popc(hi);
                 __syncwarp();
+                if (qn >= 64) {
+                    qn -= 64;
+                    run_candidates<THETA_FULL>(cand + qn, 64, row_ij, row_ik, JK, p, Hw, q, slot, ia, g.b0, g.c0);
+                    bn += 64;
+                    __syncwarp();
+                }
             }
-        }
+        };
+        emit(cm0, w20, 0);
+        emit(cm1, w21, 32);
         if (qn > 0) {
             run_candidates<THETA_FULL>(cand, qn, row_ij, row_ik, JK, p, Hw, q, slot, ia, g.b0, g.c0);
             bn += qn;
@@ -558,14 +644,14 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
 
 template <bool THETA_FULL>
 __device__ __forceinline__ void triangle_dispatch(const DevJob& J, uint4 task, const TriParams& p, float4* P,
-                                                  int2* JK, int2* IJ, int2* IK, uint32_t* Q, uint32_t* KL,
-                                                  JMasks* JM, unsigned int* Hw, RecheckQueue& q,
+                                                  int2* JK, int2* IJ, int2* IK, uint32_t* Q,
+                                                  unsigned long long* JM, unsigned int* Hw, RecheckQueue& q,
                                                   unsigned long long& ev, unsigned long long& bn, int* next_i) {
     switch ((task.x >> TASK_PRED_SHIFT) & 0xFF) {
-        case PRED_NONE: triangle_task_fast<PRED_NONE, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, KL, JM, Hw, q, ev, bn, next_i); break;
-        case PRED_DDR: triangle_task_fast<PRED_DDR, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, KL, JM, Hw, q, ev, bn, next_i); break;
-        case PRED_SAME: triangle_task_fast<PRED_SAME, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, KL, JM, Hw, q, ev, bn, next_i); break;
-        default: triangle_task_fast<PRED_ONE, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, KL, JM, Hw, q, ev, bn, next_i); break;
+        case PRED_NONE: triangle_task_fast<PRED_NONE, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, JM, Hw, q, ev, bn, next_i); break;
+        case PRED_DDR: triangle_task_fast<PRED_DDR, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, JM, Hw, q, ev, bn, next_i); break;
+        case PRED_SAME: triangle_task_fast<PRED_SAME, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, JM, Hw, q, ev, bn, next_i); break;
+        default: triangle_task_fast<PRED_ONE, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, JM, Hw, q, ev, bn, next_i); break;
     }
 }
 
@@ -582,9 +668,8 @@ triangle_fast_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ 
     int2* IJ = JK + TILE * TILE;
     int2* IK = IJ + TRI_WARPS * TILE;
     uint32_t* Q = reinterpret_cast<uint32_t*>(IK + TRI_WARPS * TILE);
-    uint32_t* KL = Q + TRI_WARPS * TRI_QCAP;
-    JMasks* JM = reinterpret_cast<JMasks*>(KL + TRI_WARPS * TILE);
-    unsigned int* H = reinterpret_cast<unsigned int*>(JM + TILE);
+    unsigned long long* JM = reinterpret_cast<unsigned long long*>(Q + TRI_WARPS * TRI_QCAP);
+    unsigned int* H = reinterpret_cast<unsigned int*>(JM + JM_WORDS * TILE);
     __shared__ uint4 s_task;
     __shared__ int s_next_i;
     for (int b = threadIdx.x; b < copies * p.len; b += blockDim.x) H[b] = 0;
@@ -608,7 +693,7 @@ triangle_fast_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ 
         cur = slot;
         if (slot < 0) break;
         since++;
-        triangle_dispatch<THETA_FULL>(jobs[slot], task, p, P, JK, IJ, IK, Q, KL, JM, Hw, q, ev, bn, &s_next_i);
+        triangle_dispatch<THETA_FULL>(jobs[slot], task, p, P, JK, IJ, IK, Q, JM, Hw, q, ev, bn, &s_next_i);
     }
     if ((threadIdx.x & 31) == 0) {
         if (ev) atomicAdd(q.evaluated, ev);
@@ -636,33 +721,46 @@ __global__ void triangle_recheck_kernel(const DevJob* __restrict__ jobs, Recheck
 // Triangle parametrization, plain FP64: every triangle through the exact
 // reference arithmetic with each float operation done in FP64.
 
-template <int PRED>
+template <bool GEOM> struct SideReal { typedef float type; };
+template <> struct SideReal<true> { typedef double type; };
+
+template <bool GEOM>
+__device__ __forceinline__ typename SideReal<GEOM>::type side_fp64(float4 a, float4 b) {
+    if constexpr (GEOM) return geo_dist(a, b);
+    else return ref_dist<true>(a, b);
+}
+
+// GEOM false: the reference's float arithmetic done in FP64 (identical
+// histograms); true: the FP64-geometry truth (tp_geom).
+template <int PRED, bool GEOM>
 __device__ void triangle_task_fp64(const DevJob& J, uint4 task, const TriParams& p, const AcosTable& t,
                                    float4* P, int2* JK, int2* IJ, unsigned int* Hw) {
+    typedef typename SideReal<GEOM>::type R;  // at most 8 bytes: fits the int2 slots
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const TaskGeom g = task_geom(J, task);
     const bool diag_ij = task.x & TASK_DIAG_IJ, diag_jk = task.x & TASK_DIAG_JK;
+    R* jk = reinterpret_cast<R*>(JK);
     load_points(P, J, g);
     __syncthreads();
     for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
         int j = e / TILE, k = e % TILE;
-        if (j < g.nB && k < g.nC) JK[e].x = __float_as_int(ref_dist<true>(P[TILE + j], P[2 * TILE + k]));
+        if (j < g.nB && k < g.nC) jk[e] = side_fp64<GEOM>(P[TILE + j], P[2 * TILE + k]);
     }
     __syncthreads();
-    int2* row = IJ + warp * TILE;
+    R* row = reinterpret_cast<R*>(IJ + warp * TILE);
     for (int i = warp; i < g.nA; i += TRI_WARPS) {
         const float4 pi = P[i];
-        float dik[2];
+        R dik[2];
 #pragma unroll
         for (int r = 0; r < 2; r++) {
             int k = lane + 32 * r;
-            dik[r] = k < g.nC ? ref_dist<true>(pi, P[2 * TILE + k]) : 0.f;
-            if (k < g.nB) row[k].x = __float_as_int(ref_dist<true>(pi, P[TILE + k]));
+            dik[r] = k < g.nC ? side_fp64<GEOM>(pi, P[2 * TILE + k]) : (R)0;
+            if (k < g.nB) row[k] = side_fp64<GEOM>(pi, P[TILE + k]);
         }
         __syncwarp();
         const int ki = pkey(pi);
         for (int j = diag_ij ? i + 1 : 0; j < g.nB; j++) {
-            const float dij = __int_as_float(row[j].x);
+            const R dij = row[j];
             const int kj = pkey(P[TILE + j]);
             if (PRED == PRED_SAME && !(ki <= kj)) continue;
 #pragma unroll
@@ -675,7 +773,8 @@ __device__ void triangle_task_fp64(const DevJob& J, uint4 task, const TriParams&
                 if (PRED == PRED_SAME || PRED == PRED_ONE) w = kj <= kkey ? 1u : 0u;
                 if (!w) continue;
                 int out[3];
-                tp_exact<true>(dij, dik[r], __int_as_float(JK[j * TILE + k].x), p, t, out);
+                if constexpr (GEOM) tp_geom(dij, dik[r], jk[j * TILE + k], p, out);
+                else tp_exact<true>(dij, dik[r], jk[j * TILE + k], p, t, out);
                 for (int b = 0; b < 3; b++)
                     if (out[b] >= 0) atomicAdd(Hw + out[b], w);
             }
@@ -684,6 +783,7 @@ __device__ void triangle_task_fp64(const DevJob& J, uint4 task, const TriParams&
     }
 }
 
+template <bool GEOM>
 __global__ void __launch_bounds__(TRI_THREADS, 1)
 triangle_fp64_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ tasks, unsigned int ntasks,
                      unsigned int* task_counter, TriParams p, AcosTable t, int copies) {
@@ -715,10 +815,10 @@ triangle_fp64_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ 
         since++;
         const DevJob& J = jobs[slot];
         switch ((task.x >> TASK_PRED_SHIFT) & 0xFF) {
-            case PRED_NONE: triangle_task_fp64<PRED_NONE>(J, task, p, t, P, JK, IJ, Hw); break;
-            case PRED_DDR: triangle_task_fp64<PRED_DDR>(J, task, p, t, P, JK, IJ, Hw); break;
-            case PRED_SAME: triangle_task_fp64<PRED_SAME>(J, task, p, t, P, JK, IJ, Hw); break;
-            default: triangle_task_fp64<PRED_ONE>(J, task, p, t, P, JK, IJ, Hw); break;
+            case PRED_NONE: triangle_task_fp64<PRED_NONE, GEOM>(J, task, p, t, P, JK, IJ, Hw); break;
+            case PRED_DDR: triangle_task_fp64<PRED_DDR, GEOM>(J, task, p, t, P, JK, IJ, Hw); break;
+            case PRED_SAME: triangle_task_fp64<PRED_SAME, GEOM>(J, task, p, t, P, JK, IJ, Hw); break;
+            default: triangle_task_fp64<PRED_ONE, GEOM>(J, task, p, t, P, JK, IJ, Hw); break;
         }
     }
 }
@@ -935,11 +1035,12 @@ cudaError_t launch_triangle_recheck(const DevJob* jobs, RecheckQueue q, const Tr
 
 cudaError_t launch_triangle_fp64(const DevJob* jobs, const uint4* tasks, unsigned int ntasks,
                                  unsigned int* task_counter, const TriParams& p, AcosTable t, int grid, int copies,
-                                 cudaStream_t st) {
+                                 bool geom, cudaStream_t st) {
     size_t smem = triangle_smem_bytes(p.len, copies);
-    cudaError_t e = cudaFuncSetAttribute(triangle_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    auto kern = geom ? triangle_fp64_kernel<true> : triangle_fp64_kernel<false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    triangle_fp64_kernel<<<grid, TRI_THREADS, smem, st>>>(jobs, tasks, ntasks, task_counter, p, t, copies);
+    kern<<<grid, TRI_THREADS, smem, st>>>(jobs, tasks, ntasks, task_counter, p, t, copies);
     return cudaGetLastError();
 }
 

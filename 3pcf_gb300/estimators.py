@@ -109,3 +109,18 @@ def reduced_zeta(z, spec, sbin, qbins, xi_tab):
         with np.errstate(divide="ignore", invalid="ignore"):
             out.append(z[sbin, qb] / den)
     return np.array(out)
+
+
+def zeta_error(z, z_ref, rrr):
+    """Error of zeta against a reference zeta (e.g. from FP64-geometry counts)
+    over the bins where RRR is populated: max and RMS absolute difference and
+    the largest difference relative to max(|z_ref|, 1e-12)."""
+    z = np.asarray(z, dtype=np.float64).ravel()
+    z_ref = np.asarray(z_ref, dtype=np.float64).ravel()
+    m = np.asarray(rrr).ravel() > 0
+    if not m.any():
+        return {"bins": 0, "max_abs": 0.0, "rms": 0.0, "max_rel": 0.0}
+    d = np.abs(z[m] - z_ref[m])
+    rel = d / np.maximum(np.abs(z_ref[m]), 1e-12)
+    return {"bins": int(m.sum()), "max_abs": float(d.max()), "rms": float(np.sqrt(np.mean(d * d))),
+            "max_rel": float(rel.max())}

@@ -15,7 +15,7 @@ BIN_DIR = os.path.join(HERE, "bin")
 
 THREE_SIDE, TRIANGLE, PAIR = 0, 1, 2
 LOOP_ALL, LOOP_SAME, LOOP_ONE = 0, 1, 2
-GUARDED_FP32, PLAIN_FP64 = 0, 1
+GUARDED_FP32, PLAIN_FP64, GEOMETRY_FP64 = 0, 1, 2
 NAN_INT_MIN, NAN_ZERO = 0, 1
 OVERFLOW_COMPAT, OVERFLOW_CLEAN = 0, 1
 
@@ -53,7 +53,7 @@ class Stats(ctypes.Structure):
                 ("evaluated_units", ctypes.c_uint64), ("recheck_units", ctypes.c_uint64),
                 ("tasks", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64),
                 ("main_kernel_ms", ctypes.c_double), ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
-                ("binned_units", ctypes.c_uint64)]
+                ("binned_units", ctypes.c_uint64), ("graph_replays", ctypes.c_uint64)]
 
 
 _LIB = None

@@ -374,6 +374,26 @@ def impl_ours(args):
         fp64 = {"value": units / (st["kernel_ms"] / 1e3), "unit": "triangles/s", "ms_per_step": st["kernel_ms"],
                 "guarded_over_fp64": (units / (statistics.mean(dev_ms) / 1e3)) / (units / (st["kernel_ms"] / 1e3))}
 
+    # Szapudi-Szalay zeta from the bit-exact counts, and its error against
+    # zeta from FP64-geometry counts (one step of the FP64-geometry kernel)
+    zeta = None
+    if not args.no_fp64:
+        import estimators
+        hg = eng.count_batch(specs(tpcf.GEOMETRY_FP64), jobs)
+        geo_ms = eng.stats()["kernel_ms"]
+        nd, nr = len(d), len(r)
+        ns = [(nd, nd, nd), (nd, nd, nr), (nd, nr, nr), (nr, nr, nr)]
+        z = estimators.zeta(*ref_hists, *ns)
+        zg = estimators.zeta(*hg, *ns)
+        err = estimators.zeta_error(z, zg, ref_hists[3])
+        pop = ref_hists[3] > 0
+        zeta = {"estimator": "Szapudi-Szalay (DDD - 3DDR + 3DRR - RRR)/RRR", "fp64_oracle": "same formulas in double "
+                "from the float coordinates (TPCF_GEOMETRY_FP64 kernel)", "fp64_ms": geo_ms,
+                "populated_bins": err["bins"], "mean": float(np.mean(z[pop])) if pop.any() else 0.0,
+                "max_abs_err": err["max_abs"], "rms_err": err["rms"], "max_rel_err": err["max_rel"],
+                "counts_moved": int(sum(np.abs(a.astype(np.int64) - b.astype(np.int64)).sum()
+                                        for a, b in zip(ref_hists, hg)))}
+
     if rank != 0:
         eng.close()
         return 0
@@ -403,6 +423,7 @@ def impl_ours(args):
         "e2e": {"value": e2e_value, "unit": "triangles/s", "ms_per_step": e2e_s * 1e3, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "plain_fp64": fp64,
+        "zeta": zeta,
         "roofline": {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "Tinst/s",
                      "frac": achieved / peak, "traffic": traffic_per_launch(),
                      "kernel": "triangle_fast_kernel", "per_unit": "%d lane-instructions per binned triangle (one that reaches the s/q/theta arithmetic)" % W_TP,
@@ -485,41 +506,59 @@ def _jackknife_region(xyz):
 
 
 def run_voxel(args):
-    """configs[2]: 100k clustered + 100k uniform points in a 20x20 degree light-cone
-    slab (depth 500-1500), triangle parametrization DDD/DDR/DRR/RRR of the full
-    catalogs and of the 16 jackknife subsamples (one 4x4 angular cell left out
-    each): 68 jobs of uneven size in one persistent launch."""
+    """configs[2]: 100k clustered + 100k uniform points in a 20x20 degree
+    light-cone slab (depth 500-1500, density falling as r^-2), ordered by depth
+    as a light-cone catalog is.  One step = one launch of 4068 triangle jobs
+    of very uneven size: the reference's voxel decomposition with division 10
+    (every -x iiijjjkkk chunk triple of DDD/DDR/DRR/RRR: 4 x 1000 jobs), the
+    four full histograms, and the 16 jackknife subsamples (one 4x4 angular
+    cell left out) x 4 histograms."""
     import tpcf
     import synth
+    import voxels
     d = synth.lightcone(100000, clustered=True, seed=11)
     r = synth.lightcone(100000, seed=12)
+    d, r = d[np.argsort(d[:, 2], kind="stable")], r[np.argsort(r[:, 2], kind="stable")]
     rd, rr = _jackknife_region(d), _jackknife_region(r)
     nan = tpcf.NAN_ZERO if platform.machine() == "aarch64" else tpcf.NAN_INT_MIN
     eng = tpcf.Engine(0)
-    cats = [(eng.catalog(d), eng.catalog(r))]
+    kinds = (("DDD", tpcf.LOOP_SAME), ("DDR", tpcf.LOOP_ONE), ("DRR", tpcf.LOOP_ONE), ("RRR", tpcf.LOOP_SAME))
+    spec = {lp: tpcf.make_spec(tpcf.TRIANGLE, lp, SPEC_AXES, nan_policy=nan) for _, lp in kinds}
+
+    def four(hd, hr, ranges=None):
+        cats = {"DDD": [hd, hd, hd], "DDR": [hd, hd, hr], "DRR": [hd, hr, hr], "RRR": [hr, hr, hr]}
+        return [(spec[lp], eng.job(cats[k], ranges)) for k, lp in kinds]
+
+    hd, hr = eng.catalog(d), eng.catalog(r)
+    batch = four(hd, hr)
     for reg in range(16):
-        cats.append((eng.catalog(d[rd != reg]), eng.catalog(r[rr != reg])))
-    specs, jobs = [], []
-    for hd, hr in cats:
-        for hs, loop in (([hd, hd, hd], tpcf.LOOP_SAME), ([hd, hd, hr], tpcf.LOOP_ONE),
-                         ([hd, hr, hr], tpcf.LOOP_ONE), ([hr, hr, hr], tpcf.LOOP_SAME)):
-            specs.append(tpcf.make_spec(tpcf.TRIANGLE, loop, SPEC_AXES, nan_policy=nan))
-            jobs.append(eng.job(hs))
+        batch += four(eng.catalog(d[rd != reg]), eng.catalog(r[rr != reg]))
+    nfull = len(batch)
+    cats_of = {"DDD": (hd, hd, hd), "DDR": (hd, hd, hr), "DRR": (hd, hr, hr), "RRR": (hr, hr, hr)}
+    for k, lp in kinds:
+        for _, rng in voxels.chunk_ranges(10, [len(d) if h == hd else len(r) for h in cats_of[k]]):
+            batch.append((spec[lp], eng.job(list(cats_of[k]), rng)))
+    specs, jobs = [b[0] for b in batch], [b[1] for b in batch]
     for _ in range(args.warmup):
         eng.count_batch(specs, jobs)
-    ms, st = [], None
+    ms, wall, st = [], [], None
     for _ in range(args.steps):
-        eng.count_batch(specs, jobs)
+        t0 = time.perf_counter()
+        hs = eng.count_batch(specs, jobs)
+        wall.append((time.perf_counter() - t0) * 1e3)
         st = eng.stats()
         ms.append(st["kernel_ms"])
+    vox_sum = [sum(hs[nfull + 1000 * a: nfull + 1000 * (a + 1)]) for a in range(4)]
     mean = statistics.mean(ms) / 1e3
     _line("triangles/s (bit-exact histos)", st["loop_units"] / mean, "triangles/s", args,
-          {"workload": "light cone 100k clustered + 100k uniform, TP s8 q8 t16, full + 16 jackknife subsamples "
-                       "x DDD/DDR/DRR/RRR = 68 jobs, one launch", "jobs": len(jobs),
+          {"workload": "light cone 100k clustered + 100k uniform (depth-ordered), TP s8 q8 t16; one launch of "
+                       "4 full + 16x4 jackknife + 4x1000 voxel-chunk (division 10) jobs", "jobs": len(jobs),
            "triangles_per_step": st["loop_units"], "evaluated_triangles_per_step": st["evaluated_units"],
-           "binned_triangles_per_step": st["binned_units"], "tasks": st["tasks"]},
-          ms_per_step=mean * 1e3, wall_ms_per_step=st["total_ms"], p50_ms=statistics.median(ms),
-          p99_ms=float(np.percentile(ms, 99)),
+           "binned_triangles_per_step": st["binned_units"], "tasks": st["tasks"],
+           "voxel_sums_counted": [int(v.sum()) for v in vox_sum],
+           "full_counted": [int(h.sum()) for h in hs[:4]]},
+          ms_per_step=mean * 1e3, wall_ms_per_step=statistics.mean(wall), p50_ms=statistics.median(ms),
+          p99_ms=float(np.percentile(ms, 99)), gpu_launches=st["kernel_launches"],
           roofline={"bound": "issue", "achieved": W_TP * st["binned_units"] / (st["main_kernel_ms"] / 1e3) / 1e12,
                     "unit": "Tinst/s", "per_unit": "58 lane-instructions per binned triangle"})
     eng.close()

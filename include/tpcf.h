@@ -63,12 +63,18 @@ enum {
     TPCF_LOOP_ONE = 2   /* j from 0, k >= j (which_three_input_files == 1) */
 };
 
-/* Arithmetic of the per-triangle kernel; both give identical histograms. */
+/* Arithmetic of the per-triangle kernel.  The first two give identical
+ * histograms (the reference's); the third is a different, more accurate count. */
 enum {
     TPCF_GUARDED_FP32 = 0, /* FP32 fast path; values within a bounded guard band of
                               a bin edge are recomputed exactly */
-    TPCF_PLAIN_FP64 = 1    /* every reference float operation done in FP64 and
+    TPCF_PLAIN_FP64 = 1,   /* every reference float operation done in FP64 and
                               rounded to float (exact for + - * / sqrt) */
+    TPCF_GEOMETRY_FP64 = 2 /* triangle only: the same formulas evaluated in double
+                              from the float coordinates (acos in double); NOT the
+                              reference's counts -- the FP64 truth that the error of
+                              the derived correlation function is measured against
+                              (no counterpart in the reference) */
 };
 
 /* int(NaN) in distance_to_bin (src/3pcf_C_version_triangle_parametrization.cc:99)
@@ -124,6 +130,8 @@ typedef struct {
     uint64_t h2d_bytes;          /* host-to-device bytes copied since the previous tpcf_last_stats */
     uint64_t d2h_bytes;          /* device-to-host bytes copied since the previous tpcf_last_stats */
     uint64_t binned_units;       /* triangles (pairs) that reached the full binning arithmetic */
+    uint64_t graph_replays;      /* launches replayed from a captured CUDA graph (a repeated
+                                    batch); the rest were issued one by one */
 } tpcf_stats;
 
 typedef struct tpcf_ctx tpcf_ctx;

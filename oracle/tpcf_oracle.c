@@ -349,6 +349,105 @@ unsigned long long oracle_triangle(const ocat_t* cats, int which, const float* l
     return ncalc;
 }
 
+/* ------------------------------------------------------------------------- */
+/* FP64 geometry: the triangle formulas of :116-240 evaluated in double from
+ * the float coordinates, acos in double.  Not the reference's counts; the FP64
+ * truth that the error of the derived correlation function is measured
+ * against.  Same loop nest and counting rules as oracle_triangle. */
+
+static inline double geo_dist(float x0, float y0, float z0, float x1, float y1, float z1) {
+    double dx = (double)x0 - (double)x1, dy = (double)y0 - (double)y1, dz = (double)z0 - (double)z1;
+    return sqrt(dx * dx + dy * dy + dz * dz);
+}
+
+static inline int geo_bin(double v, float lo, float hi, int nbins, int nan_zero) {
+    double bw = ((double)hi - (double)lo) / nbins;
+    if (v < lo) return -999;
+    if (v >= hi) return -999;
+    if (v != v) return nan_zero ? 0 : INT_MIN;
+    return (int)((v - lo) / bw);
+}
+
+static inline void geo_core(double d0, double d1, double d2, const tp_spec_t* sp, int totbins[3]) {
+    double a = d0, b = d1, c = d2, t;
+    /* ascending order; ties do not matter here (equal values) */
+    if (a > b) { t = a; a = b; b = t; }
+    if (b > c) { t = b; b = c; c = t; }
+    if (a > b) { t = a; a = b; b = t; }
+    const double th0 = acos((a * a + b * b - c * c) / (2 * a * b)) / 3.14159;
+    const double th1 = acos((b * b + c * c - a * a) / (2 * b * c)) / 3.14159;
+    const double sv[3] = {a, b, a}, qv[3] = {b / a, c / b, c / a}, tv[3] = {th0, th1, 1.0 - th0 - th1};
+    for (int k = 0; k < 3; k++) {
+        int i0 = geo_bin(sv[k], sp->lo[0], sp->hi[0], sp->nb[0], sp->nan_zero);
+        int i1 = geo_bin(qv[k], sp->lo[1], sp->hi[1], sp->nb[1], sp->nan_zero);
+        int i2 = geo_bin(tv[k], sp->lo[2], sp->hi[2], sp->nb[2], sp->nan_zero);
+        int tot = (i0 < 0 || i1 < 0 || i2 < 0) ? -999 : sp->nb[1] * sp->nb[2] * i0 + sp->nb[2] * i1 + i2;
+        if (d0 == 0 || d1 == 0 || d2 == 0) tot = -999;
+        totbins[k] = tot;
+    }
+}
+
+static void* geo_worker(void* arg) {
+    tp_worker_t* w = (tp_worker_t*)arg;
+    tp_task_t* t = w->shared;
+    const ocat_t* c = t->c;
+    const long size = (long)t->sp.nb[0] * t->sp.nb[1] * t->sp.nb[2];
+    for (;;) {
+        long i = grab(&t->i_next, t->mu, 1);
+        if (i >= c[0].n) break;
+        long jmin = (t->which == 0) ? i : 0;
+        for (long j = jmin; j < c[1].n; j++) {
+            double d01 = geo_dist(c[0].x[i], c[0].y[i], c[0].z[i], c[1].x[j], c[1].y[j], c[1].z[j]);
+            for (long k = j; k < c[2].n; k++) {
+                int tb[3];
+                double d02 = geo_dist(c[0].x[i], c[0].y[i], c[0].z[i], c[2].x[k], c[2].y[k], c[2].z[k]);
+                double d12 = geo_dist(c[1].x[j], c[1].y[j], c[1].z[j], c[2].x[k], c[2].y[k], c[2].z[k]);
+                geo_core(d01, d02, d12, &t->sp, tb);
+                w->ncalc++;
+                for (int b = 0; b < 3; b++)
+                    if (tb[b] >= 0 && tb[b] < size) w->hist[tb[b]]++;
+            }
+        }
+    }
+    return NULL;
+}
+
+unsigned long long oracle_triangle_geom64(const ocat_t* cats, int which, const float* lohi, const int* nb,
+                                          int nan_zero, unsigned long long* hist, int nthreads) {
+    const long size = (long)nb[0] * nb[1] * nb[2];
+    memset(hist, 0, sizeof(unsigned long long) * size);
+    if (nthreads < 1) nthreads = 1;
+    pthread_mutex_t mu = PTHREAD_MUTEX_INITIALIZER;
+    tp_task_t task;
+    task.c = cats;
+    for (int a = 0; a < 3; a++) {
+        task.sp.lo[a] = lohi[2 * a];
+        task.sp.hi[a] = lohi[2 * a + 1];
+        task.sp.nb[a] = nb[a];
+    }
+    task.sp.nan_zero = nan_zero;
+    task.which = which ? 1 : 0;
+    task.i_next = 0;
+    task.mu = &mu;
+    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * nthreads);
+    tp_worker_t* ws = (tp_worker_t*)calloc(nthreads, sizeof(tp_worker_t));
+    for (int t = 0; t < nthreads; t++) {
+        ws[t].shared = &task;
+        ws[t].hist = (unsigned long long*)calloc(size, sizeof(unsigned long long));
+        pthread_create(&th[t], NULL, geo_worker, &ws[t]);
+    }
+    unsigned long long ncalc = 0;
+    for (int t = 0; t < nthreads; t++) {
+        pthread_join(th[t], NULL);
+        for (long b = 0; b < size; b++) hist[b] += ws[t].hist[b];
+        ncalc += ws[t].ncalc;
+        free(ws[t].hist);
+    }
+    free(ws);
+    free(th);
+    return ncalc;
+}
+
 /* Exact triangle-parametrization indices of one triangle (for tests of edge
  * cases).  Returns the three histogram indices or -999. */
 void oracle_triangle_one(const float* p0, const float* p1, const float* p2, const float* lohi,

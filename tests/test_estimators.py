@@ -62,3 +62,14 @@ def test_reduced_zeta_shape_and_finite_denominator():
     q = estimators.reduced_zeta(z, spec, 3, [0, 1, 2], tab)
     assert q.shape == (3, 16)
     assert np.all(np.isfinite(q))
+
+
+def test_zeta_error_summary():
+    z_ref = np.array([0.5, -0.25, 2.0, 0.0])
+    z = z_ref + np.array([1e-3, 0.0, -2e-3, 5.0])
+    rrr = np.array([3, 1, 7, 0])  # the last bin is unpopulated and ignored
+    e = estimators.zeta_error(z, z_ref, rrr)
+    assert e["bins"] == 3
+    assert abs(e["max_abs"] - 2e-3) < 1e-15
+    assert abs(e["rms"] - np.sqrt((1e-6 + 4e-6) / 3)) < 1e-15
+    assert abs(e["max_rel"] - 2e-3) < 1e-12

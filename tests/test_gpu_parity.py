@@ -200,6 +200,36 @@ def test_triangle_vs_oracle_native_nan(eng, seed, spec):
         eng.release(h)
 
 
+@pytest.mark.parametrize("seed", [303])
+def test_geometry_fp64_vs_oracle(eng, seed):
+    """TPCF_GEOMETRY_FP64 (the FP64 truth, not the reference's counts) against
+    the oracle's double-precision loop: identical operations except acos
+    (CUDA's double acos vs the host's), so at most a couple of triangles may
+    sit on the other side of an edge."""
+    d, r = _random_case(seed)
+    hd, hr = eng.catalog(d), eng.catalog(r)
+    spec = ((8, 2.0, 10.0), (8, 1.0, 3.0), (16, 0.0, 1.0))
+    combos = [([hd, hd, hd], [d, d, d], 0), ([hd, hd, hr], [d, d, r], 1), ([hd, hr, hr], [d, r, r], 1),
+              ([hr, hr, hr], [r, r, r], 0)]
+    specs = [_tp_spec(spec, _loop_of(w), precision=tpcf.GEOMETRY_FP64, nan=NATIVE_NAN) for _, _, w in combos]
+    hists = eng.count_batch(specs, [eng.job(h) for h, _, _ in combos])
+    for (h, cats, w), got in zip(combos, hists):
+        want, _ = oracle.triangle_geom64(cats, w, spec, nan_zero=NATIVE_NAN == tpcf.NAN_ZERO)
+        diff = np.abs(got.astype(np.int64) - want.astype(np.int64)).sum()
+        assert diff <= 6, (w, int(diff))
+        assert got.sum() > 0
+    # the float-arithmetic counts differ from the FP64 truth only near edges
+    exact = eng.count_batch([_tp_spec(spec, _loop_of(w), nan=NATIVE_NAN) for _, _, w in combos],
+                            [eng.job(h) for h, _, _ in combos])
+    for a, b in zip(exact, hists):
+        assert np.abs(a.astype(np.int64) - b.astype(np.int64)).sum() <= 1e-3 * a.sum()
+    with pytest.raises(tpcf.EngineError):
+        eng.count(tpcf.make_spec(tpcf.PAIR, tpcf.LOOP_SAME, [(10, 0.0, 10.0)], precision=tpcf.GEOMETRY_FP64),
+                  eng.job([hd, hd]))
+    eng.release(hd)
+    eng.release(hr)
+
+
 def test_lattice_nan_policies(eng):
     """Degenerate lattice triangles produce rounded cosines beyond +-1; both
     int(NaN) conventions must match the oracle."""

@@ -1,0 +1,46 @@
+"""Repeated batches replay a captured CUDA graph of the whole step (zero,
+count, recheck, copy back); the counts are the same as with graphs off, and a
+changed batch is captured anew."""
+import numpy as np
+import pytest
+
+import synth
+import tpcf
+
+pytestmark = pytest.mark.gpu
+
+TP = [(8, 2.0, 10.0), (8, 1.0, 3.0), (16, 0.0, 1.0)]
+
+
+def _batch(eng, hd, hr):
+    loops = [tpcf.LOOP_SAME, tpcf.LOOP_ONE, tpcf.LOOP_ONE, tpcf.LOOP_SAME]
+    specs = [tpcf.make_spec(tpcf.TRIANGLE, lp, TP) for lp in loops]
+    jobs = [eng.job([hd, hd, hd]), eng.job([hd, hd, hr]), eng.job([hd, hr, hr]), eng.job([hr, hr, hr])]
+    return specs, jobs
+
+
+def test_graph_replay_matches_direct_launches(monkeypatch):
+    d = synth.blobs(1500, n_blobs=4, sigma=5.0, box=60.0, seed=31)
+    r = synth.uniform(1400, box=60.0, seed=32)
+    with tpcf.Engine(0) as eng:
+        hd, hr = eng.catalog(d), eng.catalog(r)
+        specs, jobs = _batch(eng, hd, hr)
+        first = eng.count_batch(specs, jobs)
+        assert eng.stats()["graph_replays"] == 1
+        again = eng.count_batch(specs, jobs)
+        assert eng.stats()["graph_replays"] == 1
+        for a, b in zip(first, again):
+            assert np.array_equal(a, b)
+        # another batch on the same lane: captured anew, still exact
+        pair = eng.count(tpcf.make_spec(tpcf.PAIR, tpcf.LOOP_SAME, [(700, 0.0, 70.0)]), eng.job([hd, hd]))
+        back = eng.count_batch(specs, jobs)
+        for a, b in zip(first, back):
+            assert np.array_equal(a, b)
+        monkeypatch.setenv("TPCF_GRAPHS", "0")
+        direct = eng.count_batch(specs, jobs)
+        assert eng.stats()["graph_replays"] == 0
+        for a, b in zip(first, direct):
+            assert np.array_equal(a, b)
+        assert np.array_equal(pair, eng.count(tpcf.make_spec(tpcf.PAIR, tpcf.LOOP_SAME, [(700, 0.0, 70.0)]),
+                                              eng.job([hd, hd])))
+        assert sum(int(a.sum()) for a in first) > 0

@@ -9,6 +9,7 @@ import pytest
 
 import oracle
 import refformat as rf
+import synth
 
 SANDBOX = os.path.join(rf.GOLDEN, "sandbox")
 SANDBOX_SPEC = ((50, 2.0, 12.0), (16, 0.9, 4.1), (25, 0.0, 1.0))
@@ -98,3 +99,45 @@ def test_oracle_acosf_is_host_libm():
     libm.acosf.argtypes = [ctypes.c_float]
     for c in np.linspace(-1, 1, 1001, dtype=np.float32):
         assert oracle.acosf(c) == libm.acosf(float(c))
+
+
+def test_geometry_fp64_oracle_matches_python_restatement():
+    """The FP64-geometry loop (oracle_triangle_geom64) against a plain-Python
+    double restatement of the same formulas on a small case."""
+    import math
+    d = synth.blobs(36, n_blobs=2, sigma=3.0, box=12.0, seed=21)
+    spec = ((8, 2.0, 10.0), (8, 1.0, 3.0), (16, 0.0, 1.0))
+    got, n = oracle.triangle_geom64([d, d, d], 0, spec, nthreads=2)
+    want = np.zeros(8 * 8 * 16, dtype=np.uint64)
+    lo = [float(np.float32(a[1])) for a in spec]
+    hi = [float(np.float32(a[2])) for a in spec]
+    nb = [a[0] for a in spec]
+    pts = [tuple(float(v) for v in p) for p in d]
+
+    def bin_(v, a):
+        if v < lo[a] or v >= hi[a]:
+            return -1
+        return int((v - lo[a]) / ((hi[a] - lo[a]) / nb[a]))
+
+    def dist(p, q):
+        dx, dy, dz = p[0] - q[0], p[1] - q[1], p[2] - q[2]
+        return math.sqrt(dx * dx + dy * dy + dz * dz)
+
+    count = 0
+    for i in range(len(pts)):
+        for j in range(i, len(pts)):
+            for k in range(j, len(pts)):
+                count += 1
+                s = sorted((dist(pts[i], pts[j]), dist(pts[i], pts[k]), dist(pts[j], pts[k])))
+                if s[0] == 0:
+                    continue
+                a, b, c = s
+                t0 = math.acos((a * a + b * b - c * c) / (2 * a * b)) / 3.14159
+                t1 = math.acos((b * b + c * c - a * a) / (2 * b * c)) / 3.14159
+                for sv, qv, tv in ((a, b / a, t0), (b, c / b, t1), (a, c / a, 1.0 - t0 - t1)):
+                    i0, i1, i2 = bin_(sv, 0), bin_(qv, 1), bin_(tv, 2)
+                    if min(i0, i1, i2) >= 0:
+                        want[128 * i0 + 16 * i1 + i2] += 1
+    assert n == count
+    assert np.array_equal(got, want)
+    assert want.sum() > 0
