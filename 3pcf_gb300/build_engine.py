@@ -18,7 +18,7 @@ LIB = os.path.join(BUILD, "libtpcf.so")
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-PROGRAMS = {"tpcf_3side": 0, "tpcf_tp": 1, "tpcf_2pcf": 2}
+PROGRAMS = {"tpcf_3side": 0, "tpcf_tp": 1, "tpcf_2pcf": 2, "tpcf_jbj": 3}
 
 HEADERS = ["engine.h", "exact_acos.h"]
 
@@ -80,6 +80,10 @@ def build(verbose=False):
         if _newer(exe, [cli, LIB] + hdr):
             cmds.append(["g++", "-O2", "-std=c++17", "-Wall", "-DTPCF_PROGRAM=%d" % num, cli, "-o", exe,
                          "-L" + BUILD, "-ltpcf", "-Wl,-rpath,$ORIGIN/../_build"])
+    sv = os.path.join(CSRC, "sum_voxels.cpp")
+    exe = os.path.join(BIN, "tpcf_sum_voxels")
+    if _newer(exe, [sv]):
+        cmds.append(["g++", "-O2", "-std=c++17", "-Wall", sv, "-o", exe])
     _run_all(cmds)
     return LIB
 

@@ -1,9 +1,10 @@
 // cli.cpp -- command-line shims with the reference programs' interface.
 //
-// Built three times (TPCF_PROGRAM = 0, 1, 2) as
+// Built four times (TPCF_PROGRAM = 0, 1, 2, 3) as
 //   tpcf_3side  <- src/3pcf_C_version.cc main()                       (:147-466)
 //   tpcf_tp     <- src/3pcf_C_version_triangle_parametrization.cc main() (:245-571)
 //   tpcf_2pcf   <- src/2pcf_C_version.cc main()                       (:118-410)
+//   tpcf_jbj    <- src/3pcf_C_version_triangle_parametrization_JBJ.cc main() (:240-560)
 // Same short options (GNU getopt, so options may follow the catalogs as the
 // reference's csh drivers pass them), same positional catalogs, same loop mode
 // from argv string identity, same -X/-x index chunks, same default output name
@@ -72,7 +73,7 @@ struct Loaded {
 }  // namespace
 
 int main(int argc, char** argv) {
-    const int program = TPCF_PROGRAM;  // 0 three-side, 1 triangle, 2 pairs
+    const int program = TPCF_PROGRAM;  // 0 three-side, 1 triangle, 2 pairs, 3 JBJ
     char* outfilename = nullptr;
     char defaultout[256];
     snprintf(defaultout, sizeof(defaultout), program == 2 ? "default_out_2pcf.dat" : "default_out.dat");
@@ -223,9 +224,10 @@ int main(int argc, char** argv) {
         spec.loop = TPCF_LOOP_ALL;
         spec.overflow = clean ? TPCF_OVERFLOW_CLEAN : TPCF_OVERFLOW_COMPAT;
         spec.axis[0] = tpcf_axis{(float)three.lo, (float)three.hi, three.n};
-    } else if (program == 1) {
-        spec.kind = TPCF_TRIANGLE;
+    } else if (program == 1 || program == 3) {
+        spec.kind = program == 1 ? TPCF_TRIANGLE : TPCF_TRIANGLE_JBJ;
         spec.loop = which ? TPCF_LOOP_ONE : TPCF_LOOP_SAME;
+        spec.overflow = clean ? TPCF_OVERFLOW_CLEAN : TPCF_OVERFLOW_COMPAT;  // JBJ: bin-0 extra counts
         spec.axis[0] = tpcf_axis{(float)S.lo, (float)S.hi, S.n};
         spec.axis[1] = tpcf_axis{(float)Q.lo, (float)Q.hi, Q.n};
         spec.axis[2] = tpcf_axis{(float)T.lo, (float)T.hi, T.n};
@@ -262,8 +264,8 @@ int main(int argc, char** argv) {
                 fprintf(out, "\n");
             }
         }
-    } else if (program == 1) {
-        // :537-569; counts are the reference's unsigned int (wrap mod 2^32)
+    } else if (program == 1 || program == 3) {
+        // :537-569 (JBJ: :527-553); counts are the reference's unsigned int (wrap mod 2^32)
         fprintf(out, "%lld\n%lld\n%lld\n", (long long)ngal[0], (long long)ngal[1], (long long)ngal[2]);
         fprintf(out, "%d %d %d\n", S.n, Q.n, T.n);
         fprintf(out, "%-6.3f %-6.3f %-6.3f\n", S.lo, S.hi, (S.hi - S.lo) / S.n);

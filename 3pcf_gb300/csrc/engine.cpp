@@ -412,6 +412,30 @@ Binning make_binning(const tpcf_spec& sp) {
         b.s_lo = p.s_lo;
         b.s_hi = p.s_hi;
         b.q_hi = (double)p.q_hi * (1 + 1e-5);
+    } else if (sp.kind == TPCF_TRIANGLE_JBJ) {
+        for (int a = 0; a < 3; a++) check_axis(sp.axis[a], "JBJ axis");
+        TriParams& p = b.tri;
+        p.S = sp.axis[0].nbins;
+        p.Q = sp.axis[1].nbins;
+        p.T = sp.axis[2].nbins;
+        if ((int64_t)p.S * p.Q * p.T > MAX_TRI_BINS) throw InvalidArg{"JBJ binning too large"};
+        p.len = p.S * p.Q * p.T;
+        p.s_lo = sp.axis[0].lo;
+        p.s_hi = sp.axis[0].hi;
+        p.s_bw = ref_bw(p.s_lo, p.s_hi, p.S);
+        p.q_lo = sp.axis[1].lo;
+        p.q_hi = sp.axis[1].hi;
+        p.q_bw = ref_bw(p.q_lo, p.q_hi, p.Q);
+        p.t_lo = sp.axis[2].lo;
+        p.t_hi = sp.axis[2].hi;
+        p.t_bw = ref_bw(p.t_lo, p.t_hi, p.T);
+        p.nan_zero = 0;  // no NaN reaches a counted JBJ bin (zero sides are dropped)
+        b.len = p.len;
+        // counted: s < s_hi, s/m >= q_lo, (l - m)/s < t_hi, so
+        // l < s_hi/q_lo + max(t_hi, 0) s_hi (margins cover the float roundings)
+        if (p.q_lo > 0 && p.s_hi > 0)
+            b.lmax = ((double)p.s_hi / (double)p.q_lo + std::max(0.0, (double)p.t_hi) * (double)p.s_hi) * (1 + 1e-5) +
+                     1e-6;
     } else if (sp.kind == TPCF_PAIR) {
         check_axis(sp.axis[0], "pair axis");
         PairParams& p = b.pair;
@@ -429,6 +453,7 @@ Binning make_binning(const tpcf_spec& sp) {
         b.tri_prune = false;
     }
     // device copy of the bound, rounded up so that a float side >= it is >= lmax
+    if (sp.kind == TPCF_TRIANGLE_JBJ) b.tri.lmax = b.lmax < 3e38 ? nextafterf((float)b.lmax, INFINITY) : INFINITY;
     if (sp.kind == TPCF_TRIANGLE) {
         b.tri.lmax = b.lmax < 3e38 ? nextafterf((float)b.lmax, INFINITY) : INFINITY;
         double mid = (double)b.tri.s_hi * (double)b.tri.q_hi * (1 + 1e-5) + 1e-6;
@@ -440,8 +465,8 @@ Binning make_binning(const tpcf_spec& sp) {
 bool same_binning(const tpcf_spec& a, const tpcf_spec& b) {
     if (a.kind != b.kind || a.precision != b.precision) return false;
     if (a.kind == TPCF_TRIANGLE && a.nan_policy != b.nan_policy) return false;
-    if (a.kind == TPCF_THREE_SIDE && a.overflow != b.overflow) return false;
-    int na = a.kind == TPCF_TRIANGLE ? 3 : 1;
+    if ((a.kind == TPCF_THREE_SIDE || a.kind == TPCF_TRIANGLE_JBJ) && a.overflow != b.overflow) return false;
+    int na = (a.kind == TPCF_TRIANGLE || a.kind == TPCF_TRIANGLE_JBJ) ? 3 : 1;
     for (int i = 0; i < na; i++)
         if (a.axis[i].lo != b.axis[i].lo || a.axis[i].hi != b.axis[i].hi || a.axis[i].nbins != b.axis[i].nbins)
             return false;
@@ -535,9 +560,19 @@ struct GroupJob {
     const tpcf_spec* spec;
     const tpcf_job* job;
     uint64_t* out;
+    bool accumulate = false;  // add into out (jobs sharing out share one device histogram)
 };
 
 }  // namespace
+
+// Launch shape of a persistent kernel: warp-private histogram copies in
+// shared memory (0: count straight into the 64-bit global histogram) and
+// resident CTAs per SM (the grid is that many per SM).
+struct Shape {
+    int copies = 1;
+    int per_sm = 1;
+    size_t smem = 0;
+};
 
 struct tpcf_ctx {
     int device = 0;
@@ -549,7 +584,8 @@ struct tpcf_ctx {
     uint64_t next_handle = 1;
     std::map<uint64_t, std::shared_ptr<Catalog>> catalogs;
     std::map<uint64_t, std::shared_ptr<DevBuf<float4>>> cat_dev;  // unsorted points (resident)
-    std::map<std::tuple<uint64_t, int64_t, int64_t, int>, std::shared_ptr<View>> views;
+    // (catalog, begin, end, tile points, global loop indices) -> view
+    std::map<std::tuple<uint64_t, int64_t, int64_t, int, bool>, std::shared_ptr<View>> views;
     int tile_points = TILE;  // points per spatial tile (<= TILE)
     uint64_t next_view_id = 0;
     // acos table
@@ -567,6 +603,9 @@ struct tpcf_ctx {
     bool stop = false;
     int64_t admit_bytes = (int64_t)8 << 30;
     int64_t inflight_bytes = 0;  // device bytes of batches running on serving lanes
+    // autotuner: launch shape per batch signature
+    std::mutex tune_mu;
+    std::map<uint64_t, Shape> tuned;
 };
 
 namespace {
@@ -577,7 +616,8 @@ tpcf_status fail(tpcf_ctx* ctx, tpcf_status s, const std::string& msg) {
     return s;
 }
 
-std::shared_ptr<View> get_view(tpcf_ctx* ctx, Lane& L, uint64_t handle, int64_t begin, int64_t end) {
+std::shared_ptr<View> get_view(tpcf_ctx* ctx, Lane& L, uint64_t handle, int64_t begin, int64_t end,
+                               bool global = false) {
     std::lock_guard<std::recursive_mutex> vlk(ctx->view_mu);
     auto it = ctx->catalogs.find(handle);
     if (it == ctx->catalogs.end()) throw InvalidArg{"unknown catalog handle"};
@@ -585,7 +625,8 @@ std::shared_ptr<View> get_view(tpcf_ctx* ctx, Lane& L, uint64_t handle, int64_t 
     if (end < 0) end = c.n;
     if (begin < 0 || begin > end || end > c.n) throw InvalidArg{"catalog range out of bounds"};
     const int tile = ctx->tile_points;
-    auto key = std::make_tuple(handle, begin, end, tile);
+    if (begin == 0) global = false;  // the same loop indices
+    auto key = std::make_tuple(handle, begin, end, tile, global);
     auto vi = ctx->views.find(key);
     if (vi != ctx->views.end()) return vi->second;
     auto v = std::make_shared<View>();
@@ -609,7 +650,8 @@ std::shared_ptr<View> get_view(tpcf_ctx* ctx, Lane& L, uint64_t handle, int64_t 
         p.x = xyz[3 * (size_t)o];
         p.y = xyz[3 * (size_t)o + 1];
         p.z = xyz[3 * (size_t)o + 2];
-        int32_t key_i = o;  // loop index inside the range
+        // loop index inside the range, or inside the whole catalog
+        int32_t key_i = global ? (int32_t)(o + begin) : o;
         memcpy(&p.w, &key_i, 4);
         pts[i] = p;
     }
@@ -773,7 +815,8 @@ void plan_triplets(const tpcf_spec& sp, const PlannedJob& pj, uint32_t slot, con
     };
     auto nAB = nbrs(A, B, bAB);
     auto nAC = nbrs(A, C, bAC);
-    if (sp.kind == TPCF_TRIANGLE && sp.loop == TPCF_LOOP_SAME && sameAB && sameBC) {
+    const bool tri = sp.kind == TPCF_TRIANGLE || sp.kind == TPCF_TRIANGLE_JBJ;
+    if (tri && sp.loop == TPCF_LOOP_SAME && sameAB && sameBC) {
         // i <= j <= k over one array: unordered distinct triples
         for (int a = 0; a < A.ntiles; a++)
             for (int b : nAB[a]) {
@@ -784,7 +827,7 @@ void plan_triplets(const tpcf_spec& sp, const PlannedJob& pj, uint32_t slot, con
                     add(a, b, c, PRED_NONE, f);
                 }
             }
-    } else if (sp.kind == TPCF_TRIANGLE && sp.loop == TPCF_LOOP_ONE && sameBC) {
+    } else if (tri && sp.loop == TPCF_LOOP_ONE && sameBC) {
         // j <= k over one array (j == k has a zero side): unordered pairs
         for (int a = 0; a < A.ntiles; a++)
             for (int b : nAB[a])
@@ -792,7 +835,7 @@ void plan_triplets(const tpcf_spec& sp, const PlannedJob& pj, uint32_t slot, con
                     if (c < b) continue;
                     add(a, b, c, PRED_NONE, b == c ? TASK_DIAG_JK : 0);
                 }
-    } else if (sp.kind == TPCF_TRIANGLE && sp.loop == TPCF_LOOP_ONE && sameAB) {
+    } else if (tri && sp.loop == TPCF_LOOP_ONE && sameAB) {
         // every ordered (i, j) of one array, k >= j: unordered {i, j} with
         // weight [k >= i] + [k >= j]
         for (int a = 0; a < A.ntiles; a++)
@@ -802,7 +845,7 @@ void plan_triplets(const tpcf_spec& sp, const PlannedJob& pj, uint32_t slot, con
             }
     } else {
         uint32_t pred = PRED_NONE;
-        if (sp.kind == TPCF_TRIANGLE) pred = sp.loop == TPCF_LOOP_SAME ? PRED_SAME : sp.loop == TPCF_LOOP_ONE ? PRED_ONE : PRED_NONE;
+        if (tri) pred = sp.loop == TPCF_LOOP_SAME ? PRED_SAME : sp.loop == TPCF_LOOP_ONE ? PRED_ONE : PRED_NONE;
         for (int a = 0; a < A.ntiles; a++)
             for (int b : nAB[a])
                 for (int c : nAC[a]) add(a, b, c, pred, 0);
@@ -831,17 +874,81 @@ void plan_pairs(const tpcf_spec& sp, const PlannedJob& pj, uint32_t slot, double
         }
 }
 
-int occupancy_grid(tpcf_ctx* ctx, int kind, size_t smem, int fp64, uint64_t ntasks) {
-    (void)kind;
-    (void)fp64;
-    int per_sm = 1;
-    int max_smem = 0;
-    cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx->device);
-    const char* bps = getenv("TPCF_TRI_BLOCKS_PER_SM");
-    const int tri_per_sm = bps ? atoi(bps) : 3;
-    if (smem > 0) per_sm = std::max(1, std::min(kind == TPCF_TRIANGLE ? tri_per_sm : 4, (int)(max_smem / (smem + 1024))));
-    else per_sm = 4;
-    uint64_t g = (uint64_t)ctx->num_sms * per_sm;
+size_t shape_smem(const tpcf_spec& sp, const Binning& bin, int copies) {
+    if (sp.kind == TPCF_TRIANGLE || sp.kind == TPCF_TRIANGLE_JBJ) return triangle_smem_bytes(bin.len, copies);
+    if (sp.kind == TPCF_THREE_SIDE) return three_side_smem_bytes(copies ? bin.len : 0, copies);
+    return pair_smem_bytes(bin.len, copies);
+}
+
+// Launch shapes worth trying for a group, the default first.  The guarded
+// triangle kernel is compiled for three CTAs per SM (its register budget);
+// the others take as many CTAs as shared memory allows, up to 8.
+std::vector<Shape> shape_candidates(tpcf_ctx* ctx, const tpcf_spec& sp, const Binning& bin, bool fp64) {
+    int max_smem_sm = 0, max_smem_block = 0;
+    cudaDeviceGetAttribute(&max_smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx->device);
+    cudaDeviceGetAttribute(&max_smem_block, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
+    auto fit = [&](int copies, int cap_per_sm) {
+        Shape sh;
+        sh.copies = copies;
+        sh.smem = shape_smem(sp, bin, copies);
+        sh.per_sm = 0;
+        if (sh.smem > (size_t)max_smem_block) return sh;
+        sh.per_sm = std::min(cap_per_sm, (int)(max_smem_sm / (sh.smem + 1024)));
+        return sh;
+    };
+    std::vector<Shape> out;
+    auto add = [&](Shape sh) {
+        if (sh.per_sm < 1) return;
+        for (const Shape& o : out)
+            if (o.copies == sh.copies && o.per_sm == sh.per_sm) return;
+        out.push_back(sh);
+    };
+    if (sp.kind == TPCF_TRIANGLE || sp.kind == TPCF_TRIANGLE_JBJ) {
+        const char* bps = getenv("TPCF_TRI_BLOCKS_PER_SM");
+        const int tri_per_sm = fp64 ? 2 : (bps ? std::max(1, atoi(bps)) : 3);
+        // default: as many copies as keep three CTAs on an SM (the kernel is
+        // latency-bound and needs the warps)
+        int c = 8;
+        while (c > 1 && fit(c, tri_per_sm).per_sm < tri_per_sm) c /= 2;
+        add(fit(c, tri_per_sm));
+        if (!fp64)
+            for (int cc : {4, 2, 1}) add(fit(cc, tri_per_sm));
+        if (out.empty()) throw InvalidArg{"triangle histogram too large for shared memory"};
+    } else if (sp.kind == TPCF_THREE_SIDE) {
+        // default: the most copies that still leave four CTAs per SM, else the
+        // global histogram
+        Shape def;
+        def.copies = -1;
+        for (int cc : {4, 2, 1}) {
+            Shape sh = fit(cc, 8);
+            if (sh.per_sm >= 4) {
+                def = sh;
+                break;
+            }
+        }
+        if (def.copies < 0) def = fit(0, 8);
+        add(def);
+        for (int cc : {8, 4, 2, 1, 0}) add(fit(cc, 8));
+    } else {
+        Shape def;
+        def.copies = -1;
+        for (int cc : {8, 4, 2, 1}) {
+            Shape sh = fit(cc, 8);
+            if (sh.per_sm >= 2) {
+                def = sh;
+                break;
+            }
+        }
+        if (def.copies < 0) def = fit(1, 8);
+        if (def.per_sm < 1) throw InvalidArg{"pair histogram too large"};
+        add(def);
+        for (int cc : {8, 4, 2, 1}) add(fit(cc, 8));
+    }
+    return out;
+}
+
+int grid_for(tpcf_ctx* ctx, const Shape& sh, uint64_t ntasks) {
+    uint64_t g = (uint64_t)ctx->num_sms * sh.per_sm;
     if (g > ntasks) g = std::max<uint64_t>(ntasks, 1);
     return (int)g;
 }
@@ -853,11 +960,31 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
     const tpcf_spec& sp = *group[0].spec;
     Binning bin = make_binning(sp);
     const int ncat = sp.kind == TPCF_PAIR ? 2 : 3;
-    if (group.size() > 0xFFFF) throw InvalidArg{"too many jobs in one batch"};
+    if (group.size() > MAX_BATCH_JOBS) throw InvalidArg{"too many jobs in one batch"};
     std::vector<PlannedJob> pj(group.size());
     std::vector<DevJob> dj(group.size());
     uint64_t evaluated = 0, units = 0;
-    size_t hist_total = (size_t)bin.len * group.size();
+    // device histogram slots: one per job, or one per distinct output for
+    // accumulating jobs
+    std::vector<size_t> slot_of(group.size());
+    std::vector<size_t> slot_job;  // first job of each slot
+    {
+        std::map<uint64_t*, size_t> by_out;
+        for (size_t g = 0; g < group.size(); g++) {
+            if (group[g].accumulate) {
+                auto it = by_out.find(group[g].out);
+                if (it != by_out.end()) {
+                    slot_of[g] = it->second;
+                    continue;
+                }
+                by_out[group[g].out] = slot_job.size();
+            }
+            slot_of[g] = slot_job.size();
+            slot_job.push_back(g);
+        }
+    }
+    const size_t nslots = slot_job.size();
+    size_t hist_total = (size_t)bin.len * nslots;
     L.d_hist.reserve(hist_total);
     // signature of the batch: a repeated batch over the same resident views
     // reuses its task list and device upload
@@ -868,7 +995,8 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
         const tpcf_spec& jsp = *group[g].spec;  // same binning as sp; the loop nest may differ
         int64_t n[3] = {0, 0, 0};
         for (int r = 0; r < ncat; r++) {
-            pj[g].v[r] = get_view(ctx, L, job.catalog[r], job.begin[r], job.end[r]);
+            pj[g].v[r] = get_view(ctx, L, job.catalog[r], job.begin[r], job.end[r],
+                                  (job.flags & TPCF_JOB_GLOBAL_INDEX) != 0);
             n[r] = pj[g].v[r]->n;
         }
         if (ncat == 2) pj[g].v[2] = pj[g].v[1];
@@ -879,7 +1007,8 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
             dj[g].tile_start[r] = pj[g].v[r]->tile_start.p;
             sig.push_back(pj[g].v[r]->id);
         }
-        dj[g].hist = L.d_hist.p + (size_t)bin.len * g;
+        dj[g].hist = L.d_hist.p + (size_t)bin.len * slot_of[g];
+        sig.push_back(slot_of[g]);
         uint64_t f[6] = {(uint64_t)jsp.kind, (uint64_t)jsp.loop, (uint64_t)jsp.prune, (uint64_t)jsp.precision,
                          (uint64_t)jsp.nan_policy, (uint64_t)jsp.overflow};
         sig.insert(sig.end(), f, f + 6);
@@ -891,7 +1020,8 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
     cudaStream_t st = L.stream;
     L.d_counters.reserve(8);
     size_t ntasks = 0;
-    if (sig == L.plan_sig) {
+    const bool plan_hit = sig == L.plan_sig;
+    if (plan_hit) {
         ntasks = L.plan_ntasks;
         evaluated = L.plan_evaluated;
     } else {
@@ -941,27 +1071,7 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
     const bool fp64 = sp.precision != TPCF_GUARDED_FP32;
     if (sp.kind == TPCF_TRIANGLE) ensure_acos(ctx);
     const AcosTable acos_t = sp.kind == TPCF_TRIANGLE ? acos_table(ctx) : AcosTable{};
-    // launch shape: warp-private histogram copies in shared memory
-    int copies = 8;
-    size_t smem = 0;
-    if (sp.kind == TPCF_TRIANGLE) {
-        // as many copies as still let three CTAs share an SM (the kernel is
-        // latency-bound and needs the warps)
-        const char* cap_env = getenv("TPCF_TRI_SMEM_CAP_KB");
-        size_t smem_cap = (cap_env ? (size_t)atoi(cap_env) : (size_t)74) * 1024;
-        while (copies > 1 && triangle_smem_bytes(bin.len, copies) > smem_cap) copies /= 2;
-        if (triangle_smem_bytes(bin.len, copies) > 227 * 1024) throw InvalidArg{"triangle histogram too large for shared memory"};
-        smem = triangle_smem_bytes(bin.len, copies);
-    } else if (sp.kind == TPCF_THREE_SIDE) {
-        while (copies > 0 && three_side_smem_bytes(bin.len, copies) > 200 * 1024) copies /= 2;
-        smem = three_side_smem_bytes(copies ? bin.len : 0, copies);
-    } else {
-        while (copies > 1 && pair_smem_bytes(bin.len, copies) > 200 * 1024) copies /= 2;
-        if (pair_smem_bytes(bin.len, copies) > 227 * 1024) throw InvalidArg{"pair histogram too large"};
-        smem = pair_smem_bytes(bin.len, copies);
-    }
     const unsigned int nt = (unsigned int)ntasks;
-    const int grid = occupancy_grid(ctx, sp.kind, smem, fp64, nt);
     const uint64_t launches = (sp.kind == TPCF_TRIANGLE && !fp64) ? 2 : 1;
     const char* genv = getenv("TPCF_GRAPHS");
     const bool graphs = L.graphs_ok && !(genv && genv[0] == '0');
@@ -969,106 +1079,173 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
     L.h_counters.reserve(8);
     unsigned int queue_cap = (unsigned int)std::max<size_t>(L.d_queue.n, (size_t)1 << 22);
     uint64_t dev_evaluated = 0, dev_binned = 0, replays = 0;
-    for (int attempt = 0; attempt < 3; attempt++) {
-        RecheckQueue q{};
-        if (sp.kind == TPCF_TRIANGLE && !fp64) {
-            if (L.d_queue.n < queue_cap) L.drop_graph();
-            L.d_queue.reserve(queue_cap);
-            q.items = L.d_queue.p;
-            q.count = L.d_counters.p + 1;
-            q.cap = queue_cap;
-            q.evaluated = reinterpret_cast<unsigned long long*>(L.d_counters.p + 2);
-        }
-        // the whole step as stream work: zero, count, recheck, copy back
-        auto enqueue = [&](bool capturing) -> cudaError_t {
-            const unsigned int ev_flags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
-            cudaError_t e;
-#define EQ(x)                                 \
-    do {                                      \
+
+    // One complete count of the group with launch shape sh: zero, count,
+    // recheck, copy back (replayed from a captured graph when allowed and
+    // the batch repeats).  Returns the device time in ms.
+    auto count_with = [&](const Shape& sh, bool allow_graph) -> float {
+        const int copies = sh.copies;
+        const int grid = grid_for(ctx, sh, nt);
+        for (int attempt = 0; attempt < 3; attempt++) {
+            RecheckQueue q{};
+            if (sp.kind == TPCF_TRIANGLE && !fp64) {
+                if (L.d_queue.n < queue_cap) L.drop_graph();
+                L.d_queue.reserve(queue_cap);
+                q.items = L.d_queue.p;
+                q.count = L.d_counters.p + 1;
+                q.cap = queue_cap;
+                q.evaluated = reinterpret_cast<unsigned long long*>(L.d_counters.p + 2);
+            }
+            auto enqueue = [&](bool capturing) -> cudaError_t {
+                const unsigned int ev_flags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+                cudaError_t e;
+#define EQ(x)                                   \
+    do {                                        \
         if ((e = (x)) != cudaSuccess) return e; \
     } while (0)
-            EQ(cudaMemsetAsync(L.d_hist.p, 0, hist_total * sizeof(unsigned long long), st));
-            EQ(cudaMemsetAsync(L.d_counters.p, 0, 8 * sizeof(unsigned int), st));
-            EQ(cudaEventRecordWithFlags(L.ev0, st, ev_flags));
-            if (sp.kind == TPCF_TRIANGLE && fp64) {
-                EQ(launch_triangle_fp64(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.tri, acos_t, grid, copies,
-                                        sp.precision == TPCF_GEOMETRY_FP64, st));
-                EQ(cudaEventRecordWithFlags(L.ev_mid, st, ev_flags));
-            } else if (sp.kind == TPCF_TRIANGLE) {
-                EQ(launch_triangle_fast(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.tri, q, grid, copies, st));
-                EQ(cudaEventRecordWithFlags(L.ev_mid, st, ev_flags));
-                EQ(launch_triangle_recheck(L.d_jobs.p, q, bin.tri, acos_t, ctx->num_sms * 8, st));
-            } else if (sp.kind == TPCF_THREE_SIDE) {
-                EQ(launch_three_side(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.three, fp64, grid, copies, st));
-                EQ(cudaEventRecordWithFlags(L.ev_mid, st, ev_flags));
-            } else {
-                EQ(launch_pairs(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.pair, fp64, grid, copies, st));
-                EQ(cudaEventRecordWithFlags(L.ev_mid, st, ev_flags));
-            }
-            EQ(cudaEventRecordWithFlags(L.ev1, st, ev_flags));
-            EQ(cudaMemcpyAsync(L.h_counters.p, L.d_counters.p, 8 * sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
-            EQ(cudaMemcpyAsync(L.h_hist.p, L.d_hist.p, hist_total * sizeof(unsigned long long),
-                               cudaMemcpyDeviceToHost, st));
-#undef EQ
-            return cudaSuccess;
-        };
-        bool replayed = false;
-        if (graphs) {
-            // everything the captured launches read: the batch, its buffers, the shape
-            std::vector<uint64_t> gsig = sig;
-            const uint64_t extra[] = {(uint64_t)(uintptr_t)L.d_jobs.p, (uint64_t)(uintptr_t)L.d_tasks.p,
-                                      (uint64_t)(uintptr_t)L.d_counters.p, (uint64_t)(uintptr_t)L.d_queue.p,
-                                      (uint64_t)(uintptr_t)L.h_hist.p, (uint64_t)(uintptr_t)L.h_counters.p,
-                                      (uint64_t)(uintptr_t)acos_t.keys, (uint64_t)(uintptr_t)acos_t.vals,
-                                      (uint64_t)(uintptr_t)acos_t.bucket, (uint64_t)acos_t.n, queue_cap, (uint64_t)grid,
-                                      (uint64_t)copies, hist_total, ntasks};
-            gsig.insert(gsig.end(), extra, extra + sizeof(extra) / sizeof(extra[0]));
-            if (!L.graph || gsig != L.graph_sig) {
-                L.drop_graph();
-                cudaGraph_t g = nullptr;
-                cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
-                if (e == cudaSuccess) {
-                    cudaError_t e1 = enqueue(true);
-                    cudaError_t e2 = cudaStreamEndCapture(st, &g);
-                    e = e1 != cudaSuccess ? e1 : e2;
-                }
-                if (e == cudaSuccess) e = cudaGraphInstantiate(&L.graph, g, 0);
-                if (g) cudaGraphDestroy(g);
-                if (e == cudaSuccess) {
-                    L.graph_sig = gsig;
+                EQ(cudaMemsetAsync(L.d_hist.p, 0, hist_total * sizeof(unsigned long long), st));
+                EQ(cudaMemsetAsync(L.d_counters.p, 0, 8 * sizeof(unsigned int), st));
+                EQ(cudaEventRecordWithFlags(L.ev0, st, ev_flags));
+                if (sp.kind == TPCF_TRIANGLE && fp64) {
+                    EQ(launch_triangle_fp64(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.tri, acos_t, grid, copies,
+                                            sp.precision == TPCF_GEOMETRY_FP64 ? 1 : 0, st));
+                    EQ(cudaEventRecordWithFlags(L.ev_mid, st, ev_flags));
+                } else if (sp.kind == TPCF_TRIANGLE) {
+                    EQ(launch_triangle_fast(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.tri, q, grid, copies, st));
+                    EQ(cudaEventRecordWithFlags(L.ev_mid, st, ev_flags));
+                    EQ(launch_triangle_recheck(L.d_jobs.p, q, bin.tri, acos_t, ctx->num_sms * 8, st));
+                } else if (sp.kind == TPCF_TRIANGLE_JBJ) {
+                    EQ(launch_triangle_fp64(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.tri, acos_t, grid, copies,
+                                            2, st));
+                    EQ(cudaEventRecordWithFlags(L.ev_mid, st, ev_flags));
+                } else if (sp.kind == TPCF_THREE_SIDE) {
+                    EQ(launch_three_side(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.three, fp64, grid, copies,
+                                         st));
+                    EQ(cudaEventRecordWithFlags(L.ev_mid, st, ev_flags));
                 } else {
-                    // capture unavailable here: issue the launches one by one from now on
-                    (void)cudaGetLastError();
-                    L.graph = nullptr;
-                    L.graphs_ok = false;
+                    EQ(launch_pairs(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.pair, fp64, grid, copies, st));
+                    EQ(cudaEventRecordWithFlags(L.ev_mid, st, ev_flags));
+                }
+                EQ(cudaEventRecordWithFlags(L.ev1, st, ev_flags));
+                EQ(cudaMemcpyAsync(L.h_counters.p, L.d_counters.p, 8 * sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                                   st));
+                EQ(cudaMemcpyAsync(L.h_hist.p, L.d_hist.p, hist_total * sizeof(unsigned long long),
+                                   cudaMemcpyDeviceToHost, st));
+#undef EQ
+                return cudaSuccess;
+            };
+            bool replayed = false;
+            if (allow_graph) {
+                // everything the captured launches read: the batch, its buffers, the shape
+                std::vector<uint64_t> gsig = sig;
+                const uint64_t extra[] = {(uint64_t)(uintptr_t)L.d_jobs.p, (uint64_t)(uintptr_t)L.d_tasks.p,
+                                          (uint64_t)(uintptr_t)L.d_counters.p, (uint64_t)(uintptr_t)L.d_queue.p,
+                                          (uint64_t)(uintptr_t)L.h_hist.p, (uint64_t)(uintptr_t)L.h_counters.p,
+                                          (uint64_t)(uintptr_t)acos_t.keys, (uint64_t)(uintptr_t)acos_t.vals,
+                                          (uint64_t)(uintptr_t)acos_t.bucket, (uint64_t)acos_t.n, queue_cap,
+                                          (uint64_t)grid, (uint64_t)copies, hist_total, ntasks};
+                gsig.insert(gsig.end(), extra, extra + sizeof(extra) / sizeof(extra[0]));
+                if (!L.graph || gsig != L.graph_sig) {
+                    L.drop_graph();
+                    cudaGraph_t g = nullptr;
+                    cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+                    if (e == cudaSuccess) {
+                        cudaError_t e1 = enqueue(true);
+                        cudaError_t e2 = cudaStreamEndCapture(st, &g);
+                        e = e1 != cudaSuccess ? e1 : e2;
+                    }
+                    if (e == cudaSuccess) e = cudaGraphInstantiate(&L.graph, g, 0);
+                    if (g) cudaGraphDestroy(g);
+                    if (e == cudaSuccess) {
+                        L.graph_sig = gsig;
+                    } else {
+                        // capture unavailable here: issue the launches one by one from now on
+                        (void)cudaGetLastError();
+                        L.graph = nullptr;
+                        L.graphs_ok = false;
+                    }
+                }
+                if (L.graph) {
+                    CK(cudaGraphLaunch(L.graph, st));
+                    replayed = true;
                 }
             }
-            if (L.graph) {
-                CK(cudaGraphLaunch(L.graph, st));
-                replayed = true;
+            if (!replayed) CK(enqueue(false));
+            CK(cudaStreamSynchronize(st));
+            replays = replayed ? 1 : 0;
+            const unsigned int* counters = L.h_counters.p;
+            L.d2h += 8 * sizeof(unsigned int) + hist_total * sizeof(unsigned long long);
+            L.stats.recheck_units = counters[1];
+            memcpy(&dev_evaluated, &counters[2], sizeof(dev_evaluated));
+            memcpy(&dev_binned, &counters[4], sizeof(dev_binned));
+            if (sp.kind == TPCF_TRIANGLE && !fp64 && counters[1] > queue_cap) {
+                // the recheck queue overflowed: grow it and count again
+                queue_cap =
+                    (unsigned int)std::min<uint64_t>((uint64_t)counters[1] + (counters[1] >> 2) + 1024, 0xF0000000ull);
+                continue;
+            }
+            break;
+        }
+        float t = 0;
+        CK(cudaEventElapsedTime(&t, L.ev0, L.ev1));
+        return t;
+    };
+
+    // Launch shape: the tuned one for this batch if the autotuner has seen it,
+    // else the default.  A batch that repeats (its plan was cached) and has no
+    // tuned shape yet is counted once with every candidate shape -- each count
+    // is exact -- and the fastest is kept for the next calls.
+    const std::vector<Shape> cands = shape_candidates(ctx, sp, bin, fp64 || sp.kind == TPCF_TRIANGLE_JBJ);
+    uint64_t key = 1469598103934665603ull;
+    for (uint64_t v : sig) key = (key ^ v) * 1099511628211ull;
+    const char* tenv = getenv("TPCF_AUTOTUNE");
+    const bool autotune = !(tenv && tenv[0] == '0');
+    Shape shape = cands[0];
+    uint64_t tuned_runs = 0;
+    {
+        std::lock_guard<std::mutex> tlk(ctx->tune_mu);
+        auto it = ctx->tuned.find(key);
+        if (it != ctx->tuned.end()) shape = it->second;
+    }
+    bool tuned_known = false;
+    {
+        std::lock_guard<std::mutex> tlk(ctx->tune_mu);
+        tuned_known = ctx->tuned.count(key) > 0;
+    }
+    if (autotune && plan_hit && !tuned_known && cands.size() > 1) {
+        float best = INFINITY;
+        for (const Shape& c : cands) {
+            float t = count_with(c, false);
+            tuned_runs++;
+            if (t < best) {
+                best = t;
+                shape = c;
             }
         }
-        if (!replayed) CK(enqueue(false));
-        CK(cudaStreamSynchronize(st));
-        replays = replayed ? 1 : 0;
-        const unsigned int* counters = L.h_counters.p;
-        L.d2h += 8 * sizeof(unsigned int) + hist_total * sizeof(unsigned long long);
-        L.stats.recheck_units = counters[1];
-        memcpy(&dev_evaluated, &counters[2], sizeof(dev_evaluated));
-        memcpy(&dev_binned, &counters[4], sizeof(dev_binned));
-        if (sp.kind == TPCF_TRIANGLE && !fp64 && counters[1] > queue_cap) {
-            // the recheck queue overflowed: grow it and count again
-            queue_cap = (unsigned int)std::min<uint64_t>((uint64_t)counters[1] + (counters[1] >> 2) + 1024, 0xF0000000ull);
-            continue;
-        }
-        break;
+        std::lock_guard<std::mutex> tlk(ctx->tune_mu);
+        ctx->tuned[key] = shape;
+    } else {
+        count_with(shape, graphs);
     }
+    L.stats.tuned_shapes = tuned_runs;
+    L.stats.hist_copies = (uint64_t)shape.copies;
+    L.stats.ctas_per_sm = (uint64_t)shape.per_sm;
     float ms = 0, ms_main = 0;
     CK(cudaEventElapsedTime(&ms, L.ev0, L.ev1));
     CK(cudaEventElapsedTime(&ms_main, L.ev0, L.ev_mid));
     L.stats.main_kernel_ms = ms_main;
-    for (size_t g = 0; g < group.size(); g++)
-        memcpy(group[g].out, L.h_hist.p + (size_t)bin.len * g, (size_t)bin.len * sizeof(uint64_t));
+    // JBJ compat: the reference's two extra counts in bin 0 per visited triangle
+    if (sp.kind == TPCF_TRIANGLE_JBJ && sp.overflow == TPCF_OVERFLOW_COMPAT && bin.len > 0)
+        for (size_t g = 0; g < group.size(); g++) L.h_hist.p[(size_t)bin.len * slot_of[g]] += 2 * pj[g].loop_units;
+    for (size_t k = 0; k < nslots; k++) {
+        const GroupJob& gj = group[slot_job[k]];
+        const unsigned long long* src = L.h_hist.p + (size_t)bin.len * k;
+        if (gj.accumulate) {
+            for (int64_t b = 0; b < bin.len; b++) gj.out[b] += src[b];
+        } else {
+            memcpy(gj.out, src, (size_t)bin.len * sizeof(uint64_t));
+        }
+    }
     L.stats.graph_replays = replays;
     L.stats.kernel_ms = ms;
     L.stats.loop_units = units;
@@ -1078,19 +1255,22 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
     L.stats.evaluated_units = (sp.kind == TPCF_TRIANGLE && !fp64) ? dev_evaluated : evaluated;
     L.stats.binned_units = (sp.kind == TPCF_TRIANGLE && !fp64) ? dev_binned : evaluated;
     L.stats.tasks = ntasks;
-    L.stats.kernel_launches = launches;
+    L.stats.kernel_launches = launches * std::max<uint64_t>(1, tuned_runs);
     L.stats.total_ms =
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_wall0).count();
 }
 
 void validate(const tpcf_spec* sp, const tpcf_job* job) {
     if (!sp || !job) throw InvalidArg{"null spec or job"};
-    if (sp->kind != TPCF_THREE_SIDE && sp->kind != TPCF_TRIANGLE && sp->kind != TPCF_PAIR) throw InvalidArg{"bad kind"};
+    if (sp->kind != TPCF_THREE_SIDE && sp->kind != TPCF_TRIANGLE && sp->kind != TPCF_PAIR &&
+        sp->kind != TPCF_TRIANGLE_JBJ)
+        throw InvalidArg{"bad kind"};
     if (sp->loop < TPCF_LOOP_ALL || sp->loop > TPCF_LOOP_ONE) throw InvalidArg{"bad loop"};
     if (sp->precision != TPCF_GUARDED_FP32 && sp->precision != TPCF_PLAIN_FP64 && sp->precision != TPCF_GEOMETRY_FP64)
         throw InvalidArg{"bad precision"};
     if (sp->precision == TPCF_GEOMETRY_FP64 && sp->kind != TPCF_TRIANGLE)
         throw InvalidArg{"TPCF_GEOMETRY_FP64 is implemented for the triangle parametrization only"};
+    if ((job->flags & ~(uint32_t)TPCF_JOB_GLOBAL_INDEX) != 0 || job->reserved != 0) throw InvalidArg{"bad job flags"};
     (void)make_binning(*sp);
 }
 
@@ -1192,7 +1372,7 @@ void worker_loop(tpcf_ctx* ctx, int lane) {
         for (auto& p : batch) {
             p->result.assign((size_t)len, 0);
             p->t_start = t_start;
-            group.push_back({&p->spec, &p->job, p->result.data()});
+            group.push_back({&p->spec, &p->job, p->result.data(), false});
         }
         tpcf_status st = guarded(ctx, [&] { run_group(ctx, L, group); });
         double t_done = now_ms();
@@ -1351,7 +1531,8 @@ tpcf_status tpcf_resident_bytes(tpcf_ctx* ctx, int64_t* bytes) {
 tpcf_status tpcf_hist_len(const tpcf_spec* sp, int64_t* len) {
     if (!sp || !len) return TPCF_ERR_INVALID;
     if (sp->kind == TPCF_THREE_SIDE) *len = (int64_t)sp->axis[0].nbins * sp->axis[0].nbins * sp->axis[0].nbins;
-    else if (sp->kind == TPCF_TRIANGLE) *len = (int64_t)sp->axis[0].nbins * sp->axis[1].nbins * sp->axis[2].nbins;
+    else if (sp->kind == TPCF_TRIANGLE || sp->kind == TPCF_TRIANGLE_JBJ)
+        *len = (int64_t)sp->axis[0].nbins * sp->axis[1].nbins * sp->axis[2].nbins;
     else if (sp->kind == TPCF_PAIR) *len = sp->axis[0].nbins;
     else return TPCF_ERR_INVALID;
     return TPCF_OK;
@@ -1372,17 +1553,34 @@ tpcf_status tpcf_loop_units(tpcf_ctx* ctx, const tpcf_spec* sp, const tpcf_job* 
     return TPCF_OK;
 }
 
-tpcf_status tpcf_count_batch(tpcf_ctx* ctx, const tpcf_spec* specs, const tpcf_job* jobs, int32_t n,
-                             uint64_t* const* hists) {
-    if (!ctx || !specs || !jobs || !hists || n < 0) return fail(ctx, TPCF_ERR_INVALID, "bad batch arguments");
+namespace {
+
+// Jobs grouped by binning (and pruning); each group is one persistent launch.
+// out_index == nullptr: job i writes hists[i]; else job i adds into
+// hists[out_index[i]] (zeroed first).
+tpcf_status count_jobs(tpcf_ctx* ctx, const tpcf_spec* specs, const tpcf_job* jobs, int32_t n,
+                       const int32_t* out_index, int32_t n_out, uint64_t* const* hists) {
     std::lock_guard<std::recursive_mutex> lk(ctx->mu);
     return guarded(ctx, [&] {
         CK(cudaSetDevice(ctx->device));
+        std::vector<int64_t> out_len(out_index ? n_out : 0, -1);
         for (int i = 0; i < n; i++) {
             validate(&specs[i], &jobs[i]);
-            if (!hists[i]) throw InvalidArg{"null histogram pointer"};
+            if (out_index) {
+                const int32_t o = out_index[i];
+                if (o < 0 || o >= n_out) throw InvalidArg{"out_index out of range"};
+                if (!hists[o]) throw InvalidArg{"null histogram pointer"};
+                int64_t len = 0;
+                tpcf_hist_len(&specs[i], &len);
+                if (out_len[o] >= 0 && out_len[o] != len) throw InvalidArg{"jobs of one output differ in histogram length"};
+                out_len[o] = len;
+            } else if (!hists[i]) {
+                throw InvalidArg{"null histogram pointer"};
+            }
         }
-        // group by (binning, loop); each group is one persistent launch
+        if (out_index)
+            for (int32_t o = 0; o < n_out; o++)
+                if (out_len[o] > 0) memset(hists[o], 0, (size_t)out_len[o] * sizeof(uint64_t));
         std::vector<char> done(n, 0);
         tpcf_stats acc{};
         for (int i = 0; i < n; i++) {
@@ -1390,7 +1588,8 @@ tpcf_status tpcf_count_batch(tpcf_ctx* ctx, const tpcf_spec* specs, const tpcf_j
             std::vector<GroupJob> g;
             for (int k = i; k < n; k++)
                 if (!done[k] && same_binning(specs[k], specs[i]) && specs[k].prune == specs[i].prune) {
-                    g.push_back({&specs[k], &jobs[k], hists[k]});
+                    if (out_index) g.push_back({&specs[k], &jobs[k], hists[out_index[k]], true});
+                    else g.push_back({&specs[k], &jobs[k], hists[k], false});
                     done[k] = 1;
                 }
             Lane& L = *ctx->lanes[0];
@@ -1405,8 +1604,57 @@ tpcf_status tpcf_count_batch(tpcf_ctx* ctx, const tpcf_spec* specs, const tpcf_j
             acc.tasks += L.stats.tasks;
             acc.kernel_launches += L.stats.kernel_launches;
             acc.graph_replays += L.stats.graph_replays;
+            acc.tuned_shapes += L.stats.tuned_shapes;
+            acc.hist_copies = L.stats.hist_copies;
+            acc.ctas_per_sm = L.stats.ctas_per_sm;
         }
         ctx->lanes[0]->stats = acc;
+    });
+}
+
+}  // namespace
+
+tpcf_status tpcf_count_batch(tpcf_ctx* ctx, const tpcf_spec* specs, const tpcf_job* jobs, int32_t n,
+                             uint64_t* const* hists) {
+    if (!ctx || !specs || !jobs || !hists || n < 0) return fail(ctx, TPCF_ERR_INVALID, "bad batch arguments");
+    return count_jobs(ctx, specs, jobs, n, nullptr, 0, hists);
+}
+
+tpcf_status tpcf_count_batch_into(tpcf_ctx* ctx, const tpcf_spec* specs, const tpcf_job* jobs, int32_t n,
+                                  const int32_t* out_index, int32_t n_out, uint64_t* const* hists) {
+    if (!ctx || !specs || !jobs || !out_index || !hists || n < 0 || n_out < 0)
+        return fail(ctx, TPCF_ERR_INVALID, "bad batch arguments");
+    return count_jobs(ctx, specs, jobs, n, out_index, n_out, hists);
+}
+
+tpcf_status tpcf_convert_radecz(tpcf_ctx* ctx, const double* ra, const double* dec, const double* redshift,
+                                int64_t n, const double* poly, float* x, float* y, float* z) {
+    if (!ctx || n < 0 || (n > 0 && (!ra || !dec || !redshift || !x || !y || !z)))
+        return fail(ctx, TPCF_ERR_INVALID, "bad conversion arguments");
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    return guarded(ctx, [&] {
+        if (n == 0) return;
+        CK(cudaSetDevice(ctx->device));
+        const double mice[3] = {-1.07199554e+00, 3.01313296e+03, -6.38827998e+02};  // the script's fit
+        const double* pc = poly ? poly : mice;
+        Lane& L = *ctx->lanes[0];
+        DevBuf<double> d_in;
+        DevBuf<float> d_out;
+        d_in.reserve(3 * (size_t)n);
+        d_out.reserve(3 * (size_t)n);
+        const size_t b = (size_t)n * sizeof(double);
+        CK(cudaMemcpyAsync(d_in.p, ra, b, cudaMemcpyHostToDevice, L.stream));
+        CK(cudaMemcpyAsync(d_in.p + n, dec, b, cudaMemcpyHostToDevice, L.stream));
+        CK(cudaMemcpyAsync(d_in.p + 2 * n, redshift, b, cudaMemcpyHostToDevice, L.stream));
+        CK(launch_radecz_to_xyz(d_in.p, d_in.p + n, d_in.p + 2 * n, n, pc, d_out.p, d_out.p + n, d_out.p + 2 * n,
+                                L.stream));
+        const size_t fb = (size_t)n * sizeof(float);
+        CK(cudaMemcpyAsync(x, d_out.p, fb, cudaMemcpyDeviceToHost, L.stream));
+        CK(cudaMemcpyAsync(y, d_out.p + n, fb, cudaMemcpyDeviceToHost, L.stream));
+        CK(cudaMemcpyAsync(z, d_out.p + 2 * n, fb, cudaMemcpyDeviceToHost, L.stream));
+        CK(cudaStreamSynchronize(L.stream));
+        L.h2d += 3 * b;
+        L.d2h += 3 * fb;
     });
 }
 

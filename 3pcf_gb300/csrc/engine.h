@@ -19,11 +19,15 @@ enum Pred : uint32_t {
     PRED_SAME = 2,   // key_i <= key_j <= key_k                      (loop SAME, generic arrays)
     PRED_ONE = 3     // key_j <= key_k                               (loop ONE, generic arrays)
 };
-// Task flag bits (task.x bits 24..31)
-constexpr uint32_t TASK_DIAG_IJ = 1u << 24;  // tiles I and J are the same tile of one view: j > i
-constexpr uint32_t TASK_DIAG_JK = 1u << 25;  // tiles J and K are the same tile of one view: k > j
-constexpr uint32_t TASK_SLOT_MASK = 0xFFFFu;
-constexpr int TASK_PRED_SHIFT = 16;          // bits 16..23: Pred
+// task.x: bits 0..21 job slot, 22..24 Pred, 28/29 diagonal flags
+constexpr uint32_t TASK_SLOT_MASK = 0x3FFFFFu;
+constexpr uint32_t MAX_BATCH_JOBS = TASK_SLOT_MASK;  // jobs of one launch
+constexpr int TASK_PRED_SHIFT = 22;
+constexpr uint32_t TASK_PRED_MASK = 0x7u;
+constexpr uint32_t TASK_DIAG_IJ = 1u << 28;  // tiles I and J are the same tile of one view: j > i
+constexpr uint32_t TASK_DIAG_JK = 1u << 29;  // tiles J and K are the same tile of one view: k > j
+// recheck queue item .x: job slot | weight << 22
+constexpr int RECHECK_WEIGHT_SHIFT = 22;
 
 // Per-side word of the triangle kernels: word = code * 128 + class_weight.
 // code is the side's s-bin times Q*T (monotone in the side length, so the
@@ -100,7 +104,7 @@ struct AcosTable {
 
 // Guard-band recheck queue (device scratch).
 struct RecheckQueue {
-    uint4* items;                // {slot | weight << 16, ia, ib, ic}
+    uint4* items;                // {slot | weight << RECHECK_WEIGHT_SHIFT, ia, ib, ic}
     unsigned int* count;
     unsigned int cap;
     unsigned long long* evaluated;  // triangles of (i,j) pairs the fast kernel walked
@@ -118,7 +122,7 @@ cudaError_t launch_triangle_recheck(const DevJob* jobs, RecheckQueue q, const Tr
                                     int grid, cudaStream_t st);
 cudaError_t launch_triangle_fp64(const DevJob* jobs, const uint4* tasks, unsigned int ntasks,
                                  unsigned int* task_counter, const TriParams& p, AcosTable t, int grid,
-                                 int hist_copies, bool geometry, cudaStream_t st);
+                                 int hist_copies, int mode, cudaStream_t st);  // mode: 0 FP64, 1 geometry, 2 JBJ
 cudaError_t launch_three_side(const DevJob* jobs, const uint4* tasks, unsigned int ntasks,
                               unsigned int* task_counter, const ThreeParams& p, int fp64, int grid,
                               int hist_copies, cudaStream_t st);
@@ -127,6 +131,8 @@ cudaError_t launch_pairs(const DevJob* jobs, const uint4* tasks, unsigned int nt
                          int hist_copies, cudaStream_t st);
 cudaError_t launch_acos_check(AcosTable t, uint32_t key_begin, uint32_t count, unsigned int* mismatches,
                               cudaStream_t st);
+cudaError_t launch_radecz_to_xyz(const double* ra, const double* dec, const double* redshift, int64_t n,
+                                 const double poly[3], float* x, float* y, float* z, cudaStream_t st);
 
 // shared-memory bytes of a launch (for occupancy / admission)
 size_t triangle_smem_bytes(int hist_len, int hist_copies);

@@ -261,7 +261,8 @@ __device__ __forceinline__ float rsqrt_approx(float x) {
 
 constexpr int TRI_WARPS = 8;
 constexpr int TRI_THREADS = TRI_WARPS * 32;
-constexpr int TRI_QCAP = 128;  // per-warp candidate queue: up to 63 pending + 64 new
+constexpr int TRI_QCAP = 256;  // per-warp candidate list window
+constexpr int TRI_HEAVY = 8;   // candidate k's from which a j is expanded by the whole warp
 // per j of role B: bit masks over k of the classes of side j-k (B, I, M, H)
 // and of key_k >= key_j; held in shared memory as five 64-entry arrays
 // (JM_WORDS x TILE, word-major) so that lanes reading different j's do not
@@ -404,7 +405,7 @@ __device__ __forceinline__ bool triangle_full(float a, int wa, float b, int wb, 
 __device__ __forceinline__ void push_recheck(RecheckQueue& q, uint32_t slot, unsigned w, uint32_t ia, uint32_t ib,
                                              uint32_t ic) {
     unsigned int pos = atomicAdd(q.count, 1u);
-    if (pos < q.cap) q.items[pos] = make_uint4(slot | (w << 16), ia, ib, ic);
+    if (pos < q.cap) q.items[pos] = make_uint4(slot | (w << RECHECK_WEIGHT_SHIFT), ia, ib, ic);
 }
 
 struct TaskGeom {
@@ -492,9 +493,9 @@ __device__ __forceinline__ unsigned long long candidate_mask(int cij, unsigned l
 
 template <int PRED, bool THETA_FULL>
 __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams& p, float4* P, int2* JK,
-                                   int2* IJ, int2* IK, uint32_t* Q, unsigned long long* JM, unsigned int* Hw,
-                                   RecheckQueue& q, unsigned long long& evaluated, unsigned long long& binned,
-                                   int* next_i) {
+                                   int2* IJ, int2* IK, uint32_t* Q, unsigned long long* JM, float* BX,
+                                   unsigned int* Hw, RecheckQueue& q, unsigned long long& evaluated,
+                                   unsigned long long& binned, int* next_i) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const TaskGeom g = task_geom(J, task);
     const uint32_t slot = task.x & TASK_SLOT_MASK;
@@ -502,10 +503,58 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
     load_points(P, J, g);
     if (threadIdx.x == 0) *next_i = 0;
     __syncthreads();
+    // bounding boxes of the three tiles (two 32-point halves each)
+    if (warp < 6) {
+        const int role = warp >> 1, idx = (warp & 1) * 32 + lane;
+        const int n = role == 0 ? g.nA : (role == 1 ? g.nB : g.nC);
+        const float4 pt = P[role * TILE + idx];
+        const bool valid = idx < n;
+        float lo[3] = {valid ? pt.x : INFINITY, valid ? pt.y : INFINITY, valid ? pt.z : INFINITY};
+        float hi[3] = {valid ? pt.x : -INFINITY, valid ? pt.y : -INFINITY, valid ? pt.z : -INFINITY};
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+                hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+            }
+        if (lane < 3) BX[warp * 6 + lane] = lo[lane];
+        else if (lane < 6) BX[warp * 6 + lane] = hi[lane - 3];
+    }
+    __syncthreads();
+    // a side that provably reaches lmax is rejected whatever its exact value:
+    // points farther than that from a whole tile take no part in the task
+    // (the 1e-5 margin covers the rounding of the bound and of the distance)
+    const float reach = p.lmax * (1.0f + 1e-5f);
+    const float reach2 = reach * reach;
+    auto far_from = [&](float4 pt, int role) -> bool {
+        const float* b0 = BX + role * 12;
+        float s2 = 0.f;
+        {
+            const float lo = fminf(b0[0], b0[6]), hi = fmaxf(b0[3], b0[9]);
+            const float gap = fmaxf(0.f, fmaxf(lo - pt.x, pt.x - hi));
+            s2 = fmaf(gap, gap, s2);
+        }
+        {
+            const float lo = fminf(b0[1], b0[7]), hi = fmaxf(b0[4], b0[10]);
+            const float gap = fmaxf(0.f, fmaxf(lo - pt.y, pt.y - hi));
+            s2 = fmaf(gap, gap, s2);
+        }
+        {
+            const float lo = fminf(b0[2], b0[8]), hi = fmaxf(b0[5], b0[11]);
+            const float gap = fmaxf(0.f, fmaxf(lo - pt.z, pt.z - hi));
+            s2 = fmaf(gap, gap, s2);
+        }
+        return s2 >= reach2;
+    };
     // rows j of the j-k side table and their class masks, one warp per row
     const int key_k0 = pkey(P[2 * TILE + lane]), key_k1 = pkey(P[2 * TILE + lane + 32]);
     for (int j = warp; j < g.nB; j += TRI_WARPS) {
         const float4 pj = P[TILE + j];
+        if (far_from(pj, 0)) {  // no i reaches j: empty masks, the row is never read
+            if (lane < JM_WORDS) JM[lane * TILE + j] = 0ull;
+            continue;
+        }
         int c0 = 0, c1 = 0;
         if (lane < g.nC) {
             float d = ref_dist<false>(pj, P[2 * TILE + lane]);
@@ -531,7 +580,6 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
     int2* row_ij = IJ + warp * TILE;
     int2* row_ik = IK + warp * TILE;
     uint32_t* cand = Q + warp * TRI_QCAP;
-    const unsigned lt = (1u << lane) - 1u;
     unsigned ev = 0, bn = 0;
     for (;;) {
         // points of role A are handed out to warps dynamically (balances the
@@ -541,6 +589,7 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
         i = __shfl_sync(0xffffffffu, i, 0);
         if (i >= g.nA) break;
         const float4 pi = P[i];
+        if (far_from(pi, 1) || far_from(pi, 2)) continue;
         const int ki = pkey(pi);
         // i-k sides: words for the binning path, class masks for the filter
         int c0 = 0, c1 = 0;
@@ -559,6 +608,7 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
         const unsigned long long nB = ballot64(c0 == 1, c1 == 1), nI = ballot64(c0 == 2, c1 == 2);
         const unsigned long long nM = ballot64(c0 == 3, c1 == 3), nH = ballot64(c0 == 4, c1 == 4);
         const unsigned long long any_k = nB | nI | nM | nH;
+        if (!any_k) continue;  // no k within reach of i (warp-uniform)
         unsigned long long kge_i = 0;
         if (PRED == PRED_DDR) kge_i = ballot64(lane < g.nC && key_k0 >= ki, lane + 32 < g.nC && key_k1 >= ki);
         // i-j sides: words for the binning path; each lane then forms the
@@ -596,14 +646,70 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
               (unsigned)(__popc(__ballot_sync(0xffffffffu, ok0)) + __popc(__ballot_sync(0xffffffffu, ok1)));
         __syncwarp();
         const uint32_t ia = (uint32_t)(g.a0 + i);
-        int qn = 0;  // queued candidates (warp-uniform)
-        // queue the candidates of every j whose mask is not empty, in turn
-        auto emit = [&](unsigned long long cmv, unsigned long long w2v, int jbase) {
-            unsigned live = __ballot_sync(0xffffffffu, cmv != 0ull);
+        // Candidate list of this i.  A j with many candidate k's is expanded
+        // by the whole warp (lanes over k, one j at a time); the candidates of
+        // the other j's are compacted lane-parallel: each lane walks the few
+        // bits of its own two j's into slots from a prefix sum of the counts.
+        // Both lists are binned in chunks of up to 64.
+        const bool heavy0 = __popcll(cm0) >= TRI_HEAVY, heavy1 = __popcll(cm1) >= TRI_HEAVY;
+        {
+            const unsigned long long l0 = heavy0 ? 0ull : cm0, l1 = heavy1 ? 0ull : cm1;
+            const int cnt = __popcll(l0) + __popcll(l1);
+            int incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += v;
+            }
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            const int base = incl - cnt;
+            for (int w0 = 0; w0 < total; w0 += TRI_QCAP) {
+                const int w1 = w0 + TRI_QCAP;
+                if (cnt > 0 && base < w1 && base + cnt > w0) {
+                    int pos = base;
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        unsigned long long m = h ? l1 : l0;
+                        const unsigned long long m2 = h ? w21 : w20;
+                        const int j = lane + 32 * h;
+                        // skip the candidates of earlier windows
+                        if (pos + __popcll(m) <= w0) {
+                            pos += __popcll(m);
+                            m = 0;
+                        }
+                        while (m && pos < w0) {
+                            m &= m - 1ull;
+                            pos++;
+                        }
+                        while (m && pos < w1) {
+                            const int k = __ffsll((long long)m) - 1;
+                            m &= m - 1ull;
+                            const unsigned w = PRED == PRED_DDR ? 1u + (unsigned)((m2 >> k) & 1ull) : 1u;
+                            cand[pos - w0] = pack_cand(j, k, w);
+                            pos++;
+                        }
+                    }
+                }
+                __syncwarp();
+                const int nwin = min(TRI_QCAP, total - w0);
+                for (int c = 0; c < nwin; c += 64) {
+                    const int nc = min(64, nwin - c);
+                    run_candidates<THETA_FULL>(cand + c, nc, row_ij, row_ik, JK, p, Hw, q, slot, ia, g.b0, g.c0);
+                }
+                bn += nwin;
+                __syncwarp();
+            }
+        }
+        const unsigned lt = (1u << lane) - 1u;
+        int qn = 0;  // queued candidates of heavy j's (warp-uniform)
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            unsigned live = __ballot_sync(0xffffffffu, h ? heavy1 : heavy0);
+            const unsigned long long cmv = h ? cm1 : cm0, w2v = h ? w21 : w20;
             while (live) {
                 const int src = __ffs(live) - 1;
                 live &= live - 1u;
-                const int j = src + jbase;
+                const int j = src + 32 * h;
                 const unsigned lo = __shfl_sync(0xffffffffu, (unsigned)cmv, src);
                 const unsigned hi = __shfl_sync(0xffffffffu, (unsigned)(cmv >> 32), src);
                 unsigned w2lo = 0, w2hi = 0;
@@ -629,9 +735,7 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
                     __syncwarp();
                 }
             }
-        };
-        emit(cm0, w20, 0);
-        emit(cm1, w21, 32);
+        }
         if (qn > 0) {
             run_candidates<THETA_FULL>(cand, qn, row_ij, row_ik, JK, p, Hw, q, slot, ia, g.b0, g.c0);
             bn += qn;
@@ -645,13 +749,13 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
 template <bool THETA_FULL>
 __device__ __forceinline__ void triangle_dispatch(const DevJob& J, uint4 task, const TriParams& p, float4* P,
                                                   int2* JK, int2* IJ, int2* IK, uint32_t* Q,
-                                                  unsigned long long* JM, unsigned int* Hw, RecheckQueue& q,
+                                                  unsigned long long* JM, float* BX, unsigned int* Hw, RecheckQueue& q,
                                                   unsigned long long& ev, unsigned long long& bn, int* next_i) {
-    switch ((task.x >> TASK_PRED_SHIFT) & 0xFF) {
-        case PRED_NONE: triangle_task_fast<PRED_NONE, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, JM, Hw, q, ev, bn, next_i); break;
-        case PRED_DDR: triangle_task_fast<PRED_DDR, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, JM, Hw, q, ev, bn, next_i); break;
-        case PRED_SAME: triangle_task_fast<PRED_SAME, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, JM, Hw, q, ev, bn, next_i); break;
-        default: triangle_task_fast<PRED_ONE, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, JM, Hw, q, ev, bn, next_i); break;
+    switch ((task.x >> TASK_PRED_SHIFT) & TASK_PRED_MASK) {
+        case PRED_NONE: triangle_task_fast<PRED_NONE, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i); break;
+        case PRED_DDR: triangle_task_fast<PRED_DDR, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i); break;
+        case PRED_SAME: triangle_task_fast<PRED_SAME, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i); break;
+        default: triangle_task_fast<PRED_ONE, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i); break;
     }
 }
 
@@ -672,6 +776,7 @@ triangle_fast_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ 
     unsigned int* H = reinterpret_cast<unsigned int*>(JM + JM_WORDS * TILE);
     __shared__ uint4 s_task;
     __shared__ int s_next_i;
+    __shared__ float s_box[6 * 6];  // tile bounding boxes: 6 half-tiles x {lo, hi}
     for (int b = threadIdx.x; b < copies * p.len; b += blockDim.x) H[b] = 0;
     unsigned int* Hw = H + ((threadIdx.x >> 5) % copies) * p.len;
     int cur = -1;
@@ -693,7 +798,7 @@ triangle_fast_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ 
         cur = slot;
         if (slot < 0) break;
         since++;
-        triangle_dispatch<THETA_FULL>(jobs[slot], task, p, P, JK, IJ, IK, Q, JM, Hw, q, ev, bn, &s_next_i);
+        triangle_dispatch<THETA_FULL>(jobs[slot], task, p, P, JK, IJ, IK, Q, JM, s_box, Hw, q, ev, bn, &s_next_i);
     }
     if ((threadIdx.x & 31) == 0) {
         if (ev) atomicAdd(q.evaluated, ev);
@@ -707,8 +812,8 @@ __global__ void triangle_recheck_kernel(const DevJob* __restrict__ jobs, Recheck
     if (n > q.cap) n = q.cap;
     for (unsigned int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
         uint4 it = q.items[e];
-        const DevJob& J = jobs[it.x & 0xFFFF];
-        unsigned w = it.x >> 16;
+        const DevJob& J = jobs[it.x & TASK_SLOT_MASK];
+        unsigned w = it.x >> RECHECK_WEIGHT_SHIFT;
         float4 pa = J.pts[0][it.y], pb = J.pts[1][it.z], pc = J.pts[2][it.w];
         int out[3];
         tp_exact<false>(ref_dist<false>(pa, pb), ref_dist<false>(pa, pc), ref_dist<false>(pb, pc), p, t, out);
@@ -721,21 +826,63 @@ __global__ void triangle_recheck_kernel(const DevJob* __restrict__ jobs, Recheck
 // Triangle parametrization, plain FP64: every triangle through the exact
 // reference arithmetic with each float operation done in FP64.
 
-template <bool GEOM> struct SideReal { typedef float type; };
-template <> struct SideReal<true> { typedef double type; };
+// JBJ shape parametrization (src/3pcf_C_version_triangle_parametrization_JBJ.cc
+// distance(), :116-229): one permutation, s = shortest, q = shortest/middle,
+// theta = (longest - middle)/shortest, in float, binned like the triangle
+// program; -1 if not counted (zero side, out of range, past the array).
+__device__ __forceinline__ int jbj_index(float dist0, float dist1, float dist2, const TriParams& p) {
+    float shortest, middle, longest;
+    if (dist0 > dist1) {
+        if (dist0 > dist2) {
+            longest = dist0;
+            if (dist1 > dist2) { middle = dist1; shortest = dist2; }
+            else { middle = dist2; shortest = dist1; }
+        } else {
+            middle = dist0;
+            if (dist1 > dist2) { longest = dist1; shortest = dist2; }
+            else { longest = dist2; shortest = dist1; }
+        }
+    } else {
+        if (dist1 > dist2) {
+            longest = dist1;
+            if (dist0 > dist2) { middle = dist0; shortest = dist2; }
+            else { middle = dist2; shortest = dist0; }
+        } else {
+            middle = dist1; longest = dist2; shortest = dist0;
+        }
+    }
+    if (dist0 == 0.f || dist1 == 0.f || dist2 == 0.f) return -1;
+    const float q = __fdiv_rn(shortest, middle);
+    const float th = __fdiv_rn(__fsub_rn(longest, middle), shortest);
+    const int i0 = ref_bin_tp<false>(shortest, p.s_lo, p.s_hi, p.S, p.nan_zero);
+    const int i1 = ref_bin_tp<false>(q, p.q_lo, p.q_hi, p.Q, p.nan_zero);
+    const int i2 = ref_bin_tp<false>(th, p.t_lo, p.t_hi, p.T, p.nan_zero);
+    if (i0 < 0 || i1 < 0 || i2 < 0) return -1;
+    const long long idx = (long long)p.Q * p.T * i0 + (long long)p.T * i1 + i2;
+    return idx < p.len ? (int)idx : -1;
+}
 
-template <bool GEOM>
-__device__ __forceinline__ typename SideReal<GEOM>::type side_fp64(float4 a, float4 b) {
-    if constexpr (GEOM) return geo_dist(a, b);
+// Arithmetic of the exact per-triangle kernel.
+enum ExactMode : int {
+    MODE_FP64 = 0,  // the reference's float arithmetic done in FP64 (identical histograms)
+    MODE_GEOM = 1,  // the FP64-geometry truth (tp_geom)
+    MODE_JBJ = 2    // the JBJ parametrization in the reference's float arithmetic
+};
+
+template <int MODE> struct SideReal { typedef float type; };
+template <> struct SideReal<MODE_GEOM> { typedef double type; };
+
+template <int MODE>
+__device__ __forceinline__ typename SideReal<MODE>::type side_fp64(float4 a, float4 b) {
+    if constexpr (MODE == MODE_GEOM) return geo_dist(a, b);
+    else if constexpr (MODE == MODE_JBJ) return ref_dist<false>(a, b);
     else return ref_dist<true>(a, b);
 }
 
-// GEOM false: the reference's float arithmetic done in FP64 (identical
-// histograms); true: the FP64-geometry truth (tp_geom).
-template <int PRED, bool GEOM>
+template <int PRED, int MODE>
 __device__ void triangle_task_fp64(const DevJob& J, uint4 task, const TriParams& p, const AcosTable& t,
                                    float4* P, int2* JK, int2* IJ, unsigned int* Hw) {
-    typedef typename SideReal<GEOM>::type R;  // at most 8 bytes: fits the int2 slots
+    typedef typename SideReal<MODE>::type R;  // at most 8 bytes: fits the int2 slots
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const TaskGeom g = task_geom(J, task);
     const bool diag_ij = task.x & TASK_DIAG_IJ, diag_jk = task.x & TASK_DIAG_JK;
@@ -744,7 +891,7 @@ __device__ void triangle_task_fp64(const DevJob& J, uint4 task, const TriParams&
     __syncthreads();
     for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
         int j = e / TILE, k = e % TILE;
-        if (j < g.nB && k < g.nC) jk[e] = side_fp64<GEOM>(P[TILE + j], P[2 * TILE + k]);
+        if (j < g.nB && k < g.nC) jk[e] = side_fp64<MODE>(P[TILE + j], P[2 * TILE + k]);
     }
     __syncthreads();
     R* row = reinterpret_cast<R*>(IJ + warp * TILE);
@@ -754,8 +901,8 @@ __device__ void triangle_task_fp64(const DevJob& J, uint4 task, const TriParams&
 #pragma unroll
         for (int r = 0; r < 2; r++) {
             int k = lane + 32 * r;
-            dik[r] = k < g.nC ? side_fp64<GEOM>(pi, P[2 * TILE + k]) : (R)0;
-            if (k < g.nB) row[k] = side_fp64<GEOM>(pi, P[TILE + k]);
+            dik[r] = k < g.nC ? side_fp64<MODE>(pi, P[2 * TILE + k]) : (R)0;
+            if (k < g.nB) row[k] = side_fp64<MODE>(pi, P[TILE + k]);
         }
         __syncwarp();
         const int ki = pkey(pi);
@@ -772,8 +919,13 @@ __device__ void triangle_task_fp64(const DevJob& J, uint4 task, const TriParams&
                 if (PRED == PRED_DDR) w = (unsigned)(kkey >= ki) + (unsigned)(kkey >= kj);
                 if (PRED == PRED_SAME || PRED == PRED_ONE) w = kj <= kkey ? 1u : 0u;
                 if (!w) continue;
+                if constexpr (MODE == MODE_JBJ) {
+                    const int b = jbj_index(dij, dik[r], jk[j * TILE + k], p);
+                    if (b >= 0) atomicAdd(Hw + b, w);
+                    continue;
+                }
                 int out[3];
-                if constexpr (GEOM) tp_geom(dij, dik[r], jk[j * TILE + k], p, out);
+                if constexpr (MODE == MODE_GEOM) tp_geom(dij, dik[r], jk[j * TILE + k], p, out);
                 else tp_exact<true>(dij, dik[r], jk[j * TILE + k], p, t, out);
                 for (int b = 0; b < 3; b++)
                     if (out[b] >= 0) atomicAdd(Hw + out[b], w);
@@ -783,7 +935,7 @@ __device__ void triangle_task_fp64(const DevJob& J, uint4 task, const TriParams&
     }
 }
 
-template <bool GEOM>
+template <int MODE>
 __global__ void __launch_bounds__(TRI_THREADS, 1)
 triangle_fp64_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ tasks, unsigned int ntasks,
                      unsigned int* task_counter, TriParams p, AcosTable t, int copies) {
@@ -814,11 +966,11 @@ triangle_fp64_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ 
         if (slot < 0) break;
         since++;
         const DevJob& J = jobs[slot];
-        switch ((task.x >> TASK_PRED_SHIFT) & 0xFF) {
-            case PRED_NONE: triangle_task_fp64<PRED_NONE, GEOM>(J, task, p, t, P, JK, IJ, Hw); break;
-            case PRED_DDR: triangle_task_fp64<PRED_DDR, GEOM>(J, task, p, t, P, JK, IJ, Hw); break;
-            case PRED_SAME: triangle_task_fp64<PRED_SAME, GEOM>(J, task, p, t, P, JK, IJ, Hw); break;
-            default: triangle_task_fp64<PRED_ONE, GEOM>(J, task, p, t, P, JK, IJ, Hw); break;
+        switch ((task.x >> TASK_PRED_SHIFT) & TASK_PRED_MASK) {
+            case PRED_NONE: triangle_task_fp64<PRED_NONE, MODE>(J, task, p, t, P, JK, IJ, Hw); break;
+            case PRED_DDR: triangle_task_fp64<PRED_DDR, MODE>(J, task, p, t, P, JK, IJ, Hw); break;
+            case PRED_SAME: triangle_task_fp64<PRED_SAME, MODE>(J, task, p, t, P, JK, IJ, Hw); break;
+            default: triangle_task_fp64<PRED_ONE, MODE>(J, task, p, t, P, JK, IJ, Hw); break;
         }
     }
 }
@@ -868,6 +1020,7 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
             if (k < g.nB) row[k] = side_code3<FP64>(ref_dist<FP64>(pi, P[TILE + k]), p, 1u);
         }
         __syncwarp();
+#pragma unroll 4
         for (int j = 0; j < g.nB; j++) {
             const uint32_t cij = row[j];
 #pragma unroll
@@ -983,7 +1136,7 @@ pair_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ tasks, un
         cur = slot;
         if (slot < 0) break;
         since++;
-        if (((task.x >> TASK_PRED_SHIFT) & 0xFF) == PRED_SAME) pair_task<FP64, PRED_SAME>(jobs[slot], task, p, P, Hw);
+        if (((task.x >> TASK_PRED_SHIFT) & TASK_PRED_MASK) == PRED_SAME) pair_task<FP64, PRED_SAME>(jobs[slot], task, p, P, Hw);
         else pair_task<FP64, PRED_NONE>(jobs[slot], task, p, P, Hw);
     }
 }
@@ -1035,9 +1188,11 @@ cudaError_t launch_triangle_recheck(const DevJob* jobs, RecheckQueue q, const Tr
 
 cudaError_t launch_triangle_fp64(const DevJob* jobs, const uint4* tasks, unsigned int ntasks,
                                  unsigned int* task_counter, const TriParams& p, AcosTable t, int grid, int copies,
-                                 bool geom, cudaStream_t st) {
+                                 int mode, cudaStream_t st) {
     size_t smem = triangle_smem_bytes(p.len, copies);
-    auto kern = geom ? triangle_fp64_kernel<true> : triangle_fp64_kernel<false>;
+    auto kern = mode == MODE_GEOM ? triangle_fp64_kernel<MODE_GEOM>
+                : mode == MODE_JBJ  ? triangle_fp64_kernel<MODE_JBJ>
+                                    : triangle_fp64_kernel<MODE_FP64>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     kern<<<grid, TRI_THREADS, smem, st>>>(jobs, tasks, ntasks, task_counter, p, t, copies);
@@ -1060,6 +1215,40 @@ cudaError_t launch_three_side(const DevJob* jobs, const uint4* tasks, unsigned i
         if (global) { TS_LAUNCH(false, true) } else { TS_LAUNCH(false, false) }
     }
 #undef TS_LAUNCH
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Catalog conversion (sample_data/gen_flat_MICE_data.py:53-99): comoving
+// distance from redshift by the quadratic fit r = p0 + p1 z + p2 z^2, then
+//   x = r sin(rad (90 - dec)) sin(rad ra), y = r sin(rad (90 - dec)) cos(rad ra),
+//   z = r cos(rad (90 - dec)),  rad = pi/180,
+// in double with the script's order of operations (no contraction), rounded
+// to the float coordinates the counting kernels use.
+__global__ void radecz_kernel(const double* __restrict__ ra, const double* __restrict__ dec,
+                              const double* __restrict__ zr, int64_t n, double p0, double p1, double p2,
+                              float* __restrict__ x, float* __restrict__ y, float* __restrict__ z) {
+    const double rad = 3.141592653589793 / 180.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double zz = zr[i];
+        const double r = __dadd_rn(__dadd_rn(p0, __dmul_rn(p1, zz)), __dmul_rn(__dmul_rn(p2, zz), zz));
+        const double polar = __dmul_rn(rad, __dsub_rn(90.0, dec[i]));
+        const double az = __dmul_rn(rad, ra[i]);
+        double sp, cp, sa, ca;
+        sincos(polar, &sp, &cp);
+        sincos(az, &sa, &ca);
+        const double rs = __dmul_rn(r, sp);
+        x[i] = __double2float_rn(__dmul_rn(rs, sa));
+        y[i] = __double2float_rn(__dmul_rn(rs, ca));
+        z[i] = __double2float_rn(__dmul_rn(r, cp));
+    }
+}
+
+cudaError_t launch_radecz_to_xyz(const double* ra, const double* dec, const double* redshift, int64_t n,
+                                 const double poly[3], float* x, float* y, float* z, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    int64_t blocks = std::min<int64_t>((n + 255) / 256, 152 * 16);
+    radecz_kernel<<<(unsigned)blocks, 256, 0, st>>>(ra, dec, redshift, n, poly[0], poly[1], poly[2], x, y, z);
     return cudaGetLastError();
 }
 

@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.environ.get("TPCF_LIB") or os.path.join(HERE, "_build", "libtpcf.so")
 BIN_DIR = os.path.join(HERE, "bin")
 
-THREE_SIDE, TRIANGLE, PAIR = 0, 1, 2
+THREE_SIDE, TRIANGLE, PAIR, TRIANGLE_JBJ = 0, 1, 2, 3
 LOOP_ALL, LOOP_SAME, LOOP_ONE = 0, 1, 2
 GUARDED_FP32, PLAIN_FP64, GEOMETRY_FP64 = 0, 1, 2
 NAN_INT_MIN, NAN_ZERO = 0, 1
@@ -24,7 +24,8 @@ ABI_SYMBOLS = [
     "tpcf_create", "tpcf_destroy", "tpcf_last_error", "tpcf_status_string", "tpcf_abi_version",
     "tpcf_catalog_create", "tpcf_catalog_release", "tpcf_resident_bytes", "tpcf_hist_len", "tpcf_count",
     "tpcf_count_batch", "tpcf_submit", "tpcf_wait", "tpcf_cancel", "tpcf_last_stats", "tpcf_loop_units",
-    "tpcf_read_catalog", "tpcf_pair_count_noalloc", "tpcf_wait_timed",
+    "tpcf_read_catalog", "tpcf_pair_count_noalloc", "tpcf_wait_timed", "tpcf_count_batch_into",
+    "tpcf_convert_radecz",
 ]
 
 
@@ -45,7 +46,11 @@ class Spec(ctypes.Structure):
 
 
 class Job(ctypes.Structure):
-    _fields_ = [("catalog", ctypes.c_uint64 * 3), ("begin", ctypes.c_int64 * 3), ("end", ctypes.c_int64 * 3)]
+    _fields_ = [("catalog", ctypes.c_uint64 * 3), ("begin", ctypes.c_int64 * 3), ("end", ctypes.c_int64 * 3),
+                ("flags", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+JOB_GLOBAL_INDEX = 1
 
 
 class Stats(ctypes.Structure):
@@ -53,7 +58,8 @@ class Stats(ctypes.Structure):
                 ("evaluated_units", ctypes.c_uint64), ("recheck_units", ctypes.c_uint64),
                 ("tasks", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64),
                 ("main_kernel_ms", ctypes.c_double), ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
-                ("binned_units", ctypes.c_uint64), ("graph_replays", ctypes.c_uint64)]
+                ("binned_units", ctypes.c_uint64), ("graph_replays", ctypes.c_uint64),
+                ("tuned_shapes", ctypes.c_uint64), ("hist_copies", ctypes.c_uint64), ("ctas_per_sm", ctypes.c_uint64)]
 
 
 _LIB = None
@@ -77,6 +83,8 @@ def lib():
         L.tpcf_hist_len.argtypes = [ctypes.POINTER(Spec), ctypes.POINTER(ctypes.c_int64)]
         L.tpcf_count.argtypes = [P, ctypes.POINTER(Spec), ctypes.POINTER(Job), P, ctypes.c_int64]
         L.tpcf_count_batch.argtypes = [P, P, P, ctypes.c_int32, P]
+        L.tpcf_count_batch_into.argtypes = [P, P, P, ctypes.c_int32, P, ctypes.c_int32, P]
+        L.tpcf_convert_radecz.argtypes = [P, P, P, P, ctypes.c_int64, P, P, P, P]
         L.tpcf_submit.argtypes = [P, ctypes.POINTER(Spec), ctypes.POINTER(Job), ctypes.POINTER(ctypes.c_uint64)]
         L.tpcf_wait.argtypes = [P, ctypes.c_uint64, P, ctypes.c_int64, ctypes.c_int64]
         L.tpcf_cancel.argtypes = [P, ctypes.c_uint64]
@@ -169,13 +177,16 @@ class Engine:
         self._check(lib().tpcf_catalog_release(self._ctx, handle), "catalog_release")
 
     @staticmethod
-    def job(handles, ranges=None):
+    def job(handles, ranges=None, global_index=False):
+        """ranges: per catalog [begin, end) (end -1: to the end).  global_index:
+        the mode predicates compare positions in the whole catalog."""
         j = Job()
         hs = list(handles) + [handles[-1]] * (3 - len(handles))
         for r in range(3):
             j.catalog[r] = hs[r]
             lo, hi = (0, -1) if ranges is None else (list(ranges) + [ranges[-1]] * 3)[r]
             j.begin[r], j.end[r] = lo, hi
+        j.flags = JOB_GLOBAL_INDEX if global_index else 0
         return j
 
     def count(self, spec, job):
@@ -192,6 +203,33 @@ class Engine:
         ptrs = (ctypes.c_void_p * n)(*[h.ctypes.data for h in hists])
         self._check(lib().tpcf_count_batch(self._ctx, sa, ja, n, ptrs), "count_batch")
         return hists
+
+    def count_batch_into(self, specs, jobs, out_index, n_out):
+        """Job i adds into output out_index[i]; returns the n_out summed histograms."""
+        n = len(specs)
+        sa = (Spec * n)(*specs)
+        ja = (Job * n)(*jobs)
+        oi = np.ascontiguousarray(np.asarray(out_index, dtype=np.int32))
+        lens = [0] * n_out
+        for s, o in zip(specs, oi):
+            if 0 <= int(o) < n_out:  # the engine rejects the rest
+                lens[int(o)] = hist_len(s)
+        hists = [np.zeros(max(1, ln), dtype=np.uint64) for ln in lens]
+        ptrs = (ctypes.c_void_p * n_out)(*[h.ctypes.data for h in hists])
+        self._check(lib().tpcf_count_batch_into(self._ctx, sa, ja, n, oi.ctypes.data, n_out, ptrs), "count_batch_into")
+        return [h[:ln] for h, ln in zip(hists, lens)]
+
+    def convert_radecz(self, ra, dec, redshift, poly=None):
+        """(n,3) float32 Cartesian coordinates of ra/dec (degrees) and redshift."""
+        cols = [np.ascontiguousarray(np.asarray(v, dtype=np.float64)) for v in (ra, dec, redshift)]
+        n = len(cols[0])
+        out = [np.zeros(n, dtype=np.float32) for _ in range(3)]
+        pc = None if poly is None else np.ascontiguousarray(np.asarray(poly, dtype=np.float64))
+        self._check(lib().tpcf_convert_radecz(self._ctx, cols[0].ctypes.data, cols[1].ctypes.data,
+                                              cols[2].ctypes.data, n, None if pc is None else pc.ctypes.data,
+                                              out[0].ctypes.data, out[1].ctypes.data, out[2].ctypes.data),
+                    "convert_radecz")
+        return np.stack(out, axis=1)
 
     def submit(self, spec, job):
         t = ctypes.c_uint64()

@@ -8,6 +8,7 @@ range(division)^3 as its own job and examples/sum_voxels.py adds the files.
 The loops of a chunk job compare LOCAL indices, so the sum over chunk jobs is
 what the reference's voxel workflow produces (not the one-file count).
 """
+import numpy as np
 
 
 def vox2gal(division, index, ngals):
@@ -43,3 +44,113 @@ def chunk_ranges(division, sizes):
                 out.append(((i, j, k), [vox2gal(division, i, sizes[0]), vox2gal(division, j, sizes[1]),
                                         vox2gal(division, k, sizes[2])]))
     return out
+
+
+# ---------------------------------------------------------------------------
+# Spatial voxels whose job sum equals the one-job count.
+#
+# The catalogs are ordered by voxel (a grid over their common bounding box);
+# a voxel is then a contiguous index range.  With voxel edges at least the
+# longest side a counted triangle can have, every counted triangle lies in
+# voxels that are pairwise neighbours (index difference <= 1 on each axis), so
+# canonical neighbour-voxel triples cover every counted triangle exactly once:
+#   DDD, RRR (unordered distinct triples of one catalog):
+#       V=V=V -> (V, V, V) same-array loop; V=V<W -> (W, V, V) one-array loop;
+#       U<V=V -> (U, V, V) one-array loop;  U<V<W -> (U, V, W) every triple
+#   DRR (every data point with every unordered random pair):
+#       (U, V, V) one-array loop; (U, V, W), V<W, every triple
+#   DDR (ordered data pairs (i, j), randoms k, k >= j in catalog order):
+#       (U, U, W) one-array loop; (U, V, W) and (V, U, W), U<V, one-array loop,
+#       all with catalog-wide loop indices.
+
+
+def voxel_order(points, lo, hi, grid):
+    """Stable order of the points by voxel id (x-major), the voxel id of each
+    sorted point, and the [start, end) of every voxel id."""
+    pts = np.asarray(points, dtype=np.float64)
+    g = np.asarray(grid)
+    cell = np.floor((pts - lo) / (hi - lo) * g).astype(np.int64)
+    cell = np.clip(cell, 0, g - 1)
+    vid = (cell[:, 0] * g[1] + cell[:, 1]) * g[2] + cell[:, 2]
+    order = np.argsort(vid, kind="stable")
+    svid = vid[order]
+    nvox = int(g.prod())
+    start = np.searchsorted(svid, np.arange(nvox), side="left")
+    end = np.searchsorted(svid, np.arange(nvox), side="right")
+    return order, start, end
+
+
+def _coords(v, grid):
+    return v // (grid[1] * grid[2]), (v // grid[2]) % grid[1], v % grid[2]
+
+
+def _adjacent(a, b, grid):
+    ca, cb = _coords(a, grid), _coords(b, grid)
+    return all(abs(x - y) <= 1 for x, y in zip(ca, cb))
+
+
+def _neighbours(v, grid, occupied):
+    x, y, z = _coords(v, grid)
+    out = []
+    for dx in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            for dz in (-1, 0, 1):
+                a, b, c = x + dx, y + dy, z + dz
+                if 0 <= a < grid[0] and 0 <= b < grid[1] and 0 <= c < grid[2]:
+                    w = (a * grid[1] + b) * grid[2] + c
+                    if occupied[w]:
+                        out.append(w)
+    return sorted(out)
+
+
+def spatial_jobs(kind, d_range, r_range, grid):
+    """Voxel jobs of one histogram kind ("DDD", "DDR", "DRR", "RRR").
+    d_range / r_range: (start, end) arrays per voxel id of the voxel-ordered
+    data and random catalogs.  Returns a list of (roles, ranges, loop,
+    global_index) with roles 'D'/'R' per position and loop one of
+    "same", "one", "all"."""
+    grid = tuple(int(x) for x in grid)
+    ds, de = d_range
+    rs, rend = r_range
+    occ_d = de > ds
+    occ_r = rend > rs
+    rng = lambda role, v: (int(ds[v]), int(de[v])) if role == "D" else (int(rs[v]), int(rend[v]))
+    jobs = []
+    if kind in ("DDD", "RRR"):
+        X = kind[0]
+        occ = occ_d if X == "D" else occ_r
+        for a in np.nonzero(occ)[0]:
+            nb = _neighbours(a, grid, occ)
+            jobs.append(((X, X, X), [rng(X, a)] * 3, "same", False))
+            for b in nb:
+                if b <= a:
+                    continue
+                jobs.append(((X, X, X), [rng(X, b), rng(X, a), rng(X, a)], "one", False))  # a=a<b
+                jobs.append(((X, X, X), [rng(X, a), rng(X, b), rng(X, b)], "one", False))  # a<b=b
+                for c in nb:
+                    if c > b and _adjacent(b, c, grid):
+                        jobs.append(((X, X, X), [rng(X, a), rng(X, b), rng(X, c)], "all", False))
+    elif kind == "DRR":
+        for u in np.nonzero(occ_d)[0]:
+            nb = _neighbours(u, grid, occ_r)
+            for v in nb:
+                jobs.append((("D", "R", "R"), [rng("D", u), rng("R", v), rng("R", v)], "one", False))
+                for w in nb:
+                    if w > v and _adjacent(v, w, grid):
+                        jobs.append((("D", "R", "R"), [rng("D", u), rng("R", v), rng("R", w)], "all", False))
+    elif kind == "DDR":
+        for u in np.nonzero(occ_d)[0]:
+            nbd = _neighbours(u, grid, occ_d)
+            nbr = _neighbours(u, grid, occ_r)
+            for w in nbr:
+                jobs.append((("D", "D", "R"), [rng("D", u), rng("D", u), rng("R", w)], "one", True))
+            for v in nbd:
+                if v <= u:
+                    continue
+                for w in nbr:
+                    if _adjacent(v, w, grid):
+                        jobs.append((("D", "D", "R"), [rng("D", u), rng("D", v), rng("R", w)], "one", True))
+                        jobs.append((("D", "D", "R"), [rng("D", v), rng("D", u), rng("R", w)], "one", True))
+    else:
+        raise ValueError(kind)
+    return jobs

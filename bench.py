@@ -507,61 +507,86 @@ def _jackknife_region(xyz):
 
 def run_voxel(args):
     """configs[2]: 100k clustered + 100k uniform points in a 20x20 degree
-    light-cone slab (depth 500-1500, density falling as r^-2), ordered by depth
-    as a light-cone catalog is.  One step = one launch of 4068 triangle jobs
-    of very uneven size: the reference's voxel decomposition with division 10
-    (every -x iiijjjkkk chunk triple of DDD/DDR/DRR/RRR: 4 x 1000 jobs), the
-    four full histograms, and the 16 jackknife subsamples (one 4x4 angular
-    cell left out) x 4 histograms."""
+    light-cone slab (depth 500-1500, density falling as r^-2).  The common
+    bounding box is cut into 10x10x10 voxels (~53x54x103, each edge above the
+    longest counted side, 40); the catalogs are ordered by voxel.  One step is
+    ONE launch of: the four full histograms (DDD, DDR, DRR, RRR), every
+    canonical neighbour-voxel job of each (summed on the device into one
+    histogram per kind, which must equal the full one exactly), and the 16
+    jackknife subsamples (one 4x4 angular cell left out) x 4 histograms."""
     import tpcf
     import synth
     import voxels
     d = synth.lightcone(100000, clustered=True, seed=11)
     r = synth.lightcone(100000, seed=12)
-    d, r = d[np.argsort(d[:, 2], kind="stable")], r[np.argsort(r[:, 2], kind="stable")]
+    lo = np.minimum(d.min(0), r.min(0)).astype(np.float64)
+    hi = np.maximum(d.max(0), r.max(0)).astype(np.float64)
+    hi = hi + 1e-6 * (hi - lo)
+    grid = (10, 10, 10)
+    od, sd, ed = voxels.voxel_order(d, lo, hi, grid)
+    orr, sr, er = voxels.voxel_order(r, lo, hi, grid)
+    d, r = d[od], r[orr]
     rd, rr = _jackknife_region(d), _jackknife_region(r)
     nan = tpcf.NAN_ZERO if platform.machine() == "aarch64" else tpcf.NAN_INT_MIN
     eng = tpcf.Engine(0)
     kinds = (("DDD", tpcf.LOOP_SAME), ("DDR", tpcf.LOOP_ONE), ("DRR", tpcf.LOOP_ONE), ("RRR", tpcf.LOOP_SAME))
-    spec = {lp: tpcf.make_spec(tpcf.TRIANGLE, lp, SPEC_AXES, nan_policy=nan) for _, lp in kinds}
-
-    def four(hd, hr, ranges=None):
-        cats = {"DDD": [hd, hd, hd], "DDR": [hd, hd, hr], "DRR": [hd, hr, hr], "RRR": [hr, hr, hr]}
-        return [(spec[lp], eng.job(cats[k], ranges)) for k, lp in kinds]
-
+    loops = {"same": tpcf.LOOP_SAME, "one": tpcf.LOOP_ONE, "all": tpcf.LOOP_ALL}
+    spec = {lp: tpcf.make_spec(tpcf.TRIANGLE, lp, SPEC_AXES, nan_policy=nan) for lp in loops.values()}
     hd, hr = eng.catalog(d), eng.catalog(r)
-    batch = four(hd, hr)
-    for reg in range(16):
-        batch += four(eng.catalog(d[rd != reg]), eng.catalog(r[rr != reg]))
-    nfull = len(batch)
-    cats_of = {"DDD": (hd, hd, hd), "DDR": (hd, hd, hr), "DRR": (hd, hr, hr), "RRR": (hr, hr, hr)}
-    for k, lp in kinds:
-        for _, rng in voxels.chunk_ranges(10, [len(d) if h == hd else len(r) for h in cats_of[k]]):
-            batch.append((spec[lp], eng.job(list(cats_of[k]), rng)))
-    specs, jobs = [b[0] for b in batch], [b[1] for b in batch]
-    for _ in range(args.warmup):
-        eng.count_batch(specs, jobs)
+    cat = {"D": hd, "R": hr}
+    specs, jobs, outs = [], [], []
+
+    def add(sp, jb, out):
+        specs.append(sp)
+        jobs.append(jb)
+        outs.append(out)
+
+    roles = {"DDD": "DDD", "DDR": "DDR", "DRR": "DRR", "RRR": "RRR"}
+    for o, (k, lp) in enumerate(kinds):  # outputs 0-3: full histograms
+        add(spec[lp], eng.job([cat[x] for x in roles[k]]), o)
+    nvox = 0
+    for o, (k, lp) in enumerate(kinds):  # outputs 4-7: voxel sums
+        for rl, rg, loop, glob in voxels.spatial_jobs(k, (sd, ed), (sr, er), grid):
+            add(spec[loops[loop]], eng.job([cat[x] for x in rl], rg, global_index=glob), 4 + o)
+            nvox += 1
+    for reg in range(16):  # outputs 8-71: jackknife subsamples
+        jd, jr = eng.catalog(d[rd != reg]), eng.catalog(r[rr != reg])
+        jc = {"D": jd, "R": jr}
+        for o, (k, lp) in enumerate(kinds):
+            add(spec[lp], eng.job([jc[x] for x in roles[k]]), 8 + 4 * reg + o)
+    n_out = 8 + 64
+    t0 = time.perf_counter()
+    hs = eng.count_batch_into(specs, jobs, outs, n_out)
+    first_s = time.perf_counter() - t0  # includes views and planning of every job
+    for _ in range(max(0, args.warmup - 1)):
+        eng.count_batch_into(specs, jobs, outs, n_out)
     ms, wall, st = [], [], None
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        hs = eng.count_batch(specs, jobs)
+        hs = eng.count_batch_into(specs, jobs, outs, n_out)
         wall.append((time.perf_counter() - t0) * 1e3)
         st = eng.stats()
         ms.append(st["kernel_ms"])
-    vox_sum = [sum(hs[nfull + 1000 * a: nfull + 1000 * (a + 1)]) for a in range(4)]
+    exact = [bool(np.array_equal(hs[o], hs[4 + o])) for o in range(4)]
     mean = statistics.mean(ms) / 1e3
     _line("triangles/s (bit-exact histos)", st["loop_units"] / mean, "triangles/s", args,
-          {"workload": "light cone 100k clustered + 100k uniform (depth-ordered), TP s8 q8 t16; one launch of "
-                       "4 full + 16x4 jackknife + 4x1000 voxel-chunk (division 10) jobs", "jobs": len(jobs),
+          {"workload": "light cone 100k clustered + 100k uniform, TP s8 q8 t16; one launch of 4 full histograms "
+                       "+ %d canonical neighbour-voxel jobs (10x10x10 voxels, summed per kind on the device) "
+                       "+ 16x4 jackknife jobs" % nvox, "jobs": len(jobs),
+           "voxel_jobs": nvox, "occupied_voxels": [int((ed > sd).sum()), int((er > sr).sum())],
+           "voxel_sum_equals_full": exact, "counted_full": [int(hs[o].sum()) for o in range(4)],
            "triangles_per_step": st["loop_units"], "evaluated_triangles_per_step": st["evaluated_units"],
            "binned_triangles_per_step": st["binned_units"], "tasks": st["tasks"],
-           "voxel_sums_counted": [int(v.sum()) for v in vox_sum],
-           "full_counted": [int(h.sum()) for h in hs[:4]]},
+           "first_call_s": first_s, "launch_shape": {"hist_copies": st["hist_copies"], "ctas_per_sm": st["ctas_per_sm"]}},
           ms_per_step=mean * 1e3, wall_ms_per_step=statistics.mean(wall), p50_ms=statistics.median(ms),
-          p99_ms=float(np.percentile(ms, 99)), gpu_launches=st["kernel_launches"],
+          p99_ms=float(np.percentile(ms, 99)), gpu_launches=st["kernel_launches"] * args.steps,
+          graph_replays=st["graph_replays"],
           roofline={"bound": "issue", "achieved": W_TP * st["binned_units"] / (st["main_kernel_ms"] / 1e3) / 1e12,
                     "unit": "Tinst/s", "per_unit": "58 lane-instructions per binned triangle"})
     eng.close()
+    if not all(exact):
+        print("voxel sums differ from the full histograms", exact, file=sys.stderr)
+        return 1
     return 0
 
 

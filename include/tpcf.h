@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define TPCF_ABI_VERSION 1
+#define TPCF_ABI_VERSION 2
 
 typedef int32_t tpcf_status;
 enum {
@@ -49,7 +49,13 @@ enum {
 enum {
     TPCF_THREE_SIDE = 0, /* src/3pcf_C_version.cc: sides d01,d02,d12 binned unsorted */
     TPCF_TRIANGLE = 1,   /* src/3pcf_C_version_triangle_parametrization.cc: (s,q,theta) */
-    TPCF_PAIR = 2        /* src/2pcf_C_version.cc: pair separation */
+    TPCF_PAIR = 2,       /* src/2pcf_C_version.cc: pair separation */
+    TPCF_TRIANGLE_JBJ = 3 /* src/3pcf_C_version_triangle_parametrization_JBJ.cc:116-229:
+                             one count per triangle at (s, q, theta) = (shortest,
+                             shortest/middle, (longest-middle)/shortest); with
+                             TPCF_OVERFLOW_COMPAT bin 0 also gets the reference's 2
+                             counts per visited triangle (:455, :511-518), with
+                             TPCF_OVERFLOW_CLEAN it does not */
 };
 
 /* Loop nest.  The reference decides it from argv string identity and keeps it
@@ -103,7 +109,7 @@ typedef struct {
     int32_t loop;       /* TPCF_LOOP_* */
     int32_t precision;  /* TPCF_GUARDED_FP32 / TPCF_PLAIN_FP64 */
     int32_t nan_policy; /* TPCF_NAN_* (triangle only) */
-    int32_t overflow;   /* TPCF_OVERFLOW_* (three-side only) */
+    int32_t overflow;   /* TPCF_OVERFLOW_* (three-side and JBJ) */
     int32_t prune;      /* 1: skip point tiles that provably cannot contribute
                            (exact); 0: visit every tile of the loop nest */
     tpcf_axis axis[3];  /* three-side: axis[0]; triangle: s, q, theta; pair: axis[0] */
@@ -112,10 +118,21 @@ typedef struct {
 /* One histogram request: 3 catalog ranges (2 for pairs).  The loop indices of
  * the reference are positions inside [begin, end) of each range, which is how
  * the reference's -X/-x index chunks (vox2gal, :52-80) behave. */
+/* Job flags. */
+enum {
+    /* The loop indices the mode predicates compare (j >= i, k >= j) are
+     * positions in the whole catalog instead of positions inside [begin, end).
+     * The reference's -x chunk jobs use positions inside the chunk (default);
+     * spatial sub-jobs whose sum must equal the one-job count use this flag. */
+    TPCF_JOB_GLOBAL_INDEX = 1
+};
+
 typedef struct {
     uint64_t catalog[3];
     int64_t begin[3];
     int64_t end[3];     /* -1: to the end of the catalog */
+    uint32_t flags;     /* TPCF_JOB_* */
+    uint32_t reserved;  /* 0 */
 } tpcf_job;
 
 typedef struct {
@@ -132,6 +149,10 @@ typedef struct {
     uint64_t binned_units;       /* triangles (pairs) that reached the full binning arithmetic */
     uint64_t graph_replays;      /* launches replayed from a captured CUDA graph (a repeated
                                     batch); the rest were issued one by one */
+    uint64_t tuned_shapes;       /* launch shapes the autotuner timed in this call (0: none) */
+    uint64_t hist_copies;        /* launch shape of the last group: histogram copies per CTA
+                                    in shared memory (0: global histogram) ... */
+    uint64_t ctas_per_sm;        /* ... and resident CTAs per SM */
 } tpcf_stats;
 
 typedef struct tpcf_ctx tpcf_ctx;
@@ -172,6 +193,15 @@ tpcf_status tpcf_count(tpcf_ctx* ctx, const tpcf_spec* spec, const tpcf_job* job
 tpcf_status tpcf_count_batch(tpcf_ctx* ctx, const tpcf_spec* specs, const tpcf_job* jobs, int32_t n,
                              uint64_t* const* hists);
 
+/* Batched count with summed outputs: job i adds its counts into
+ * hists[out_index[i]] (0 <= out_index[i] < n_out; every job of one output has
+ * the same histogram length), all in one persistent launch per binning.  This
+ * is examples/sum_voxels.py done on the device: a spatial or index-chunk
+ * decomposition of one count into many jobs (up to 4,194,303 per binning)
+ * returns the summed histogram.  No counterpart in the reference. */
+tpcf_status tpcf_count_batch_into(tpcf_ctx* ctx, const tpcf_spec* specs, const tpcf_job* jobs, int32_t n,
+                                  const int32_t* out_index, int32_t n_out, uint64_t* const* hists);
+
 /* Asynchronous submit / wait (serving).  Serving workers (TPCF_SERVING_LANES,
  * default 2), each with its own stream, take the oldest pending job together
  * with every pending job of the same binning, while the device bytes of all
@@ -192,6 +222,19 @@ tpcf_status tpcf_last_stats(tpcf_ctx* ctx, tpcf_stats* stats);
 /* Number of reference loop iterations (triangles or pairs) of a job, the
  * reference's numcalc / fake_tot counter (:520, src/3pcf_C_version.cc:429). */
 tpcf_status tpcf_loop_units(tpcf_ctx* ctx, const tpcf_spec* spec, const tpcf_job* job, uint64_t* units);
+
+/* ---- catalog conversion ---------------------------------------------------- */
+/* ra/dec in degrees and redshift -> Cartesian comoving coordinates (Mpc), on the
+ * device, as sample_data/gen_flat_MICE_data.py:53-99 computes them: r = p0 +
+ * p1 z + p2 z^2 with poly = {p0, p1, p2} (NULL: the script's MICE fit
+ * {-1.07199554, 3013.13296, -638.827998}), x = r sin((90-dec) deg) sin(ra deg),
+ * y = r sin((90-dec) deg) cos(ra deg), z = r cos((90-dec) deg), in double,
+ * rounded to float.  Host arrays in and out.  The double sin/cos are the GPU's
+ * (within 2 ulp of a correctly rounded one), so a coordinate can differ from
+ * the script's by one float ulp where the double result sits at a float
+ * rounding boundary. */
+tpcf_status tpcf_convert_radecz(tpcf_ctx* ctx, const double* ra, const double* dec, const double* redshift,
+                                int64_t n, const double* poly, float* x, float* y, float* z);
 
 /* ---- pair counts without device allocation -------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device

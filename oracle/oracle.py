@@ -28,6 +28,8 @@ def lib():
         L.oracle_triangle.restype = ctypes.c_ulonglong
         L.oracle_triangle.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                       ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
+        L.oracle_triangle_jbj.restype = ctypes.c_ulonglong
+        L.oracle_triangle_jbj.argtypes = L.oracle_triangle.argtypes
         L.oracle_triangle_geom64.restype = ctypes.c_ulonglong
         L.oracle_triangle_geom64.argtypes = L.oracle_triangle.argtypes
         L.oracle_triangle_one.restype = None
@@ -80,6 +82,18 @@ def triangle(cats, which, spec, nan_zero=False, nthreads=None):
     hist = np.zeros(int(nb.prod()), dtype=np.uint64)
     n = lib().oracle_triangle(arr, int(which), lohi.ctypes.data, nb.ctypes.data, int(nan_zero),
                               hist.ctypes.data, nthreads or _threads())
+    return hist, n
+
+
+def triangle_jbj(cats, which, spec, compat=True, nthreads=None):
+    """JBJ shape histogram (s, s/m, (l-m)/s) with the reference's loop nest;
+    compat adds the reference's 2 counts per visited triangle to bin 0."""
+    arr, keep = _cats(cats)
+    lohi = np.array([spec[0][1], spec[0][2], spec[1][1], spec[1][2], spec[2][1], spec[2][2]], dtype=np.float32)
+    nb = np.array([spec[0][0], spec[1][0], spec[2][0]], dtype=np.int32)
+    hist = np.zeros(int(nb.prod()), dtype=np.uint64)
+    n = lib().oracle_triangle_jbj(arr, int(which), lohi.ctypes.data, nb.ctypes.data, int(compat),
+                                  hist.ctypes.data, nthreads or _threads())
     return hist, n
 
 

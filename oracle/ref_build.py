@@ -52,6 +52,9 @@ VARIANTS = {
     "tp_sandbox_wide": ("tp", dict(S=(60, "0.", "120."), Q=(16, "0.9", "4.1"), T=(25, "0.", "1."))),
     "tp_s8_q8_t16": ("tp", dict(S=(8, "2.0", "10.0"), Q=(8, "1.0", "3.0"), T=(16, "0.", "1."))),
     "tp_s6_q5_t7_zero": ("tp", dict(S=(6, "0.0", "15.0"), Q=(5, "1.0", "2.5"), T=(7, "0.1", "0.9"))),
+    # JBJ shape parametrization (s, s/m, (l-m)/s): S, Q, THETA (nbins, lo, hi)
+    "jbj_default": ("jbj", None),
+    "jbj_s10_q8_t10": ("jbj", dict(S=(10, "1.0", "11.0"), Q=(8, "0.2", "1.0"), T=(10, "0.", "1."))),
     # 2pcf: S (nbins, lo, hi)
     "2pcf_default": ("2pcf", None),
     "2pcf_s40_1_21": ("2pcf", dict(S=(40, "1.0", "21.0"))),
@@ -61,6 +64,7 @@ SOURCES = {
     "3side": "3pcf_C_version.cc",
     "tp": "3pcf_C_version_triangle_parametrization.cc",
     "2pcf": "2pcf_C_version.cc",
+    "jbj": "3pcf_C_version_triangle_parametrization_JBJ.cc",
 }
 
 
@@ -82,7 +86,7 @@ def configure(program, params, text):
             text = _sub1(r"^(\s*)float hist_max = sqrt\(3\*24\*24\);", r"\g<1>float hist_max = %s;" % params["hi"], text, "hist_max")
         text = _sub1(r"malloc\(size_hist_bytes\)", "malloc(8*(size_t)size_hist_bytes)", text, "hist malloc")
         return text
-    if program == "tp":
+    if program in ("tp", "jbj"):
         if params is not None:
             for ax, key in (("S", "S"), ("Q", "Q"), ("THETA", "T")):
                 n, lo, hi = params[key]
@@ -153,6 +157,7 @@ _DEFAULTS = {
     "3side": dict(nbins=64, lo="0", hi=None),  # hist_max = (float)sqrt(3*24*24), src/3pcf_C_version.cc:172
     "tp": dict(S=(50, "2.0", "12.0"), Q=(16, "0.9", "4.1"), T=(32, "0.", "1.")),  # :31-42
     "2pcf": dict(S=(700, "0.0", "70.0")),  # src/2pcf_C_version.cc:14-16
+    "jbj": dict(S=(50, "2.0", "12.0"), Q=(16, "0.9", "4.1"), T=(32, "0.", "1.")),  # _JBJ.cc:31-42
 }
 
 

@@ -350,6 +350,107 @@ unsigned long long oracle_triangle(const ocat_t* cats, int which, const float* l
 }
 
 /* ------------------------------------------------------------------------- */
+/* JBJ shape parametrization: src/3pcf_C_version_triangle_parametrization_JBJ.cc
+ * distance(), :116-229: one permutation only, s = shortest, q = shortest /
+ * middle, theta = (longest - middle) / shortest, binned by the same
+ * distance_to_bin (:84-113); zero sides drop the triangle.  main() passes a
+ * three-entry bins array initialised to {0, 0, 0} (:455) of which distance()
+ * only writes entry 0, so every visited triangle also adds 2 to hist[0]
+ * (:511-518); compat = 1 reproduces that, 0 leaves it out. */
+
+static inline int jbj_core(float dist0, float dist1, float dist2, const tp_spec_t* sp) {
+    float shortest, middle, longest;
+    if (dist0 > dist1) {
+        if (dist0 > dist2) {
+            longest = dist0;
+            if (dist1 > dist2) { middle = dist1; shortest = dist2; }
+            else { middle = dist2; shortest = dist1; }
+        } else {
+            middle = dist0;
+            if (dist1 > dist2) { longest = dist1; shortest = dist2; }
+            else { longest = dist2; shortest = dist1; }
+        }
+    } else {
+        if (dist1 > dist2) {
+            longest = dist1;
+            if (dist0 > dist2) { middle = dist0; shortest = dist2; }
+            else { middle = dist2; shortest = dist0; }
+        } else {
+            middle = dist1; longest = dist2; shortest = dist0;
+        }
+    }
+    float s = shortest;
+    float q = shortest / middle;
+    float theta = (longest - middle) / shortest;
+    int i2 = tp_bin(theta, sp->lo[2], sp->hi[2], sp->nb[2], sp->nan_zero);
+    int i0 = tp_bin(s, sp->lo[0], sp->hi[0], sp->nb[0], sp->nan_zero);
+    int i1 = tp_bin(q, sp->lo[1], sp->hi[1], sp->nb[1], sp->nan_zero);
+    int tot = (i0 < 0 || i1 < 0 || i2 < 0) ? -999 : sp->nb[1] * sp->nb[2] * i0 + sp->nb[2] * i1 + i2;
+    if (dist0 == 0 || dist1 == 0 || dist2 == 0) tot = -999;
+    return tot;
+}
+
+static void* jbj_worker(void* arg) {
+    tp_worker_t* w = (tp_worker_t*)arg;
+    tp_task_t* t = w->shared;
+    const ocat_t* c = t->c;
+    const long size = (long)t->sp.nb[0] * t->sp.nb[1] * t->sp.nb[2];
+    for (;;) {
+        long i = grab(&t->i_next, t->mu, 1);
+        if (i >= c[0].n) break;
+        long jmin = (t->which == 0) ? i : 0;
+        for (long j = jmin; j < c[1].n; j++) {
+            float d01 = ref_dist(c[0].x[i], c[0].y[i], c[0].z[i], c[1].x[j], c[1].y[j], c[1].z[j]);
+            for (long k = j; k < c[2].n; k++) {
+                float d02 = ref_dist(c[0].x[i], c[0].y[i], c[0].z[i], c[2].x[k], c[2].y[k], c[2].z[k]);
+                float d12 = ref_dist(c[1].x[j], c[1].y[j], c[1].z[j], c[2].x[k], c[2].y[k], c[2].z[k]);
+                int b = jbj_core(d01, d02, d12, &t->sp);
+                w->ncalc++;
+                if (b >= 0 && b < size) w->hist[b]++;
+            }
+        }
+    }
+    return NULL;
+}
+
+unsigned long long oracle_triangle_jbj(const ocat_t* cats, int which, const float* lohi, const int* nb,
+                                       int compat, unsigned long long* hist, int nthreads) {
+    const long size = (long)nb[0] * nb[1] * nb[2];
+    memset(hist, 0, sizeof(unsigned long long) * size);
+    if (nthreads < 1) nthreads = 1;
+    pthread_mutex_t mu = PTHREAD_MUTEX_INITIALIZER;
+    tp_task_t task;
+    task.c = cats;
+    for (int a = 0; a < 3; a++) {
+        task.sp.lo[a] = lohi[2 * a];
+        task.sp.hi[a] = lohi[2 * a + 1];
+        task.sp.nb[a] = nb[a];
+    }
+    task.sp.nan_zero = 0;
+    task.which = which ? 1 : 0;
+    task.i_next = 0;
+    task.mu = &mu;
+    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * nthreads);
+    tp_worker_t* ws = (tp_worker_t*)calloc(nthreads, sizeof(tp_worker_t));
+    for (int t = 0; t < nthreads; t++) {
+        ws[t].shared = &task;
+        ws[t].hist = (unsigned long long*)calloc(size, sizeof(unsigned long long));
+        pthread_create(&th[t], NULL, jbj_worker, &ws[t]);
+    }
+    unsigned long long ncalc = 0;
+    for (int t = 0; t < nthreads; t++) {
+        pthread_join(th[t], NULL);
+        for (long b = 0; b < size; b++) hist[b] += ws[t].hist[b];
+        ncalc += ws[t].ncalc;
+        free(ws[t].hist);
+    }
+    free(ws);
+    free(th);
+    if (compat && size > 0) hist[0] += 2 * ncalc;
+    return ncalc;
+}
+
+/* ------------------------------------------------------------------------- */
 /* FP64 geometry: the triangle formulas of :116-240 evaluated in double from
  * the float coordinates, acos in double.  Not the reference's counts; the FP64
  * truth that the error of the derived correlation function is measured

@@ -113,6 +113,14 @@ def cases():
           ("tp_s6_q5_t7_zero_lattice", "tp_s6_q5_t7_zero", ["c_lattice"] * 3, []),
           ("tp_s6_q5_t7_zero_DDR", "tp_s6_q5_t7_zero", ["c_lattice", "c_lattice", "c_third"], []),
           ("tp_sandbox_lattice", "tp_sandbox", ["c_lattice"] * 3, [])]
+    for var in ("jbj_s10_q8_t10", "jbj_default"):
+        c += [(var + "_DDD", var, ["c_blobs"] * 3, []),
+              (var + "_DDR", var, ["c_blobs", "c_blobs", "c_unif"], []),
+              (var + "_DRR", var, ["c_blobs", "c_unif", "c_unif"], []),
+              (var + "_RRR", var, ["c_unif"] * 3, [])]
+    c += [("jbj_s10_q8_t10_lattice", "jbj_s10_q8_t10", ["c_lattice"] * 3, []),
+          ("jbj_s10_q8_t10_vox2_DDR", "jbj_s10_q8_t10", ["c_blobs", "c_blobs", "c_unif"], ["-X", "2", "-x", "001000001"]),
+          ("jbj_s10_q8_t10_three", "jbj_s10_q8_t10", ["c_blobs", "c_unif", "c_third"], [])]
     for var in ("2pcf_default", "2pcf_s40_1_21"):
         c += [(var + "_DD", var, ["c_pairs_d"] * 2, []),
               (var + "_DR", var, ["c_pairs_d", "c_pairs_r"], []),

@@ -123,7 +123,7 @@ def ref_binning(variant):
     if program == "3side":
         hi = float(np.float32(math.sqrt(1728.0))) if p["hi"] is None else float(p["hi"])
         return program, (int(p["nbins"]), float(p["lo"]), hi)
-    if program == "tp":
+    if program in ("tp", "jbj"):
         return program, tuple((int(n), float(lo), float(hi)) for n, lo, hi in (p["S"], p["Q"], p["T"]))
     n, lo, hi = p["S"]
     return program, (int(n), float(lo), float(hi))

@@ -29,7 +29,7 @@ def test_library_exports_every_declared_symbol():
     L = ctypes.CDLL(tpcf.LIB_PATH)
     for name in declared_symbols():
         assert hasattr(L, name), name
-    assert L.tpcf_abi_version() == 1
+    assert L.tpcf_abi_version() == 2
 
 
 def _has_gpu():
@@ -125,3 +125,24 @@ def test_x86_acos_fixture_matches_this_host():
     assert np.array_equal(keys, fk)
     assert np.array_equal(dirs > 0, fu)
     assert np.all(np.abs(dirs) == 1)
+
+
+def test_sum_voxels_tool_matches_reference_script(tmp_path):
+    """tpcf_sum_voxels on the reference's own eight DDD_voxel2 chunk files
+    against the restatement of examples/sum_voxels.py, byte for byte."""
+    import glob
+    import subprocess
+    import refformat as rf
+    import sum_voxels_ref
+    exe = os.path.join(rf.ROOT, "3pcf_gb300", "bin", "tpcf_sum_voxels")
+    files = []
+    for src in sorted(glob.glob(os.path.join(rf.GOLDEN, "sandbox", "DDD_voxel2_*_1k.dat.gz"))):
+        dst = str(tmp_path / os.path.basename(src)[:-3])
+        rf.gunzip_to(src, dst)
+        files.append(dst)
+    assert len(files) == 8
+    got = subprocess.run([exe] + files, capture_output=True, check=True).stdout.decode()
+    assert got == sum_voxels_ref.sum_voxels(files)
+    assert got.endswith("\n\n")
+    bad = subprocess.run([exe, files[0], str(tmp_path / "missing.dat")], capture_output=True)
+    assert bad.returncode == 1

@@ -89,6 +89,9 @@ def test_engine_matches_compiled_reference(eng_x86, name, precision):
         got = rf.format_three_side(eng.count(s, job), n)
     elif program == "tp":
         got = rf.format_triangle(eng.count(_tp_spec(spec, _loop_of(which), precision), job), ngal, spec)
+    elif program == "jbj":
+        s = tpcf.make_spec(tpcf.TRIANGLE_JBJ, _loop_of(which), spec, precision=precision)
+        got = rf.format_triangle(eng.count(s, job), ngal, spec)
     else:
         n, lo, hi = spec
         s = tpcf.make_spec(tpcf.PAIR, _loop_of(which), [spec], precision=precision)
@@ -324,14 +327,15 @@ def test_duplicate_points_zero_sides(eng):
 
 
 @pytest.mark.parametrize("name", ["tp_s8_q8_t16_DDR", "tp_s8_q8_t16_vox3_DDD", "tp_default_DRR",
-                                  "3side_n16_0_40_DDR", "2pcf_default_DD", "2pcf_default_vox2"])
+                                  "3side_n16_0_40_DDR", "2pcf_default_DD", "2pcf_default_vox2",
+                                  "jbj_default_DDD", "jbj_s10_q8_t10_vox2_DDR"])
 def test_cli_byte_exact(tmp_path, name):
     case = CASES[name]
     var = case["variant"]
-    prog = {"3side": "tpcf_3side", "tp": "tpcf_tp", "2pcf": "tpcf_2pcf"}[rf.ref_binning(var)[0]]
+    prog = {"3side": "tpcf_3side", "tp": "tpcf_tp", "2pcf": "tpcf_2pcf", "jbj": "tpcf_jbj"}[rf.ref_binning(var)[0]]
     program, spec = rf.ref_binning(var)
     extra = []
-    if program == "tp":
+    if program in ("tp", "jbj"):
         extra = ["--s-axis", "%d,%r,%r" % spec[0], "--q-axis", "%d,%r,%r" % spec[1],
                  "--theta-axis", "%d,%r,%r" % spec[2], "--nan-policy", "int_min"]
     elif program == "3side":
@@ -350,3 +354,24 @@ def test_acos_exception_table(eng):
     mism, n = eng.acos_selfcheck()
     assert mism == 0
     assert 1_000_000 < n < 20_000_000
+
+
+@pytest.mark.parametrize("spec", [((50, 2.0, 12.0), (16, 0.9, 4.1), (32, 0.0, 1.0)),
+                                  ((10, 1.0, 11.0), (8, 0.2, 1.0), (10, 0.0, 1.0))])
+def test_jbj_vs_oracle_both_overflow_modes(eng, spec):
+    """JBJ parametrization: compat (the reference's two extra bin-0 counts per
+    visited triangle) and clean, every loop nest, pruned and unpruned."""
+    d, r = _random_case(404)
+    hd, hr = eng.catalog(d), eng.catalog(r)
+    combos = [([hd, hd, hd], [d, d, d], 0), ([hd, hd, hr], [d, d, r], 1), ([hd, hr, hr], [d, r, r], 1),
+              ([hr, hr, hr], [r, r, r], 0)]
+    for overflow in (tpcf.OVERFLOW_COMPAT, tpcf.OVERFLOW_CLEAN):
+        for prune in (True, False):
+            specs = [tpcf.make_spec(tpcf.TRIANGLE_JBJ, _loop_of(w), spec, overflow=overflow, prune=prune)
+                     for _, _, w in combos]
+            hists = eng.count_batch(specs, [eng.job(h) for h, _, _ in combos])
+            for (h, cats, w), got in zip(combos, hists):
+                want, n = oracle.triangle_jbj(cats, w, spec, compat=overflow == tpcf.OVERFLOW_COMPAT)
+                assert np.array_equal(got, want), (overflow, prune, w)
+    eng.release(hd)
+    eng.release(hr)

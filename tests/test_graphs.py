@@ -20,6 +20,7 @@ def _batch(eng, hd, hr):
 
 
 def test_graph_replay_matches_direct_launches(monkeypatch):
+    monkeypatch.setenv("TPCF_AUTOTUNE", "0")  # the autotuner times shapes without graphs
     d = synth.blobs(1500, n_blobs=4, sigma=5.0, box=60.0, seed=31)
     r = synth.uniform(1400, box=60.0, seed=32)
     with tpcf.Engine(0) as eng:
@@ -44,3 +45,29 @@ def test_graph_replay_matches_direct_launches(monkeypatch):
         assert np.array_equal(pair, eng.count(tpcf.make_spec(tpcf.PAIR, tpcf.LOOP_SAME, [(700, 0.0, 70.0)]),
                                               eng.job([hd, hd])))
         assert sum(int(a.sum()) for a in first) > 0
+
+
+@pytest.mark.parametrize("kind", ["triangle", "three_side", "pair"])
+def test_autotuner_times_every_shape_once_and_stays_exact(kind):
+    """A batch seen for the second time is counted once per candidate launch
+    shape (every count exact); later calls use the fastest shape."""
+    d = synth.blobs(1200, n_blobs=4, sigma=5.0, box=60.0, seed=41)
+    with tpcf.Engine(0) as eng:
+        h = eng.catalog(d)
+        if kind == "triangle":
+            spec, job = tpcf.make_spec(tpcf.TRIANGLE, tpcf.LOOP_SAME, TP), eng.job([h, h, h])
+        elif kind == "three_side":
+            spec, job = tpcf.make_spec(tpcf.THREE_SIDE, tpcf.LOOP_ALL, [(16, 0.0, 40.0)]), eng.job([h, h, h])
+        else:
+            spec, job = tpcf.make_spec(tpcf.PAIR, tpcf.LOOP_SAME, [(700, 0.0, 70.0)]), eng.job([h, h])
+        first = eng.count(spec, job)
+        assert eng.stats()["tuned_shapes"] == 0
+        second = eng.count(spec, job)
+        n_shapes = eng.stats()["tuned_shapes"]
+        assert n_shapes >= 2
+        third = eng.count(spec, job)
+        st = eng.stats()
+        assert st["tuned_shapes"] == 0
+        assert st["ctas_per_sm"] >= 1
+        assert np.array_equal(first, second) and np.array_equal(first, third)
+        assert first.sum() > 0

@@ -74,6 +74,9 @@ def test_oracle_matches_compiled_reference(name):
     elif program == "tp":
         hist, _ = oracle.triangle(cats, which, spec, nan_zero=False)
         got = rf.format_triangle(hist, ngal, spec)
+    elif program == "jbj":
+        hist, _ = oracle.triangle_jbj(cats, which, spec, compat=True)
+        got = rf.format_triangle(hist, ngal, spec)
     else:
         n, lo, hi = spec
         hist, _ = oracle.pair(cats, which, lo, hi, n)

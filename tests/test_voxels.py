@@ -1,0 +1,113 @@
+"""Spatial voxel decomposition: the sum of the canonical neighbour-voxel jobs
+(tpcf_count_batch_into, catalog-wide loop indices for DDR) equals the one-job
+count of every histogram, exactly; plus the summed-output batch semantics."""
+import numpy as np
+import pytest
+
+import synth
+import tpcf
+import voxels
+
+TP = [(8, 2.0, 10.0), (8, 1.0, 3.0), (16, 0.0, 1.0)]  # longest counted side < 40
+LOOP = {"same": tpcf.LOOP_SAME, "one": tpcf.LOOP_ONE, "all": tpcf.LOOP_ALL}
+
+
+def test_spatial_jobs_cover_each_canonical_triple_once():
+    """CPU check of the enumeration: on a 3x3x3 grid with every voxel
+    occupied, DDD jobs cover each unordered neighbour triple of voxels once."""
+    grid = (3, 3, 3)
+    n = 27
+    occ_range = (np.arange(n) * 10, np.arange(n) * 10 + 10)
+    jobs = voxels.spatial_jobs("DDD", occ_range, occ_range, grid)
+    seen = set()
+    for roles, ranges, loop, glob in jobs:
+        vs = tuple(sorted(r[0] // 10 for r in ranges))
+        assert vs not in seen
+        seen.add(vs)
+    want = set()
+    for a in range(n):
+        for b in range(a, n):
+            for c in range(b, n):
+                if voxels._adjacent(a, b, grid) and voxels._adjacent(a, c, grid) and voxels._adjacent(b, c, grid):
+                    want.add((a, b, c))
+    assert seen == want
+
+
+def _setup(seed):
+    d = synth.blobs(2500, n_blobs=12, sigma=5.0, box=130.0, seed=seed)
+    r = synth.uniform(2000, box=130.0, seed=seed + 1)
+    lo = np.minimum(d.min(0), r.min(0)).astype(np.float64) - 1e-3
+    hi = np.maximum(d.max(0), r.max(0)).astype(np.float64) + 1e-3
+    assert ((hi - lo) / 3 >= 40.0).all()
+    od, sd, ed = voxels.voxel_order(d, lo, hi, (3, 3, 3))
+    orr, sr, er = voxels.voxel_order(r, lo, hi, (3, 3, 3))
+    return d[od], r[orr], (sd, ed), (sr, er)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed", [5])
+def test_voxel_sum_equals_full_count(seed):
+    d, r, dr, rr = _setup(seed)
+    with tpcf.Engine(0) as eng:
+        hd, hr = eng.catalog(d), eng.catalog(r)
+        cat = {"D": hd, "R": hr}
+        full = {"DDD": ([hd, hd, hd], tpcf.LOOP_SAME), "DDR": ([hd, hd, hr], tpcf.LOOP_ONE),
+                "DRR": ([hd, hr, hr], tpcf.LOOP_ONE), "RRR": ([hr, hr, hr], tpcf.LOOP_SAME)}
+        specs, jobs, outs = [], [], []
+        for o, k in enumerate(full):
+            hs, loop = full[k]
+            specs.append(tpcf.make_spec(tpcf.TRIANGLE, loop, TP))
+            jobs.append(eng.job(hs))
+            outs.append(o)
+        for o, k in enumerate(full):
+            for roles, ranges, loop, glob in voxels.spatial_jobs(k, dr, rr, (3, 3, 3)):
+                specs.append(tpcf.make_spec(tpcf.TRIANGLE, LOOP[loop], TP))
+                jobs.append(eng.job([cat[x] for x in roles], ranges, global_index=glob))
+                outs.append(4 + o)
+        got = eng.count_batch_into(specs, jobs, outs, 8)
+        assert eng.stats()["kernel_launches"] == 2  # one counting launch + recheck
+        for o, k in enumerate(full):
+            assert got[o].sum() > 0, k
+            assert np.array_equal(got[o], got[4 + o]), (k, int(np.abs(got[o].astype(np.int64) - got[4 + o].astype(np.int64)).sum()))
+        # the same full counts through the plain batch
+        plain = eng.count_batch(specs[:4], jobs[:4])
+        for a, b in zip(plain, got[:4]):
+            assert np.array_equal(a, b)
+
+
+@pytest.mark.gpu
+def test_count_batch_into_sums_and_checks():
+    d = synth.blobs(800, n_blobs=3, sigma=5.0, box=50.0, seed=9)
+    with tpcf.Engine(0) as eng:
+        h = eng.catalog(d)
+        sp = tpcf.make_spec(tpcf.PAIR, tpcf.LOOP_SAME, [(100, 0.0, 50.0)])
+        chunks = [voxels.vox2gal(4, i, len(d)) for i in range(4)]
+        jobs = [eng.job([h, h], [chunks[i], chunks[j]]) for i in range(4) for j in range(4)]
+        single = eng.count_batch([sp] * len(jobs), jobs)
+        summed = eng.count_batch_into([sp] * len(jobs), jobs, [0] * len(jobs), 1)[0]
+        assert np.array_equal(summed, sum(single))
+        two = eng.count_batch_into([sp] * len(jobs), jobs, [i % 2 for i in range(len(jobs))], 2)
+        assert np.array_equal(two[0], sum(single[0::2])) and np.array_equal(two[1], sum(single[1::2]))
+        with pytest.raises(tpcf.EngineError):
+            eng.count_batch_into([sp], jobs[:1], [3], 2)
+
+
+@pytest.mark.gpu
+def test_radecz_conversion_matches_script():
+    """Device conversion of ra/dec/redshift against the numpy restatement of
+    the reference's script: equal floats except at a float rounding boundary
+    of the double result (then one float ulp)."""
+    import convert_ref
+    rng = np.random.Generator(np.random.PCG64(77))
+    n = 200000
+    ra = 20.0 * rng.random(n)
+    dec = np.rad2deg(np.arccos(np.cos(np.deg2rad(70)) * rng.random(n))) - 70
+    zr = ((0.55 ** 3 - 0.15 ** 3) * rng.random(n) + 0.15 ** 3) ** (1.0 / 3)
+    want = convert_ref.radecz_to_xyz(ra, dec, zr).astype(np.float32)
+    with tpcf.Engine(0) as eng:
+        got = eng.convert_radecz(ra, dec, zr)
+        other = eng.convert_radecz(ra[:10], dec[:10], zr[:10], poly=(0.0, 1000.0, 0.0))
+    ulp = np.abs(got.view(np.int32).astype(np.int64) - want.view(np.int32).astype(np.int64))
+    assert ulp.max() <= 1
+    assert (ulp == 0).mean() > 0.9999
+    assert np.allclose(other, convert_ref.radecz_to_xyz(ra[:10], dec[:10], zr[:10], (0.0, 1000.0, 0.0)), rtol=1e-6)
