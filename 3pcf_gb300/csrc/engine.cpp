@@ -795,9 +795,10 @@ void plan_triplets(const tpcf_spec& sp, const PlannedJob& pj, uint32_t slot, con
         if (prune) {
             double lab = bAB.L(a, b), lac = bAC.L(a, c), lbc = bBC.L(b, c);
             if (!(lbc < lmax)) return;
-            if (bin.tri_prune &&
-                !tri_triple_possible(bin, lab, lac, lbc, bAB.U(a, b), bAC.U(a, c), bBC.U(b, c)))
-                return;
+            const double uab = bAB.U(a, b), uac = bAC.U(a, c);
+            if (bin.tri_prune && !tri_triple_possible(bin, lab, lac, lbc, uab, uac, bBC.U(b, c))) return;
+            if (uab >= lmax) flags |= TASK_CHECK_B;
+            if (uac >= lmax) flags |= TASK_CHECK_C;
         }
         uint64_t u = task_units3(A, a, B, b, C, c, flags);
         if (u == 0) return;
@@ -1068,6 +1069,8 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
         L.plan_ntasks = ntasks;
         L.plan_evaluated = evaluated;
     }
+    L.stats.plan_ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_wall0).count();
     const bool fp64 = sp.precision != TPCF_GUARDED_FP32;
     if (sp.kind == TPCF_TRIANGLE) ensure_acos(ctx);
     const AcosTable acos_t = sp.kind == TPCF_TRIANGLE ? acos_table(ctx) : AcosTable{};
@@ -1604,6 +1607,7 @@ tpcf_status count_jobs(tpcf_ctx* ctx, const tpcf_spec* specs, const tpcf_job* jo
             acc.tasks += L.stats.tasks;
             acc.kernel_launches += L.stats.kernel_launches;
             acc.graph_replays += L.stats.graph_replays;
+            acc.plan_ms += L.stats.plan_ms;
             acc.tuned_shapes += L.stats.tuned_shapes;
             acc.hist_copies = L.stats.hist_copies;
             acc.ctas_per_sm = L.stats.ctas_per_sm;

@@ -19,13 +19,17 @@ enum Pred : uint32_t {
     PRED_SAME = 2,   // key_i <= key_j <= key_k                      (loop SAME, generic arrays)
     PRED_ONE = 3     // key_j <= key_k                               (loop ONE, generic arrays)
 };
-// task.x: bits 0..21 job slot, 22..24 Pred, 28/29 diagonal flags
+// task.x: bits 0..21 job slot, 22..24 Pred, 28/29 diagonal flags, 30/31 reach checks
 constexpr uint32_t TASK_SLOT_MASK = 0x3FFFFFu;
 constexpr uint32_t MAX_BATCH_JOBS = TASK_SLOT_MASK;  // jobs of one launch
 constexpr int TASK_PRED_SHIFT = 22;
 constexpr uint32_t TASK_PRED_MASK = 0x7u;
 constexpr uint32_t TASK_DIAG_IJ = 1u << 28;  // tiles I and J are the same tile of one view: j > i
 constexpr uint32_t TASK_DIAG_JK = 1u << 29;  // tiles J and K are the same tile of one view: k > j
+// points of tile A may lie out of reach (>= lmax) of tile B / C: worth
+// testing point by point (the guarded triangle kernel; others ignore them)
+constexpr uint32_t TASK_CHECK_B = 1u << 30;
+constexpr uint32_t TASK_CHECK_C = 1u << 31;
 // recheck queue item .x: job slot | weight << 22
 constexpr int RECHECK_WEIGHT_SHIFT = 22;
 

