@@ -35,6 +35,7 @@
 #include <unistd.h>
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
@@ -738,18 +739,22 @@ struct PairBounds {
     const View* b = nullptr;
     bool dense = false;
     std::vector<float> lb, ub;
-    void build(const View& A, const View& B) {
+    // sizes the table; fill_rows(i0, i1) then fills rows independently (threads)
+    void alloc(const View& A, const View& B) {
         a = &A;
         b = &B;
         dense = (int64_t)A.ntiles * B.ntiles <= ((int64_t)1 << 24);
         if (!dense) return;
         lb.resize((size_t)A.ntiles * B.ntiles);
         ub.resize(lb.size());
-        for (int i = 0; i < A.ntiles; i++)
-            for (int j = 0; j < B.ntiles; j++) {
+    }
+    void fill_rows(int i0, int i1) {
+        if (!dense) return;
+        for (int i = i0; i < i1; i++)
+            for (int j = 0; j < b->ntiles; j++) {
                 // float copies rounded outwards so they stay conservative
-                lb[(size_t)i * B.ntiles + j] = nextafterf((float)box_lower_bound(A.boxes[i], B.boxes[j]), 0.f);
-                ub[(size_t)i * B.ntiles + j] = nextafterf((float)box_upper_bound(A.boxes[i], B.boxes[j]), INFINITY);
+                lb[(size_t)i * b->ntiles + j] = nextafterf((float)box_lower_bound(a->boxes[i], b->boxes[j]), 0.f);
+                ub[(size_t)i * b->ntiles + j] = nextafterf((float)box_upper_bound(a->boxes[i], b->boxes[j]), INFINITY);
             }
     }
     double L(int i, int j) const {
@@ -778,87 +783,121 @@ bool tri_triple_possible(const Binning& bin, double l0, double l1, double l2, do
     return p0 || p1;
 }
 
-void plan_triplets(const tpcf_spec& sp, const PlannedJob& pj, uint32_t slot, const Binning& bin,
-                   std::vector<std::pair<uint64_t, uint4>>& tasks, uint64_t& evaluated) {
-    const double lmax = bin.lmax;
-    const View &A = *pj.v[0], &B = *pj.v[1], &C = *pj.v[2];
-    const bool sameAB = pj.v[0] == pj.v[1], sameBC = pj.v[1] == pj.v[2];
-    if (A.ntiles == 0 || B.ntiles == 0 || C.ntiles == 0) return;
-    const bool prune = lmax < INFINITY;
-    PairBounds bAB, bAC, bBC;
-    if (prune) {
-        bAB.build(A, B);
-        bAC.build(A, C);
-        bBC.build(B, C);
-    }
-    auto add = [&](int a, int b, int c, uint32_t pred, uint32_t flags) {
-        if (prune) {
-            double lab = bAB.L(a, b), lac = bAC.L(a, c), lbc = bBC.L(b, c);
-            if (!(lbc < lmax)) return;
-            const double uab = bAB.U(a, b), uac = bAC.U(a, c);
-            if (bin.tri_prune && !tri_triple_possible(bin, lab, lac, lbc, uab, uac, bBC.U(b, c))) return;
-            if (uab >= lmax) flags |= TASK_CHECK_B;
-            if (uac >= lmax) flags |= TASK_CHECK_C;
-        }
-        uint64_t u = task_units3(A, a, B, b, C, c, flags);
-        if (u == 0) return;
-        evaluated += u;
-        tasks.push_back({u, make_uint4(slot | (pred << TASK_PRED_SHIFT) | flags, (uint32_t)a, (uint32_t)b,
-                                       (uint32_t)c)});
-    };
-    // neighbour lists (tile pairs whose lower bound is below lmax)
-    auto nbrs = [&](const View& X, const View& Y, const PairBounds& pb) {
-        std::vector<std::vector<int>> nb(X.ntiles);
-        for (int i = 0; i < X.ntiles; i++)
-            for (int j = 0; j < Y.ntiles; j++)
-                if (!prune || pb.L(i, j) < lmax) nb[i].push_back(j);
-        return nb;
-    };
-    auto nAB = nbrs(A, B, bAB);
-    auto nAC = nbrs(A, C, bAC);
-    const bool tri = sp.kind == TPCF_TRIANGLE || sp.kind == TPCF_TRIANGLE_JBJ;
-    if (tri && sp.loop == TPCF_LOOP_SAME && sameAB && sameBC) {
-        // i <= j <= k over one array: unordered distinct triples
-        for (int a = 0; a < A.ntiles; a++)
-            for (int b : nAB[a]) {
-                if (b < a) continue;
-                for (int c : nAC[a]) {
-                    if (c < b) continue;
-                    uint32_t f = (a == b ? TASK_DIAG_IJ : 0) | (b == c ? TASK_DIAG_JK : 0);
-                    add(a, b, c, PRED_NONE, f);
-                }
-            }
-    } else if (tri && sp.loop == TPCF_LOOP_ONE && sameBC) {
-        // j <= k over one array (j == k has a zero side): unordered pairs
-        for (int a = 0; a < A.ntiles; a++)
-            for (int b : nAB[a])
-                for (int c : nAC[a]) {
-                    if (c < b) continue;
-                    add(a, b, c, PRED_NONE, b == c ? TASK_DIAG_JK : 0);
-                }
-    } else if (tri && sp.loop == TPCF_LOOP_ONE && sameAB) {
-        // every ordered (i, j) of one array, k >= j: unordered {i, j} with
-        // weight [k >= i] + [k >= j]
-        for (int a = 0; a < A.ntiles; a++)
-            for (int b : nAB[a]) {
-                if (b < a) continue;
-                for (int c : nAC[a]) add(a, b, c, PRED_DDR, a == b ? TASK_DIAG_IJ : 0);
-            }
-    } else {
-        uint32_t pred = PRED_NONE;
-        if (tri) pred = sp.loop == TPCF_LOOP_SAME ? PRED_SAME : sp.loop == TPCF_LOOP_ONE ? PRED_ONE : PRED_NONE;
-        for (int a = 0; a < A.ntiles; a++)
-            for (int b : nAB[a])
-                for (int c : nAC[a]) add(a, b, c, pred, 0);
-    }
-}
+typedef std::vector<std::pair<uint64_t, uint4>> TaskList;
 
-void plan_pairs(const tpcf_spec& sp, const PlannedJob& pj, uint32_t slot, double lmax,
-                std::vector<std::pair<uint64_t, uint4>>& tasks, uint64_t& evaluated) {
+// Tile tasks of one triangle/three-side job, planned in two parallel phases:
+// rows(): tile-pair bound tables and neighbour lists, a range of rows at a
+// time; enumerate(): the tile triples of a range of A tiles.
+struct TripletPlan {
+    const tpcf_spec* sp = nullptr;
+    const PlannedJob* pj = nullptr;
+    const Binning* bin = nullptr;
+    uint32_t slot = 0;
+    bool empty = true, prune = false, tri = false, sameAB = false, sameBC = false;
+    PairBounds bAB, bAC, bBC;
+    std::vector<std::vector<int>> nAB, nAC;  // tile pairs whose lower bound is below lmax
+
+    void init(const tpcf_spec& s, const PlannedJob& p, uint32_t sl, const Binning& b) {
+        sp = &s;
+        pj = &p;
+        bin = &b;
+        slot = sl;
+        const View &A = *p.v[0], &B = *p.v[1], &C = *p.v[2];
+        empty = A.ntiles == 0 || B.ntiles == 0 || C.ntiles == 0;
+        if (empty) return;
+        prune = b.lmax < INFINITY;
+        tri = s.kind == TPCF_TRIANGLE || s.kind == TPCF_TRIANGLE_JBJ;
+        sameAB = p.v[0] == p.v[1];
+        sameBC = p.v[1] == p.v[2];
+        if (prune) {
+            bAB.alloc(A, B);
+            bAC.alloc(A, C);
+            bBC.alloc(B, C);
+        }
+        nAB.assign(A.ntiles, {});
+        nAC.assign(A.ntiles, {});
+    }
+    int nrows(int which) const {
+        if (empty) return 0;
+        return which == 2 ? pj->v[1]->ntiles : pj->v[0]->ntiles;
+    }
+    // which: 0 = A-B rows and neighbour lists, 1 = A-C, 2 = B-C bounds
+    void rows(int which, int r0, int r1) {
+        PairBounds& pb = which == 0 ? bAB : which == 1 ? bAC : bBC;
+        if (prune) pb.fill_rows(r0, r1);
+        if (which == 2) return;
+        const View& Y = which == 0 ? *pj->v[1] : *pj->v[2];
+        auto& nb = which == 0 ? nAB : nAC;
+        for (int i = r0; i < r1; i++) {
+            nb[i].clear();
+            for (int j = 0; j < Y.ntiles; j++)
+                if (!prune || pb.L(i, j) < bin->lmax) nb[i].push_back(j);
+        }
+    }
+    void enumerate(int a0, int a1, TaskList& tasks, uint64_t& evaluated) const {
+        if (empty) return;  // a role without tiles: no triple (and no neighbour lists)
+        const View &A = *pj->v[0], &B = *pj->v[1], &C = *pj->v[2];
+        const double lmax = bin->lmax;
+        auto add = [&](int a, int b, int c, uint32_t pred, uint32_t flags) {
+            if (prune) {
+                double lab = bAB.L(a, b), lac = bAC.L(a, c), lbc = bBC.L(b, c);
+                if (!(lbc < lmax)) return;
+                const double uab = bAB.U(a, b), uac = bAC.U(a, c);
+                if (bin->tri_prune && !tri_triple_possible(*bin, lab, lac, lbc, uab, uac, bBC.U(b, c))) return;
+                if (uab >= lmax) flags |= TASK_CHECK_B;
+                if (uac >= lmax) flags |= TASK_CHECK_C;
+            }
+            uint64_t u = task_units3(A, a, B, b, C, c, flags);
+            if (u == 0) return;
+            evaluated += u;
+            tasks.push_back({u, make_uint4(slot | (pred << TASK_PRED_SHIFT) | flags, (uint32_t)a, (uint32_t)b,
+                                           (uint32_t)c)});
+        };
+        const tpcf_spec& s = *sp;
+        if (tri && s.loop == TPCF_LOOP_SAME && sameAB && sameBC) {
+            // i <= j <= k over one array: unordered distinct triples
+            for (int a = a0; a < a1; a++)
+                for (int b : nAB[a]) {
+                    if (b < a) continue;
+                    for (int c : nAC[a]) {
+                        if (c < b) continue;
+                        uint32_t f = (a == b ? TASK_DIAG_IJ : 0) | (b == c ? TASK_DIAG_JK : 0);
+                        add(a, b, c, PRED_NONE, f);
+                    }
+                }
+        } else if (tri && s.loop == TPCF_LOOP_ONE && sameBC) {
+            // j <= k over one array (j == k has a zero side): unordered pairs
+            for (int a = a0; a < a1; a++)
+                for (int b : nAB[a])
+                    for (int c : nAC[a]) {
+                        if (c < b) continue;
+                        add(a, b, c, PRED_NONE, b == c ? TASK_DIAG_JK : 0);
+                    }
+        } else if (tri && s.loop == TPCF_LOOP_ONE && sameAB) {
+            // every ordered (i, j) of one array, k >= j: unordered {i, j} with
+            // weight [k >= i] + [k >= j]
+            for (int a = a0; a < a1; a++)
+                for (int b : nAB[a]) {
+                    if (b < a) continue;
+                    for (int c : nAC[a]) add(a, b, c, PRED_DDR, a == b ? TASK_DIAG_IJ : 0);
+                }
+        } else {
+            uint32_t pred = PRED_NONE;
+            if (tri) pred = s.loop == TPCF_LOOP_SAME ? PRED_SAME : s.loop == TPCF_LOOP_ONE ? PRED_ONE : PRED_NONE;
+            for (int a = a0; a < a1; a++)
+                for (int b : nAB[a])
+                    for (int c : nAC[a]) add(a, b, c, pred, 0);
+        }
+    }
+};
+
+// Pair tasks of A tiles [a0, a1).
+void plan_pairs(const tpcf_spec& sp, const PlannedJob& pj, uint32_t slot, double lmax, int a0, int a1,
+                TaskList& tasks, uint64_t& evaluated) {
     const View &A = *pj.v[0], &B = *pj.v[1];
     if (A.ntiles == 0 || B.ntiles == 0) return;
     const bool same = pj.v[0] == pj.v[1] && sp.loop == TPCF_LOOP_SAME;
-    for (int a = 0; a < A.ntiles; a++)
+    for (int a = a0; a < a1; a++)
         for (int b = same ? a : 0; b < B.ntiles; b++) {
             if (!close_enough(A, a, B, b, lmax)) continue;
             uint64_t na = A.h_tile_start[a + 1] - A.h_tile_start[a], nb = B.h_tile_start[b + 1] - B.h_tile_start[b];
@@ -873,6 +912,27 @@ void plan_pairs(const tpcf_spec& sp, const PlannedJob& pj, uint32_t slot, double
             evaluated += u;
             tasks.push_back({u, make_uint4(slot | (pred << TASK_PRED_SHIFT) | flags, (uint32_t)a, (uint32_t)b, 0)});
         }
+}
+
+// Runs fn(item) for item in [0, n) on up to the host's cores.
+template <typename F>
+void parallel_items(size_t n, F&& fn) {
+    const size_t nth = std::min<size_t>(n, std::max(1u, std::thread::hardware_concurrency()));
+    std::atomic<size_t> next(0);
+    auto worker = [&](size_t t) {
+        for (;;) {
+            size_t i = next.fetch_add(1);
+            if (i >= n) break;
+            fn(i, t);
+        }
+    };
+    if (nth <= 1) {
+        worker(0);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (size_t t = 0; t < nth; t++) th.emplace_back(worker, t);
+    for (auto& t : th) t.join();
 }
 
 size_t shape_smem(const tpcf_spec& sp, const Binning& bin, int copies) {
@@ -893,7 +953,7 @@ std::vector<Shape> shape_candidates(tpcf_ctx* ctx, const tpcf_spec& sp, const Bi
         sh.copies = copies;
         sh.smem = shape_smem(sp, bin, copies);
         sh.per_sm = 0;
-        if (sh.smem > (size_t)max_smem_block) return sh;
+        if (sh.smem + 1024 > (size_t)max_smem_block) return sh;  // leaves room for the kernels' static shared memory
         sh.per_sm = std::min(cap_per_sm, (int)(max_smem_sm / (sh.smem + 1024)));
         return sh;
     };
@@ -1026,37 +1086,54 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
         ntasks = L.plan_ntasks;
         evaluated = L.plan_evaluated;
     } else {
-        // plan the jobs in parallel (one host thread per job, bounded)
-        std::vector<std::vector<std::pair<uint64_t, uint4>>> part(group.size());
-        std::vector<uint64_t> part_eval(group.size(), 0);
-        std::atomic<size_t> next(0);
-        auto worker = [&]() {
-            for (;;) {
-                size_t g = next.fetch_add(1);
-                if (g >= group.size()) break;
-                const tpcf_spec& jsp = *group[g].spec;
-                if (jsp.kind == TPCF_PAIR) plan_pairs(jsp, pj[g], (uint32_t)g, bin.lmax, part[g], part_eval[g]);
-                else plan_triplets(jsp, pj[g], (uint32_t)g, bin, part[g], part_eval[g]);
-            }
-        };
-        size_t nth = std::min<size_t>(group.size(), std::max(1u, std::thread::hardware_concurrency()));
-        if (nth <= 1) {
-            worker();
-        } else {
-            std::vector<std::thread> th;
-            for (size_t t = 0; t < nth; t++) th.emplace_back(worker);
-            for (auto& t : th) t.join();
+        // plan in parallel: bound tables and neighbour lists by rows, then
+        // tile triples (pairs) by ranges of A tiles
+        const bool pairs = sp.kind == TPCF_PAIR;
+        std::vector<TripletPlan> tp(pairs ? 0 : group.size());
+        if (!pairs) {
+            for (size_t g = 0; g < group.size(); g++) tp[g].init(*group[g].spec, pj[g], (uint32_t)g, bin);
+            std::vector<std::array<int, 4>> items;  // job, which, row begin, row end
+            for (size_t g = 0; g < group.size(); g++)
+                for (int w = 0; w < 3; w++)
+                    for (int r = 0; r < tp[g].nrows(w); r += 16)
+                        items.push_back({(int)g, w, r, std::min(r + 16, tp[g].nrows(w))});
+            parallel_items(items.size(), [&](size_t i, size_t) {
+                const auto& it = items[i];
+                tp[it[0]].rows(it[1], it[2], it[3]);
+            });
         }
-        std::vector<std::pair<uint64_t, uint4>> tasks;
+        std::vector<std::array<int, 3>> items;  // job, A-tile begin, end
         for (size_t g = 0; g < group.size(); g++) {
-            evaluated += part_eval[g];
-            tasks.insert(tasks.end(), part[g].begin(), part[g].end());
+            const int na = pj[g].v[0]->ntiles, step = pairs ? 16 : 2;
+            for (int a0 = 0; a0 < na; a0 += step) items.push_back({(int)g, a0, std::min(a0 + step, na)});
         }
-        // largest tasks first (dynamic fetch then balances the tail)
-        std::stable_sort(tasks.begin(), tasks.end(),
-                         [](const std::pair<uint64_t, uint4>& a, const std::pair<uint64_t, uint4>& b) { return a.first > b.first; });
-        std::vector<uint4> h_tasks(tasks.size());
-        for (size_t i = 0; i < tasks.size(); i++) h_tasks[i] = tasks[i].second;
+        // one task list per item, so that the concatenation keeps job order
+        // (a CTA flushes its shared histogram whenever the job changes)
+        std::vector<TaskList> part(items.size());
+        std::vector<uint64_t> part_eval(items.size(), 0);
+        parallel_items(items.size(), [&](size_t i, size_t) {
+            const auto& it = items[i];
+            if (pairs)
+                plan_pairs(*group[it[0]].spec, pj[it[0]], (uint32_t)it[0], bin.lmax, it[1], it[2], part[i],
+                           part_eval[i]);
+            else
+                tp[it[0]].enumerate(it[1], it[2], part[i], part_eval[i]);
+        });
+        // largest tasks first (dynamic fetch then balances the tail): a stable
+        // counting pass over 64 size classes (floor(log2(units)))
+        size_t total = 0;
+        for (size_t i = 0; i < part.size(); i++) {
+            evaluated += part_eval[i];
+            total += part[i].size();
+        }
+        auto cls = [](uint64_t u) { return 63 - (u ? 63 - __builtin_clzll(u) : 0); };
+        std::vector<size_t> start(65, 0);
+        for (auto& pt : part)
+            for (auto& e : pt) start[cls(e.first) + 1]++;
+        for (int c = 0; c < 64; c++) start[c + 1] += start[c];
+        std::vector<uint4> h_tasks(total);
+        for (auto& pt : part)
+            for (auto& e : pt) h_tasks[start[cls(e.first)]++] = e.second;
         ntasks = h_tasks.size();
         L.d_jobs.reserve(dj.size());
         L.d_tasks.reserve(std::max<size_t>(h_tasks.size(), 1));
@@ -1432,6 +1509,7 @@ tpcf_status tpcf_create(tpcf_ctx** out, int32_t device) {
         ctx->device = device;
         CK(cudaSetDevice(device));
         CK(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device));
+        CK(prepare_kernels(device));
         const char* tp = getenv("TPCF_TILE_POINTS");
         if (tp) ctx->tile_points = std::max(8, std::min(TILE, atoi(tp)));
         const char* adm = getenv("TPCF_ADMIT_BYTES");

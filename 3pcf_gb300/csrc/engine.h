@@ -119,6 +119,7 @@ struct LaunchStats {
 };
 
 // ---- kernel launchers (kernels.cu) ----
+cudaError_t prepare_kernels(int device);  // once per device before any launch
 cudaError_t launch_triangle_fast(const DevJob* jobs, const uint4* tasks, unsigned int ntasks,
                                  unsigned int* task_counter, const TriParams& p, RecheckQueue q,
                                  int grid, int hist_copies, cudaStream_t st);

@@ -958,15 +958,31 @@ __device__ __forceinline__ uint32_t side_code3(float d, const ThreeParams& p, ui
 
 template <bool FP64, bool GLOBAL_HIST>
 __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& p, float4* P, uint32_t* JK,
-                                uint32_t* IJ, unsigned int* Hw) {
+                                uint32_t* IJ, unsigned long long* JKM, unsigned int* Hw) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const TaskGeom g = task_geom(J, task);
     const uint32_t n = p.n, n2 = (uint32_t)p.n * p.n, len = (uint32_t)p.len;
     load_points(P, J, g);
     __syncthreads();
-    for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
-        int j = e / TILE, k = e % TILE;
-        if (j < g.nB && k < g.nC) JK[e] = side_code3<FP64>(ref_dist<FP64>(P[TILE + j], P[2 * TILE + k]), p, n2);
+    if (p.clean) {
+        // j-k codes, one warp per row j, and JKM[j]: the k's whose side is
+        // below hist_max (clean mode drops every triple with a longer side)
+        for (int j = warp; j < g.nB; j += TS_WARPS) {
+            const float4 pj = P[TILE + j];
+            uint32_t c0 = TS_FAR, c1 = TS_FAR;
+            if (lane < g.nC) c0 = side_code3<FP64>(ref_dist<FP64>(pj, P[2 * TILE + lane]), p, n2);
+            if (lane + 32 < g.nC) c1 = side_code3<FP64>(ref_dist<FP64>(pj, P[2 * TILE + lane + 32]), p, n2);
+            JK[j * TILE + lane] = c0;
+            JK[j * TILE + lane + 32] = c1;
+            const unsigned long long m = ballot64(c0 < TS_FAR, c1 < TS_FAR);
+            if (lane == 0) JKM[j] = m;
+        }
+    } else {
+        for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
+            const int j = e / TILE, k = e % TILE;
+            JK[e] = (j < g.nB && k < g.nC) ? side_code3<FP64>(ref_dist<FP64>(P[TILE + j], P[2 * TILE + k]), p, n2)
+                                           : TS_FAR;
+        }
     }
     __syncthreads();
     uint32_t* row = IJ + warp * TILE;
@@ -975,18 +991,26 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
         uint32_t cik[2];
 #pragma unroll
         for (int r = 0; r < 2; r++) {
-            int k = lane + 32 * r;
+            const int k = lane + 32 * r;
             cik[r] = k < g.nC ? side_code3<FP64>(ref_dist<FP64>(pi, P[2 * TILE + k]), p, n) : TS_FAR;
+        }
+        // k's whose i-k side can count (clean mode drops sides >= hist_max)
+        const unsigned long long mk = p.clean ? ballot64(cik[0] < TS_FAR, cik[1] < TS_FAR) : ~0ull;
+        if (!mk) continue;  // warp-uniform
+#pragma unroll
+        for (int r = 0; r < 2; r++) {
+            const int k = lane + 32 * r;
             if (k < g.nB) row[k] = side_code3<FP64>(ref_dist<FP64>(pi, P[TILE + k]), p, 1u);
         }
         __syncwarp();
 #pragma unroll 4
         for (int j = 0; j < g.nB; j++) {
             const uint32_t cij = row[j];
+            if (p.clean && (cij >= TS_FAR || !(mk & JKM[j]))) continue;  // warp-uniform
 #pragma unroll
             for (int r = 0; r < 2; r++) {
                 const int k = lane + 32 * r;
-                const uint32_t idx = JK[j * TILE + (k < g.nC ? k : 0)] + cik[r] + cij;
+                const uint32_t idx = JK[j * TILE + k] + cik[r] + cij;
                 if (idx < len) {
                     if (GLOBAL_HIST) atomicAdd(J.hist + idx, 1ull);
                     else atomicAdd(Hw + idx, 1u);
@@ -1006,6 +1030,7 @@ three_side_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ tas
     uint32_t* JK = reinterpret_cast<uint32_t*>(smem + 3 * TILE * sizeof(float4));
     uint32_t* IJ = JK + TILE * TILE;
     unsigned int* H = IJ + TS_WARPS * TILE;
+    __shared__ unsigned long long s_jkm[TILE];
     __shared__ uint4 s_task;
     if (!GLOBAL_HIST)
         for (int b = threadIdx.x; b < copies * p.len; b += blockDim.x) H[b] = 0;
@@ -1028,7 +1053,7 @@ three_side_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ tas
         cur = slot;
         if (slot < 0) break;
         since++;
-        three_side_task<FP64, GLOBAL_HIST>(jobs[slot], task, p, P, JK, IJ, Hw);
+        three_side_task<FP64, GLOBAL_HIST>(jobs[slot], task, p, P, JK, IJ, s_jkm, Hw);
     }
 }
 
@@ -1123,20 +1148,39 @@ int triangle_block_threads() { return TRI_THREADS; }
 int three_side_block_threads() { return TS_THREADS; }
 int pair_block_threads() { return PR_THREADS; }
 
+// Every counting kernel may use the device's whole opt-in shared memory per
+// block.  Set once per device, before any launch or graph capture, and never
+// lowered: a launch (or a captured graph replayed later) is then valid for
+// any histogram size the launch shape allows.
+cudaError_t prepare_kernels(int device) {
+    int optin = 0;
+    cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    if (e != cudaSuccess) return e;
+    const void* fns[] = {(const void*)triangle_fast_kernel<true>, (const void*)triangle_fast_kernel<false>,
+                         (const void*)triangle_fp64_kernel<MODE_FP64>, (const void*)triangle_fp64_kernel<MODE_GEOM>,
+                         (const void*)triangle_fp64_kernel<MODE_JBJ>, (const void*)three_side_kernel<true, true>,
+                         (const void*)three_side_kernel<true, false>, (const void*)three_side_kernel<false, true>,
+                         (const void*)three_side_kernel<false, false>, (const void*)pair_kernel<true>,
+                         (const void*)pair_kernel<false>};
+    for (const void* f : fns) {
+        cudaFuncAttributes fa;
+        e = cudaFuncGetAttributes(&fa, f);
+        if (e != cudaSuccess) return e;
+        // dynamic plus static shared memory may not exceed the opt-in limit
+        e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 cudaError_t launch_triangle_fast(const DevJob* jobs, const uint4* tasks, unsigned int ntasks,
                                  unsigned int* task_counter, const TriParams& p, RecheckQueue q, int grid,
                                  int copies, cudaStream_t st) {
     size_t smem = triangle_smem_bytes(p.len, copies);
-    cudaError_t e;
-    if (p.theta_full) {
-        e = cudaFuncSetAttribute(triangle_fast_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
+    if (p.theta_full)
         triangle_fast_kernel<true><<<grid, TRI_THREADS, smem, st>>>(jobs, tasks, ntasks, task_counter, p, q, copies);
-    } else {
-        e = cudaFuncSetAttribute(triangle_fast_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
+    else
         triangle_fast_kernel<false><<<grid, TRI_THREADS, smem, st>>>(jobs, tasks, ntasks, task_counter, p, q, copies);
-    }
     return cudaGetLastError();
 }
 
@@ -1153,8 +1197,6 @@ cudaError_t launch_triangle_fp64(const DevJob* jobs, const uint4* tasks, unsigne
     auto kern = mode == MODE_GEOM ? triangle_fp64_kernel<MODE_GEOM>
                 : mode == MODE_JBJ  ? triangle_fp64_kernel<MODE_JBJ>
                                     : triangle_fp64_kernel<MODE_FP64>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
     kern<<<grid, TRI_THREADS, smem, st>>>(jobs, tasks, ntasks, task_counter, p, t, copies);
     return cudaGetLastError();
 }
@@ -1164,10 +1206,7 @@ cudaError_t launch_three_side(const DevJob* jobs, const uint4* tasks, unsigned i
                               cudaStream_t st) {
     const bool global = copies == 0;
     size_t smem = three_side_smem_bytes(global ? 0 : p.len, global ? 0 : copies);
-    cudaError_t e;
-#define TS_LAUNCH(FP, GL)                                                                                   \
-    e = cudaFuncSetAttribute(three_side_kernel<FP, GL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-    if (e != cudaSuccess) return e;                                                                         \
+#define TS_LAUNCH(FP, GL) \
     three_side_kernel<FP, GL><<<grid, TS_THREADS, smem, st>>>(jobs, tasks, ntasks, task_counter, p, copies > 0 ? copies : 1);
     if (fp64) {
         if (global) { TS_LAUNCH(true, true) } else { TS_LAUNCH(true, false) }
@@ -1215,16 +1254,10 @@ cudaError_t launch_radecz_to_xyz(const double* ra, const double* dec, const doub
 cudaError_t launch_pairs(const DevJob* jobs, const uint4* tasks, unsigned int ntasks, unsigned int* task_counter,
                          const PairParams& p, int fp64, int grid, int copies, cudaStream_t st) {
     size_t smem = pair_smem_bytes(p.n, copies);
-    cudaError_t e;
-    if (fp64) {
-        e = cudaFuncSetAttribute(pair_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
+    if (fp64)
         pair_kernel<true><<<grid, PR_THREADS, smem, st>>>(jobs, tasks, ntasks, task_counter, p, copies);
-    } else {
-        e = cudaFuncSetAttribute(pair_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
+    else
         pair_kernel<false><<<grid, PR_THREADS, smem, st>>>(jobs, tasks, ntasks, task_counter, p, copies);
-    }
     return cudaGetLastError();
 }
 

@@ -50,3 +50,38 @@ def xi(dd, dr, rr, n_dd, n_dr, n_rr):
             t = 0.0
         out.append(t)
     return out
+
+
+def reduced_zeta(z, spec, sbin, qbins, xi_x, xi_y):
+    """Element-by-element restatement of examples/plot_MICE_3pcf.py:175-232:
+    sxx2cf (:7-28, nearest tabulated separation, first on ties), bin2val
+    (:30-36), sqtheta2s1s2s3 (:39-45), Q = zeta / (x12 x23 + x23 x31 + x31 x12)."""
+    import math
+    (S, slo, shi), (Q, qlo, qhi), (T, tlo, thi) = spec
+    tw = (thi - tlo) / T
+
+    def bin2val(b, lo, hi, n):
+        w = (hi - lo) / float(n)
+        return lo + (w * b) + (w / 2.0)
+
+    def nearest(s):
+        diffs = [abs(s - x) for x in xi_x]
+        m = min(diffs)
+        return xi_y[diffs.index(m)]
+
+    sval = bin2val(sbin, slo, shi, S)
+    out = []
+    for qb in qbins:
+        qval = bin2val(qb, qlo, qhi, Q)
+        row = []
+        for t in range(T):
+            x = tlo + t * tw
+            theta = math.pi * (x + tw / 2.0)
+            s12, s23 = sval, sval * qval
+            s31 = sval * math.sqrt(1 + qval * qval - 2 * qval * math.cos(theta))
+            c12, c23, c31 = nearest(s12), nearest(s23), nearest(s31)
+            den = c12 * c23 + c23 * c31 + c31 * c12
+            zz = z[(sbin * Q + qb) * T + t]
+            row.append(zz / den if den != 0 else (math.copysign(math.inf, zz) if zz != 0 else math.nan))
+        out.append(row)
+    return out

@@ -62,6 +62,8 @@ def test_reduced_zeta_shape_and_finite_denominator():
     q = estimators.reduced_zeta(z, spec, 3, [0, 1, 2], tab)
     assert q.shape == (3, 16)
     assert np.all(np.isfinite(q))
+    want = estimators_ref.reduced_zeta(z, spec, 3, [0, 1, 2], list(tab[:, 0]), list(tab[:, 1]))
+    assert np.allclose(q, np.array(want), rtol=1e-13, atol=0)
 
 
 def test_zeta_error_summary():
