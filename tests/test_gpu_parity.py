@@ -375,3 +375,30 @@ def test_jbj_vs_oracle_both_overflow_modes(eng, spec):
                 assert np.array_equal(got, want), (overflow, prune, w)
     eng.release(hd)
     eng.release(hr)
+
+
+@pytest.mark.parametrize("tile_points", [17, 32, 48])
+def test_counts_do_not_depend_on_tile_size(monkeypatch, tile_points):
+    """Smaller spatial tiles (many partial tiles) give the same histograms as
+    the default 64-point tiles.  (The number of candidates binned may differ:
+    tile triples that provably hold no counted triangle are pruned, and with
+    them class-level candidates that the exact binning would reject.)"""
+    d = synth.blobs(3000, n_blobs=6, sigma=5.0, box=80.0, seed=77)
+    r = synth.uniform(2500, box=120.0, seed=78)
+    spec = ((8, 2.0, 10.0), (8, 1.0, 3.0), (16, 0.0, 1.0))
+    loops = [tpcf.LOOP_SAME, tpcf.LOOP_ONE, tpcf.LOOP_ONE, tpcf.LOOP_SAME]
+
+    def run():
+        with tpcf.Engine(0) as e:
+            hd, hr = e.catalog(d), e.catalog(r)
+            jobs = [e.job([hd, hd, hd]), e.job([hd, hd, hr]), e.job([hd, hr, hr]), e.job([hr, hr, hr])]
+            out = []
+            return [e.count(_tp_spec(spec, lp, nan=NATIVE_NAN), jb) for lp, jb in zip(loops, jobs)]
+
+    monkeypatch.delenv("TPCF_TILE_POINTS", raising=False)
+    want = run()
+    monkeypatch.setenv("TPCF_TILE_POINTS", str(tile_points))
+    got = run()
+    for hw, hg in zip(want, got):
+        assert np.array_equal(hw, hg)
+        assert hw.sum() > 0
