@@ -603,6 +603,7 @@ struct tpcf_ctx {
     std::vector<std::thread> workers;
     bool stop = false;
     int64_t admit_bytes = (int64_t)8 << 30;
+    double heavy_cost = 1e12;  // job_cost above which a job runs alone on the first serving lane
     int64_t inflight_bytes = 0;  // device bytes of batches running on serving lanes
     // autotuner: launch shape per batch signature
     std::mutex tune_mu;
@@ -1397,9 +1398,27 @@ double now_ms() {
 // persistent launch on its own stream and completes their tickets.  Jobs that
 // arrive meanwhile are taken by the next free worker, so batches overlap on
 // the device.
+// Work estimate of a job for scheduling: the product of its catalog range
+// sizes (the loop size up to a constant).
+double job_cost(tpcf_ctx* ctx, const tpcf_spec& sp, const tpcf_job& job) {
+    double c = 1;
+    int nc = sp.kind == TPCF_PAIR ? 2 : 3;
+    for (int r = 0; r < nc; r++) {
+        auto it = ctx->catalogs.find(job.catalog[r]);
+        if (it == ctx->catalogs.end()) continue;
+        int64_t e = job.end[r] < 0 ? it->second->n : job.end[r];
+        c *= (double)std::max<int64_t>(e - job.begin[r], 0);
+    }
+    return c;
+}
+
 void worker_loop(tpcf_ctx* ctx, int lane) {
     Lane& L = *ctx->lanes[lane];
     cudaSetDevice(ctx->device);
+    // the first serving lane takes any job; the others only light ones, so
+    // that light jobs keep flowing while heavy ones run
+    const bool light_only = lane >= 2;
+    auto heavy = [&](const Pending& p) { return job_cost(ctx, p.spec, p.job) > ctx->heavy_cost; };
     for (;;) {
         std::vector<std::shared_ptr<Pending>> batch;
         int64_t used = 0;
@@ -1419,7 +1438,17 @@ void worker_loop(tpcf_ctx* ctx, int lane) {
                     }
                 }
                 if (ctx->queue.empty()) continue;
-                auto first = ctx->queue.front();
+                // the oldest job this lane takes
+                std::shared_ptr<Pending> first;
+                for (auto& p : ctx->queue)
+                    if (!light_only || !heavy(*p)) {
+                        first = p;
+                        break;
+                    }
+                if (!first) {
+                    ctx->qcv.wait(lk);
+                    continue;
+                }
                 int64_t room = ctx->admit_bytes - ctx->inflight_bytes;
                 int64_t fb = job_bytes(ctx, first->spec, first->job);
                 // the oldest job waits for memory unless nothing else is in flight
@@ -1427,9 +1456,12 @@ void worker_loop(tpcf_ctx* ctx, int lane) {
                     ctx->qcv.wait(lk);
                     continue;
                 }
+                // a heavy job runs alone; light jobs of the same binning share a launch
+                const bool first_heavy = heavy(*first);
                 for (auto it = ctx->queue.begin(); it != ctx->queue.end();) {
                     auto& p = *it;
-                    if (!same_binning(p->spec, first->spec) || p->spec.prune != first->spec.prune) {
+                    if (!same_binning(p->spec, first->spec) || p->spec.prune != first->spec.prune ||
+                        (p != first && (first_heavy || heavy(*p)))) {
                         ++it;
                         continue;
                     }
@@ -1514,6 +1546,8 @@ tpcf_status tpcf_create(tpcf_ctx** out, int32_t device) {
         if (tp) ctx->tile_points = std::max(8, std::min(TILE, atoi(tp)));
         const char* adm = getenv("TPCF_ADMIT_BYTES");
         if (adm) ctx->admit_bytes = atoll(adm);
+        const char* hc = getenv("TPCF_HEAVY_COST");
+        if (hc) ctx->heavy_cost = atof(hc);
         const char* nw = getenv("TPCF_SERVING_LANES");
         int workers = nw ? std::max(1, std::min(8, atoi(nw))) : 2;
         for (int i = 0; i <= workers; i++) {

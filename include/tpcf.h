@@ -209,8 +209,11 @@ tpcf_status tpcf_count_batch_into(tpcf_ctx* ctx, const tpcf_spec* specs, const t
  * with every pending job of the same binning, while the device bytes of all
  * running batches stay within the admission budget (TPCF_ADMIT_BYTES, default
  * 8 GiB), and count them in one launch; jobs submitted meanwhile go to the next
- * free worker, so batches overlap on the device.  tpcf_wait blocks up to
- * timeout_ms (<0: forever); tpcf_cancel drops a job that has not started. */
+ * free worker, so batches overlap on the device.  A heavy job (product of its
+ * catalog sizes above TPCF_HEAVY_COST, default 1e12) runs alone, and only the
+ * first worker takes heavy jobs, so light jobs keep flowing beside them.
+ * tpcf_wait blocks up to timeout_ms (<0: forever); tpcf_cancel drops a job that
+ * has not started. */
 tpcf_status tpcf_submit(tpcf_ctx* ctx, const tpcf_spec* spec, const tpcf_job* job, uint64_t* ticket);
 tpcf_status tpcf_wait(tpcf_ctx* ctx, uint64_t ticket, uint64_t* hist, int64_t hist_len, int64_t timeout_ms);
 /* As tpcf_wait; also returns the job's milliseconds from submission to

@@ -101,3 +101,18 @@ def test_admission_budget_serialises_but_stays_exact(monkeypatch):
         tickets = [eng.submit(s, j) for s, j in jobs]
         for (spec, _), t, want in zip(jobs, tickets, alone):
             assert np.array_equal(eng.wait(t, spec), want)
+
+
+@pytest.mark.parametrize("heavy_cost,lanes", [("1", "2"), ("1e9", "3")])
+def test_heavy_jobs_run_alone_and_stay_exact(monkeypatch, heavy_cost, lanes):
+    """Scheduling by job size: heavy jobs alone on the first worker, light
+    jobs batched on the others; every histogram as when counted alone."""
+    monkeypatch.setenv("TPCF_HEAVY_COST", heavy_cost)
+    monkeypatch.setenv("TPCF_SERVING_LANES", lanes)
+    with tpcf.Engine(0) as eng:
+        handles = [eng.catalog(c) for c in _catalogs()]
+        jobs = _jobs(eng, handles)
+        alone = [eng.count(s, j) for s, j in jobs]
+        tickets = [eng.submit(s, j) for s, j in jobs]
+        for (spec, _), t, want in zip(jobs, tickets, alone):
+            assert np.array_equal(eng.wait(t, spec), want)
