@@ -40,6 +40,7 @@
 #include <chrono>
 #include <condition_variable>
 #include <deque>
+#include <functional>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -72,23 +73,101 @@ struct InvalidArg {
 // ---------------------------------------------------------------------------
 // device buffers
 
+// Freed device blocks up to 64 MiB are kept per device and power-of-two size
+// class for reuse (at most 2 GiB in all), so that the catalogs, views and
+// task lists of a repeated upload-count-release cycle cost no cudaMalloc /
+// cudaFree (each of which also synchronises the device).  A block is only
+// freed once nothing can still use it: views and scratch buffers are released
+// after the work that read them has completed on its stream.
+class DeviceBlocks {
+  public:
+    static DeviceBlocks& get() {
+        static DeviceBlocks* d = new DeviceBlocks();  // never destroyed: blocks live until the process ends
+        return *d;
+    }
+    void* alloc(size_t bytes, size_t* cap) {
+        int dev = 0;
+        CK(cudaGetDevice(&dev));
+        size_t cls = 256;
+        while (cls < bytes) cls <<= 1;
+        if (cls > kMaxCached) {
+            void* p = nullptr;
+            CK(cudaMalloc(&p, bytes));
+            *cap = bytes;
+            return p;
+        }
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            auto& v = free_[std::make_pair(dev, cls)];
+            if (!v.empty()) {
+                void* p = v.back();
+                v.pop_back();
+                cached_ -= cls;
+                *cap = cls;
+                return p;
+            }
+        }
+        void* p = nullptr;
+        if (cudaMalloc(&p, cls) != cudaSuccess) {
+            // out of memory: give the kept blocks back and try once more
+            (void)cudaGetLastError();
+            trim();
+            CK(cudaMalloc(&p, cls));
+        }
+        *cap = cls;
+        return p;
+    }
+    void trim() {
+        std::lock_guard<std::mutex> lk(mu_);
+        int dev = 0;
+        cudaGetDevice(&dev);
+        for (auto& kv : free_) {
+            if (kv.first.first != dev) continue;
+            for (void* q : kv.second) cudaFree(q);
+            cached_ -= kv.first.second * kv.second.size();
+            kv.second.clear();
+        }
+    }
+    void release(void* p, size_t cap) {
+        if (!p) return;
+        int dev = 0;
+        if (cap <= kMaxCached && cudaGetDevice(&dev) == cudaSuccess) {
+            std::lock_guard<std::mutex> lk(mu_);
+            if (cached_ + cap <= kMaxTotal) {
+                free_[std::make_pair(dev, cap)].push_back(p);
+                cached_ += cap;
+                return;
+            }
+        }
+        cudaFree(p);
+    }
+
+  private:
+    static constexpr size_t kMaxCached = (size_t)64 << 20, kMaxTotal = (size_t)2 << 30;
+    std::mutex mu_;
+    std::map<std::pair<int, size_t>, std::vector<void*>> free_;
+    size_t cached_ = 0;
+};
+
 template <typename T>
 struct DevBuf {
     T* p = nullptr;
     size_t n = 0;
+    size_t cap = 0;  // bytes of the block
     DevBuf() = default;
     DevBuf(const DevBuf&) = delete;
     DevBuf& operator=(const DevBuf&) = delete;
     ~DevBuf() { release(); }
     void release() {
-        if (p) cudaFree(p);
+        DeviceBlocks::get().release(p, cap);
         p = nullptr;
         n = 0;
+        cap = 0;
     }
     void reserve(size_t m) {
         if (m <= n) return;
         release();
-        CK(cudaMalloc((void**)&p, std::max<size_t>(m, 1) * sizeof(T)));
+        p = (T*)DeviceBlocks::get().alloc(std::max<size_t>(m, 1) * sizeof(T), &cap);
         n = m;
     }
     size_t bytes() const { return n * sizeof(T); }
@@ -139,9 +218,12 @@ struct View {
 // Balanced k-d split: order[lo, hi) is split along the widest axis so that the
 // left part holds a multiple of TILE points, recursively, until parts hold at
 // most TILE points.  Leaves appear in order, giving spatially compact tiles.
-void kd_order(const float* xyz, std::vector<int32_t>& order, int64_t lo, int64_t hi, int tile) {
+// One split of order[lo, hi): along the widest axis, so that the left part
+// holds a multiple of `tile` points.  Returns the split point, or -1 for a
+// part of at most `tile` points (a leaf).
+int64_t kd_split(const float* xyz, std::vector<int32_t>& order, int64_t lo, int64_t hi, int tile) {
     int64_t n = hi - lo;
-    if (n <= tile) return;
+    if (n <= tile) return -1;
     float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (int64_t i = lo; i < hi; i++)
         for (int a = 0; a < 3; a++) {
@@ -160,8 +242,33 @@ void kd_order(const float* xyz, std::vector<int32_t>& order, int64_t lo, int64_t
         float vp = xyz[3 * (int64_t)p + ax], vq = xyz[3 * (int64_t)q + ax];
         return vp < vq || (vp == vq && p < q);
     });
-    kd_order(xyz, order, lo, mid, tile);
-    kd_order(xyz, order, mid, hi, tile);
+    return mid;
+}
+
+void parallel_items(size_t n, const std::function<void(size_t)>& fn);
+
+// Balanced k-d split of order[0, n) until parts hold at most `tile` points;
+// leaves appear in order, giving spatially compact tiles.  Level by level,
+// the parts of a level split in parallel (each split is deterministic, so the
+// order does not depend on the threads).
+void kd_order(const float* xyz, std::vector<int32_t>& order, int64_t n, int tile) {
+    std::vector<std::pair<int64_t, int64_t>> level{{0, n}};
+    while (!level.empty()) {
+        std::vector<int64_t> mids(level.size(), -1);
+        auto split = [&](size_t i) { mids[i] = kd_split(xyz, order, level[i].first, level[i].second, tile); };
+        if (level.size() < 4 || n < 4096) {
+            for (size_t i = 0; i < level.size(); i++) split(i);
+        } else {
+            parallel_items(level.size(), split);
+        }
+        std::vector<std::pair<int64_t, int64_t>> next;
+        for (size_t i = 0; i < level.size(); i++)
+            if (mids[i] >= 0) {
+                next.push_back({level[i].first, mids[i]});
+                next.push_back({mids[i], level[i].second});
+            }
+        level.swap(next);
+    }
 }
 
 // Lower bound on the reference's float side length between any point of box
@@ -643,7 +750,7 @@ std::shared_ptr<View> get_view(tpcf_ctx* ctx, Lane& L, uint64_t handle, int64_t 
     }
     std::vector<int32_t> order(n);
     std::iota(order.begin(), order.end(), 0);
-    kd_order(xyz.data(), order, 0, n, tile);
+    kd_order(xyz.data(), order, n, tile);
     v->ntiles = (int)((n + tile - 1) / tile);
     std::vector<float4> pts(std::max<int64_t>(n, 1));
     for (int64_t i = 0; i < n; i++) {
@@ -786,54 +893,59 @@ bool tri_triple_possible(const Binning& bin, double l0, double l1, double l2, do
 
 typedef std::vector<std::pair<uint64_t, uint4>> TaskList;
 
-// Tile tasks of one triangle/three-side job, planned in two parallel phases:
-// rows(): tile-pair bound tables and neighbour lists, a range of rows at a
-// time; enumerate(): the tile triples of a range of A tiles.
+// Lower/upper side bounds and neighbour lists (tile pairs whose lower bound is
+// below lmax) of one pair of views, shared by every job of a launch that
+// pairs those views; rows() fills a range of rows (parallel planning).
+struct PairTable {
+    const View* x = nullptr;
+    const View* y = nullptr;
+    bool prune = false, need_nb = false;
+    double lmax = INFINITY;
+    PairBounds pb;
+    std::vector<std::vector<int>> nb;
+    void init(const View& X, const View& Y, double lmax_) {
+        x = &X;
+        y = &Y;
+        lmax = lmax_;
+        prune = lmax < INFINITY;
+        if (prune) pb.alloc(X, Y);
+    }
+    void rows(int r0, int r1) {
+        if (prune) pb.fill_rows(r0, r1);
+        if (!need_nb) return;
+        for (int i = r0; i < r1; i++) {
+            nb[i].clear();
+            for (int j = 0; j < y->ntiles; j++)
+                if (!prune || pb.L(i, j) < lmax) nb[i].push_back(j);
+        }
+    }
+};
+
+// Tile tasks of one triangle/three-side job: enumerate() lists the tile
+// triples of a range of A tiles from the pair tables of (A,B), (A,C), (B,C).
 struct TripletPlan {
     const tpcf_spec* sp = nullptr;
     const PlannedJob* pj = nullptr;
     const Binning* bin = nullptr;
     uint32_t slot = 0;
     bool empty = true, prune = false, tri = false, sameAB = false, sameBC = false;
-    PairBounds bAB, bAC, bBC;
-    std::vector<std::vector<int>> nAB, nAC;  // tile pairs whose lower bound is below lmax
+    const PairTable *AB = nullptr, *AC = nullptr, *BC = nullptr;
 
-    void init(const tpcf_spec& s, const PlannedJob& p, uint32_t sl, const Binning& b) {
+    void init(const tpcf_spec& s, const PlannedJob& p, uint32_t sl, const Binning& b, const PairTable* ab,
+              const PairTable* ac, const PairTable* bc) {
         sp = &s;
         pj = &p;
         bin = &b;
         slot = sl;
         const View &A = *p.v[0], &B = *p.v[1], &C = *p.v[2];
         empty = A.ntiles == 0 || B.ntiles == 0 || C.ntiles == 0;
-        if (empty) return;
         prune = b.lmax < INFINITY;
         tri = s.kind == TPCF_TRIANGLE || s.kind == TPCF_TRIANGLE_JBJ;
         sameAB = p.v[0] == p.v[1];
         sameBC = p.v[1] == p.v[2];
-        if (prune) {
-            bAB.alloc(A, B);
-            bAC.alloc(A, C);
-            bBC.alloc(B, C);
-        }
-        nAB.assign(A.ntiles, {});
-        nAC.assign(A.ntiles, {});
-    }
-    int nrows(int which) const {
-        if (empty) return 0;
-        return which == 2 ? pj->v[1]->ntiles : pj->v[0]->ntiles;
-    }
-    // which: 0 = A-B rows and neighbour lists, 1 = A-C, 2 = B-C bounds
-    void rows(int which, int r0, int r1) {
-        PairBounds& pb = which == 0 ? bAB : which == 1 ? bAC : bBC;
-        if (prune) pb.fill_rows(r0, r1);
-        if (which == 2) return;
-        const View& Y = which == 0 ? *pj->v[1] : *pj->v[2];
-        auto& nb = which == 0 ? nAB : nAC;
-        for (int i = r0; i < r1; i++) {
-            nb[i].clear();
-            for (int j = 0; j < Y.ntiles; j++)
-                if (!prune || pb.L(i, j) < bin->lmax) nb[i].push_back(j);
-        }
+        AB = ab;
+        AC = ac;
+        BC = bc;
     }
     void enumerate(int a0, int a1, TaskList& tasks, uint64_t& evaluated) const {
         if (empty) return;  // a role without tiles: no triple (and no neighbour lists)
@@ -841,10 +953,10 @@ struct TripletPlan {
         const double lmax = bin->lmax;
         auto add = [&](int a, int b, int c, uint32_t pred, uint32_t flags) {
             if (prune) {
-                double lab = bAB.L(a, b), lac = bAC.L(a, c), lbc = bBC.L(b, c);
+                double lab = AB->pb.L(a, b), lac = AC->pb.L(a, c), lbc = BC->pb.L(b, c);
                 if (!(lbc < lmax)) return;
-                const double uab = bAB.U(a, b), uac = bAC.U(a, c);
-                if (bin->tri_prune && !tri_triple_possible(*bin, lab, lac, lbc, uab, uac, bBC.U(b, c))) return;
+                const double uab = AB->pb.U(a, b), uac = AC->pb.U(a, c);
+                if (bin->tri_prune && !tri_triple_possible(*bin, lab, lac, lbc, uab, uac, BC->pb.U(b, c))) return;
                 if (uab >= lmax) flags |= TASK_CHECK_B;
                 if (uac >= lmax) flags |= TASK_CHECK_C;
             }
@@ -858,9 +970,9 @@ struct TripletPlan {
         if (tri && s.loop == TPCF_LOOP_SAME && sameAB && sameBC) {
             // i <= j <= k over one array: unordered distinct triples
             for (int a = a0; a < a1; a++)
-                for (int b : nAB[a]) {
+                for (int b : AB->nb[a]) {
                     if (b < a) continue;
-                    for (int c : nAC[a]) {
+                    for (int c : AC->nb[a]) {
                         if (c < b) continue;
                         uint32_t f = (a == b ? TASK_DIAG_IJ : 0) | (b == c ? TASK_DIAG_JK : 0);
                         add(a, b, c, PRED_NONE, f);
@@ -869,8 +981,8 @@ struct TripletPlan {
         } else if (tri && s.loop == TPCF_LOOP_ONE && sameBC) {
             // j <= k over one array (j == k has a zero side): unordered pairs
             for (int a = a0; a < a1; a++)
-                for (int b : nAB[a])
-                    for (int c : nAC[a]) {
+                for (int b : AB->nb[a])
+                    for (int c : AC->nb[a]) {
                         if (c < b) continue;
                         add(a, b, c, PRED_NONE, b == c ? TASK_DIAG_JK : 0);
                     }
@@ -878,16 +990,16 @@ struct TripletPlan {
             // every ordered (i, j) of one array, k >= j: unordered {i, j} with
             // weight [k >= i] + [k >= j]
             for (int a = a0; a < a1; a++)
-                for (int b : nAB[a]) {
+                for (int b : AB->nb[a]) {
                     if (b < a) continue;
-                    for (int c : nAC[a]) add(a, b, c, PRED_DDR, a == b ? TASK_DIAG_IJ : 0);
+                    for (int c : AC->nb[a]) add(a, b, c, PRED_DDR, a == b ? TASK_DIAG_IJ : 0);
                 }
         } else {
             uint32_t pred = PRED_NONE;
             if (tri) pred = s.loop == TPCF_LOOP_SAME ? PRED_SAME : s.loop == TPCF_LOOP_ONE ? PRED_ONE : PRED_NONE;
             for (int a = a0; a < a1; a++)
-                for (int b : nAB[a])
-                    for (int c : nAC[a]) add(a, b, c, pred, 0);
+                for (int b : AB->nb[a])
+                    for (int c : AC->nb[a]) add(a, b, c, pred, 0);
         }
     }
 };
@@ -915,26 +1027,87 @@ void plan_pairs(const tpcf_spec& sp, const PlannedJob& pj, uint32_t slot, double
         }
 }
 
-// Runs fn(item) for item in [0, n) on up to the host's cores.
-template <typename F>
-void parallel_items(size_t n, F&& fn) {
-    const size_t nth = std::min<size_t>(n, std::max(1u, std::thread::hardware_concurrency()));
-    std::atomic<size_t> next(0);
-    auto worker = [&](size_t t) {
-        for (;;) {
-            size_t i = next.fetch_add(1);
-            if (i >= n) break;
-            fn(i, t);
-        }
-    };
-    if (nth <= 1) {
-        worker(0);
-        return;
+// Host worker threads for planning, started once per process (thread
+// creation would cost more than the planning work of a small batch).  run()
+// calls fn(i) for i in [0, n) on the workers and the calling thread; a run
+// that finds the pool busy (another lane planning) does its items inline.
+class HostPool {
+  public:
+    static HostPool& get() {
+        static HostPool pool;
+        return pool;
     }
-    std::vector<std::thread> th;
-    for (size_t t = 0; t < nth; t++) th.emplace_back(worker, t);
-    for (auto& t : th) t.join();
-}
+    void run(size_t n, const std::function<void(size_t)>& fn) {
+        if (n == 0) return;
+        std::unique_lock<std::mutex> busy(run_mu_, std::try_to_lock);
+        if (!busy.owns_lock() || workers_.empty() || n == 1) {
+            for (size_t i = 0; i < n; i++) fn(i);
+            return;
+        }
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            job_ = &fn;
+            n_ = n;
+            next_ = 0;
+            done_ = 0;
+            gen_++;
+        }
+        cv_.notify_all();
+        work();
+        std::unique_lock<std::mutex> lk(mu_);
+        done_cv_.wait(lk, [&] { return done_ == workers_.size(); });
+        job_ = nullptr;
+    }
+    ~HostPool() {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (auto& t : workers_) t.join();
+    }
+
+  private:
+    HostPool() {
+        const unsigned n = std::max(1u, std::thread::hardware_concurrency()) - 1;
+        for (unsigned t = 0; t < n; t++) workers_.emplace_back([this] { loop(); });
+    }
+    void work() {
+        for (;;) {
+            size_t i = next_.fetch_add(1);
+            if (i >= n_) break;
+            (*job_)(i);
+        }
+    }
+    void loop() {
+        uint64_t seen = 0;
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
+                if (stop_) return;
+                seen = gen_;
+            }
+            work();
+            {
+                std::lock_guard<std::mutex> lk(mu_);
+                done_++;
+            }
+            done_cv_.notify_all();
+        }
+    }
+    std::mutex run_mu_, mu_;
+    std::condition_variable cv_, done_cv_;
+    std::vector<std::thread> workers_;
+    const std::function<void(size_t)>* job_ = nullptr;
+    size_t n_ = 0;
+    std::atomic<size_t> next_{0};
+    size_t done_ = 0;
+    uint64_t gen_ = 0;
+    bool stop_ = false;
+};
+
+void parallel_items(size_t n, const std::function<void(size_t)>& fn) { HostPool::get().run(n, fn); }
 
 size_t shape_smem(const tpcf_spec& sp, const Binning& bin, int copies) {
     if (sp.kind == TPCF_TRIANGLE || sp.kind == TPCF_TRIANGLE_JBJ) return triangle_smem_bytes(bin.len, copies);
@@ -1091,16 +1264,35 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
         // tile triples (pairs) by ranges of A tiles
         const bool pairs = sp.kind == TPCF_PAIR;
         std::vector<TripletPlan> tp(pairs ? 0 : group.size());
+        std::map<std::pair<const View*, const View*>, std::unique_ptr<PairTable>> tables;
+        std::vector<PairTable*> table_list;
         if (!pairs) {
-            for (size_t g = 0; g < group.size(); g++) tp[g].init(*group[g].spec, pj[g], (uint32_t)g, bin);
-            std::vector<std::array<int, 4>> items;  // job, which, row begin, row end
-            for (size_t g = 0; g < group.size(); g++)
-                for (int w = 0; w < 3; w++)
-                    for (int r = 0; r < tp[g].nrows(w); r += 16)
-                        items.push_back({(int)g, w, r, std::min(r + 16, tp[g].nrows(w))});
-            parallel_items(items.size(), [&](size_t i, size_t) {
+            auto table = [&](const View* x, const View* y, bool nb) {
+                auto& t = tables[std::make_pair(x, y)];
+                if (!t) {
+                    t.reset(new PairTable());
+                    t->init(*x, *y, bin.lmax);
+                    table_list.push_back(t.get());
+                }
+                if (nb && !t->need_nb) {
+                    t->need_nb = true;
+                    t->nb.assign(x->ntiles, {});
+                }
+                return t.get();
+            };
+            for (size_t g = 0; g < group.size(); g++) {
+                const View *A = pj[g].v[0].get(), *B = pj[g].v[1].get(), *C = pj[g].v[2].get();
+                const bool empty = A->ntiles == 0 || B->ntiles == 0 || C->ntiles == 0;
+                tp[g].init(*group[g].spec, pj[g], (uint32_t)g, bin, empty ? nullptr : table(A, B, true),
+                           empty ? nullptr : table(A, C, true), empty ? nullptr : table(B, C, false));
+            }
+            std::vector<std::array<int, 3>> items;  // table, row begin, row end
+            for (size_t t = 0; t < table_list.size(); t++)
+                for (int r = 0; r < table_list[t]->x->ntiles; r += 16)
+                    items.push_back({(int)t, r, std::min(r + 16, table_list[t]->x->ntiles)});
+            parallel_items(items.size(), [&](size_t i) {
                 const auto& it = items[i];
-                tp[it[0]].rows(it[1], it[2], it[3]);
+                table_list[it[0]]->rows(it[1], it[2]);
             });
         }
         std::vector<std::array<int, 3>> items;  // job, A-tile begin, end
@@ -1112,7 +1304,7 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
         // (a CTA flushes its shared histogram whenever the job changes)
         std::vector<TaskList> part(items.size());
         std::vector<uint64_t> part_eval(items.size(), 0);
-        parallel_items(items.size(), [&](size_t i, size_t) {
+        parallel_items(items.size(), [&](size_t i) {
             const auto& it = items[i];
             if (pairs)
                 plan_pairs(*group[it[0]].spec, pj[it[0]], (uint32_t)it[0], bin.lmax, it[1], it[2], part[i],
@@ -1120,21 +1312,30 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
             else
                 tp[it[0]].enumerate(it[1], it[2], part[i], part_eval[i]);
         });
-        // largest tasks first (dynamic fetch then balances the tail): a stable
-        // counting pass over 64 size classes (floor(log2(units)))
         size_t total = 0;
         for (size_t i = 0; i < part.size(); i++) {
             evaluated += part_eval[i];
             total += part[i].size();
         }
-        auto cls = [](uint64_t u) { return 63 - (u ? 63 - __builtin_clzll(u) : 0); };
-        std::vector<size_t> start(65, 0);
-        for (auto& pt : part)
-            for (auto& e : pt) start[cls(e.first) + 1]++;
-        for (int c = 0; c < 64; c++) start[c + 1] += start[c];
         std::vector<uint4> h_tasks(total);
-        for (auto& pt : part)
-            for (auto& e : pt) h_tasks[start[cls(e.first)]++] = e.second;
+        if (total <= (size_t)ctx->num_sms * 3 * 64) {
+            // few tasks per CTA: largest first, so that the dynamic fetch
+            // balances the tail (a stable counting pass over 64 size classes)
+            auto cls = [](uint64_t u) { return 63 - (u ? 63 - __builtin_clzll(u) : 0); };
+            std::vector<size_t> start(65, 0);
+            for (auto& pt : part)
+                for (auto& e : pt) start[cls(e.first) + 1]++;
+            for (int c = 0; c < 64; c++) start[c + 1] += start[c];
+            for (auto& pt : part)
+                for (auto& e : pt) h_tasks[start[cls(e.first)]++] = e.second;
+        } else {
+            // many tasks per CTA: the tail is a small share; job order
+            std::vector<size_t> off(part.size() + 1, 0);
+            for (size_t i = 0; i < part.size(); i++) off[i + 1] = off[i] + part[i].size();
+            parallel_items(part.size(), [&](size_t i) {
+                for (size_t e = 0; e < part[i].size(); e++) h_tasks[off[i] + e] = part[i][e].second;
+            });
+        }
         ntasks = h_tasks.size();
         L.d_jobs.reserve(dj.size());
         L.d_tasks.reserve(std::max<size_t>(h_tasks.size(), 1));
