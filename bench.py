@@ -288,12 +288,18 @@ def impl_reference(args):
 
 
 def traffic_per_launch():
-    p = os.path.join(ROOT, "profiles", "triangle_fast_tp10k.json")
-    if os.path.exists(p):
-        with open(p) as f:
-            j = json.load(f)
-        return j.get("dram_bytes_per_launch")
-    return None
+    """DRAM bytes (read + write) of one fast-kernel launch of this workload,
+    from the ncu capture summarised in profiles/."""
+    p = os.path.join(ROOT, "profiles", "triangle_fast_kernel_tp10k_dram.txt")
+    if not os.path.exists(p):
+        return None
+    total = 0
+    with open(p) as f:
+        for line in f:
+            parts = line.split()
+            if len(parts) == 2 and parts[0].startswith("dram__bytes_"):
+                total += int(parts[1])
+    return total
 
 
 def impl_ours(args):
