@@ -726,7 +726,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--config", default="tp10k", choices=["tp10k", "three1k", "voxel100k", "lattice500k", "serving"])
     ap.add_argument("--jobs", type=int, default=2000, help="serving: number of jobs")
-    ap.add_argument("--rate", type=float, default=50.0, help="serving: Poisson arrival rate (jobs/s)")
+    ap.add_argument("--rate", type=float, default=25.0, help="serving: Poisson arrival rate (jobs/s)")
     ap.add_argument("--fp64-full", action="store_true", help="lattice500k: FP64 comparison on all points")
     args = ap.parse_args()
     if args.warmup < 3:
