@@ -50,6 +50,8 @@ SANDBOX_GOLDENS = (
     + ["%s_Debbie_LRG_CPU_10degx10deg_LRG_binning_SLAC_1k.dat" % h for h in ("DDD", "DDR", "DRR", "RRR")]
     + ["%s_evenbinning_CPU_5degx5deg_LRG_binning_10k.dat" % h for h in ("DDD", "DDR", "DRR", "RRR")]
     + ["%s_evenbinning_CPU_20degx20deg_10k.dat" % h for h in ("DDD", "DDR", "DRR", "RRR")]
+    + ["DDD_voxel4_%03d%03d%03d_evenbinning_CPU_5degx5deg_LRG_binning_1k.dat" % (i, j, k)
+       for i in range(4) for j in range(4) for k in range(4)]
 )
 
 

@@ -119,6 +119,23 @@ def test_sandbox_voxel2(eng_x86, tmp_path, vox):
     assert rf.format_triangle(got, [len(cat)] * 3, SANDBOX_SPEC) == want
 
 
+def test_sandbox_voxel4(eng_x86, tmp_path):
+    """All 64 DDD_voxel4_* chunk files (an earlier revision: k starts at j+1),
+    as the current loop with the third chunk shifted by one point."""
+    eng = eng_x86
+    cat = _sandbox_cat(tmp_path, "MICE_5degx5deg_1k_randomized.dat")
+    h = eng.catalog(cat)
+    for i in range(4):
+        for j in range(4):
+            for k in range(4):
+                r = [rf.vox2gal(4, v, len(cat)) for v in (i, j, k)]
+                r[2] = (r[2][0] + 1, r[2][1])
+                got = eng.count(_tp_spec(SANDBOX_SPEC, tpcf.LOOP_SAME), eng.job([h, h, h], r))
+                name = "DDD_voxel4_%03d%03d%03d_evenbinning_CPU_5degx5deg_LRG_binning_1k.dat.gz" % (i, j, k)
+                assert rf.format_triangle(got, [len(cat)] * 3, SANDBOX_SPEC) == rf.read_bytes(os.path.join(SANDBOX, name))
+    eng.release(h)
+
+
 PROVENANCE = json.load(open(os.path.join(SANDBOX, "provenance.json")))["sets"]
 
 

@@ -35,6 +35,24 @@ def test_sandbox_voxel2_byte_exact(tmp_path, vox):
     assert got == want
 
 
+VOXEL4 = ["%03d%03d%03d" % (i, j, k) for i in range(4) for j in range(4) for k in range(4)]
+
+
+def test_sandbox_voxel4_byte_exact(tmp_path):
+    """examples/sandbox/DDD_voxel4_* (all 64 chunk triples of -X 4): made by a
+    revision whose same-file loop starts k at j+1; the current j >= i, k >= j
+    loop over the third chunk shifted by one point reproduces it."""
+    cat = sandbox_catalog(tmp_path, "MICE_5degx5deg_1k_randomized.dat")
+    for vox in VOXEL4:
+        idx = rf.voxel_indices(int(vox), 3)
+        r = [rf.vox2gal(4, idx[a], len(cat)) for a in range(3)]
+        subs = [cat[r[0][0]:r[0][1]], cat[r[1][0]:r[1][1]], cat[r[2][0] + 1:r[2][1]]]
+        hist, _ = oracle.triangle(subs, 0, SANDBOX_SPEC)
+        got = rf.format_triangle(hist, [len(cat)] * 3, SANDBOX_SPEC)
+        want = rf.read_bytes(os.path.join(SANDBOX, "DDD_voxel4_%s_evenbinning_CPU_5degx5deg_LRG_binning_1k.dat.gz" % vox))
+        assert got == want, vox
+
+
 def test_sandbox_lrg_full_ddd(tmp_path):
     """DDD_Debbie_LRG_..._1k.dat: full TP DDD on 1316 LRGs (3.8e8 triangles).
     The golden carries one extra trailing newline from sum_voxels.py's print."""
