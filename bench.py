@@ -287,19 +287,26 @@ def impl_reference(args):
     return 0
 
 
+def kernel_counters():
+    """ncu counters of one fast-kernel launch of this workload (committed
+    summary in profiles/): name -> value."""
+    p = os.path.join(ROOT, "profiles", "triangle_fast_kernel_tp10k_counters.txt")
+    out = {}
+    if os.path.exists(p):
+        with open(p) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) == 2 and not line.startswith("#"):
+                    out[parts[0]] = float(parts[1])
+    return out
+
+
 def traffic_per_launch():
-    """DRAM bytes (read + write) of one fast-kernel launch of this workload,
-    from the ncu capture summarised in profiles/."""
-    p = os.path.join(ROOT, "profiles", "triangle_fast_kernel_tp10k_dram.txt")
-    if not os.path.exists(p):
+    """DRAM bytes (read + write) of one fast-kernel launch, from ncu."""
+    c = kernel_counters()
+    if "dram__bytes_read.sum" not in c:
         return None
-    total = 0
-    with open(p) as f:
-        for line in f:
-            parts = line.split()
-            if len(parts) == 2 and parts[0].startswith("dram__bytes_"):
-                total += int(parts[1])
-    return total
+    return int(c["dram__bytes_read.sum"] + c.get("dram__bytes_write.sum", 0))
 
 
 def impl_ours(args):
@@ -413,6 +420,13 @@ def impl_ours(args):
         nsm = 152
     peak = nsm * 128 * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
     achieved = W_TP * binned / (statistics.mean(main_ms) / 1e3) / 1e12
+    # all lane instructions the kernel issues (ncu count of one launch) over
+    # this run's kernel time: how busy the issue slots are, useful or not
+    kc = kernel_counters()
+    issue_frac = None
+    if "smsp__inst_executed.sum" in kc:
+        lane_inst = kc["smsp__inst_executed.sum"] * kc.get("smsp__thread_inst_executed_per_inst_executed.ratio", 32.0)
+        issue_frac = lane_inst / (statistics.mean(main_ms) / 1e3) / 1e12 / peak
     cpu = None if args.no_cpu_baseline else cpu_baseline_single(d)
     csum = clocks.summary()
     line = {
@@ -435,7 +449,7 @@ def impl_ours(args):
         "plain_fp64": fp64,
         "zeta": zeta,
         "roofline": {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "Tinst/s",
-                     "frac": achieved / peak, "traffic": traffic_per_launch(),
+                     "frac": achieved / peak, "traffic": traffic_per_launch(), "issue_frac": issue_frac,
                      "kernel": "triangle_fast_kernel", "per_unit": "%d lane-instructions per binned triangle (one that reaches the s/q/theta arithmetic)" % W_TP,
                      "peak_source": "%d SMs x 128 lanes x sm_max_mhz (%s MEASURED_PEAKS)" % (nsm, peak_kind)},
         "cpu_baseline": cpu,
