@@ -821,6 +821,11 @@ AcosTable acos_table(tpcf_ctx* ctx) {
 struct PlannedJob {
     std::shared_ptr<View> v[3];
     uint64_t loop_units = 0;
+    // loop ONE with roles A == B (the D-D-R nest): counted in the role order
+    // (C, A, A), the single-array point first, so that points of C out of
+    // reach of a tile pair are skipped whole (guarded kernel, PRED_RDD)
+    bool swap = false;
+    const View* role(int r) const { return swap ? (r == 0 ? v[2].get() : v[0].get()) : v[r].get(); }
 };
 
 inline bool close_enough(const View& a, int ta, const View& b, int tb, double lmax) {
@@ -937,19 +942,19 @@ struct TripletPlan {
         pj = &p;
         bin = &b;
         slot = sl;
-        const View &A = *p.v[0], &B = *p.v[1], &C = *p.v[2];
+        const View &A = *p.role(0), &B = *p.role(1), &C = *p.role(2);
         empty = A.ntiles == 0 || B.ntiles == 0 || C.ntiles == 0;
         prune = b.lmax < INFINITY;
         tri = s.kind == TPCF_TRIANGLE || s.kind == TPCF_TRIANGLE_JBJ;
-        sameAB = p.v[0] == p.v[1];
-        sameBC = p.v[1] == p.v[2];
+        sameAB = p.role(0) == p.role(1);
+        sameBC = p.role(1) == p.role(2);
         AB = ab;
         AC = ac;
         BC = bc;
     }
     void enumerate(int a0, int a1, TaskList& tasks, uint64_t& evaluated) const {
         if (empty) return;  // a role without tiles: no triple (and no neighbour lists)
-        const View &A = *pj->v[0], &B = *pj->v[1], &C = *pj->v[2];
+        const View &A = *pj->role(0), &B = *pj->role(1), &C = *pj->role(2);
         const double lmax = bin->lmax;
         auto add = [&](int a, int b, int c, uint32_t pred, uint32_t flags) {
             if (prune) {
@@ -967,7 +972,16 @@ struct TripletPlan {
                                            (uint32_t)c)});
         };
         const tpcf_spec& s = *sp;
-        if (tri && s.loop == TPCF_LOOP_SAME && sameAB && sameBC) {
+        if (pj->swap) {
+            // roles (C, A, A) of a D-D-R job: each point of C with every
+            // unordered pair of the single array, weight [k_c >= j] + [k_c >= k]
+            for (int a = a0; a < a1; a++)
+                for (int b : AB->nb[a])
+                    for (int c : AC->nb[a]) {
+                        if (c < b) continue;
+                        add(a, b, c, PRED_RDD, b == c ? TASK_DIAG_JK : 0);
+                    }
+        } else if (tri && s.loop == TPCF_LOOP_SAME && sameAB && sameBC) {
             // i <= j <= k over one array: unordered distinct triples
             for (int a = a0; a < a1; a++)
                 for (int b : AB->nb[a]) {
@@ -1225,6 +1239,8 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
     // reuses its task list and device upload
     std::vector<uint64_t> sig;
     sig.push_back((uint64_t)(uintptr_t)L.d_hist.p);
+    const char* rdd_env = getenv("TPCF_RDD");
+    const bool rdd = !(rdd_env && rdd_env[0] == '0');
     for (size_t g = 0; g < group.size(); g++) {
         const tpcf_job& job = *group[g].job;
         const tpcf_spec& jsp = *group[g].spec;  // same binning as sp; the loop nest may differ
@@ -1237,11 +1253,15 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
         if (ncat == 2) pj[g].v[2] = pj[g].v[1];
         pj[g].loop_units = loop_units(jsp.kind, jsp.loop, n);
         units += pj[g].loop_units;
+        pj[g].swap = rdd && jsp.kind == TPCF_TRIANGLE && jsp.precision == TPCF_GUARDED_FP32 &&
+                     jsp.loop == TPCF_LOOP_ONE && pj[g].v[0] == pj[g].v[1] && pj[g].v[1] != pj[g].v[2];
         for (int r = 0; r < 3; r++) {
-            dj[g].pts[r] = pj[g].v[r]->pts.p;
-            dj[g].tile_start[r] = pj[g].v[r]->tile_start.p;
-            sig.push_back(pj[g].v[r]->id);
+            const View* rv = pj[g].role(r);
+            dj[g].pts[r] = rv->pts.p;
+            dj[g].tile_start[r] = rv->tile_start.p;
+            sig.push_back(rv->id);
         }
+        sig.push_back(pj[g].swap);
         dj[g].hist = L.d_hist.p + (size_t)bin.len * slot_of[g];
         sig.push_back(slot_of[g]);
         uint64_t f[6] = {(uint64_t)jsp.kind, (uint64_t)jsp.loop, (uint64_t)jsp.prune, (uint64_t)jsp.precision,
@@ -1281,7 +1301,7 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
                 return t.get();
             };
             for (size_t g = 0; g < group.size(); g++) {
-                const View *A = pj[g].v[0].get(), *B = pj[g].v[1].get(), *C = pj[g].v[2].get();
+                const View *A = pj[g].role(0), *B = pj[g].role(1), *C = pj[g].role(2);
                 const bool empty = A->ntiles == 0 || B->ntiles == 0 || C->ntiles == 0;
                 tp[g].init(*group[g].spec, pj[g], (uint32_t)g, bin, empty ? nullptr : table(A, B, true),
                            empty ? nullptr : table(A, C, true), empty ? nullptr : table(B, C, false));
@@ -1297,7 +1317,7 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
         }
         std::vector<std::array<int, 3>> items;  // job, A-tile begin, end
         for (size_t g = 0; g < group.size(); g++) {
-            const int na = pj[g].v[0]->ntiles, step = pairs ? 16 : 2;
+            const int na = pj[g].role(0)->ntiles, step = pairs ? 16 : 2;
             for (int a0 = 0; a0 < na; a0 += step) items.push_back({(int)g, a0, std::min(a0 + step, na)});
         }
         // one task list per item, so that the concatenation keeps job order

@@ -17,7 +17,9 @@ enum Pred : uint32_t {
     PRED_NONE = 0,   // every triple of the tile triple counts once
     PRED_DDR = 1,    // weight [key_k >= key_i] + [key_k >= key_j]  (loop ONE, roles A == B)
     PRED_SAME = 2,   // key_i <= key_j <= key_k                      (loop SAME, generic arrays)
-    PRED_ONE = 3     // key_j <= key_k                               (loop ONE, generic arrays)
+    PRED_ONE = 3,    // key_j <= key_k                               (loop ONE, generic arrays)
+    PRED_RDD = 4     // weight [key_i >= key_j] + [key_i >= key_k]   (loop ONE, roles A == B, in the
+                     // role order (C, A, A): the single-array point first; guarded kernel only)
 };
 // task.x: bits 0..21 job slot, 22..24 Pred, 28/29 diagonal flags, 30/31 reach checks
 constexpr uint32_t TASK_SLOT_MASK = 0x3FFFFFu;

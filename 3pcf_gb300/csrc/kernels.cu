@@ -618,8 +618,9 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
         const unsigned long long nM = ballot64(c0 == 3, c1 == 3), nH = ballot64(c0 == 4, c1 == 4);
         const unsigned long long any_k = nB | nI | nM | nH;
         if (!any_k) continue;  // no k within reach of i (warp-uniform)
-        unsigned long long kge_i = 0;
+        unsigned long long kge_i = 0;  // PRED_DDR: key_k >= key_i; PRED_RDD: key_k <= key_i
         if (PRED == PRED_DDR) kge_i = ballot64(lane < g.nC && key_k0 >= ki, lane + 32 < g.nC && key_k1 >= ki);
+        if (PRED == PRED_RDD) kge_i = ballot64(lane < g.nC && key_k0 <= ki, lane + 32 < g.nC && key_k1 <= ki);
         // i-j sides: words for the binning path; each lane then forms the
         // candidate-k mask of its own two j's (the scan over j is lane-parallel)
         // mask of candidate k's (and of weight-2 k's) of the pair (i, j)
@@ -636,7 +637,14 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
             if (!ok) return false;
             cm = candidate_mask(c, nB, nI, nM, nH, JM[j], JM[TILE + j], JM[2 * TILE + j], JM[3 * TILE + j]);
             if (diag_jk) cm &= j >= 63 ? 0ull : (~0ull << (j + 1));
-            if (PRED != PRED_NONE) {
+            if (PRED == PRED_RDD) {
+                // weight [key_j <= key_i] + [key_k <= key_i]
+                if (pkey(P[TILE + j]) <= ki) {
+                    w2 = cm & kge_i;
+                } else {
+                    cm &= kge_i;
+                }
+            } else if (PRED != PRED_NONE) {
                 const unsigned long long kge_j = JM[4 * TILE + j];
                 if (PRED == PRED_DDR) {
                     w2 = cm & kge_i & kge_j;  // weight 2: k >= i and k >= j
@@ -673,17 +681,17 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
                 const unsigned lo = __shfl_sync(0xffffffffu, (unsigned)cmv, src);
                 const unsigned hi = __shfl_sync(0xffffffffu, (unsigned)(cmv >> 32), src);
                 unsigned w2lo = 0, w2hi = 0;
-                if (PRED == PRED_DDR) {
+                if (PRED == PRED_DDR || PRED == PRED_RDD) {
                     w2lo = __shfl_sync(0xffffffffu, (unsigned)w2v, src);
                     w2hi = __shfl_sync(0xffffffffu, (unsigned)(w2v >> 32), src);
                 }
                 const int nlo = __popc(lo);
                 if ((lo >> lane) & 1u) {
-                    const unsigned w = PRED == PRED_DDR ? 1u + ((w2lo >> lane) & 1u) : 1u;
+                    const unsigned w = (PRED == PRED_DDR || PRED == PRED_RDD) ? 1u + ((w2lo >> lane) & 1u) : 1u;
                     cand[qn + __popc(lo & lt)] = pack_cand(j, lane, w);
                 }
                 if ((hi >> lane) & 1u) {
-                    const unsigned w = PRED == PRED_DDR ? 1u + ((w2hi >> lane) & 1u) : 1u;
+                    const unsigned w = (PRED == PRED_DDR || PRED == PRED_RDD) ? 1u + ((w2hi >> lane) & 1u) : 1u;
                     cand[qn + nlo + __popc(hi & lt)] = pack_cand(j, lane + 32, w);
                 }
                 qn += nlo + __popc(hi);
@@ -714,6 +722,7 @@ __device__ __forceinline__ void triangle_dispatch(const DevJob& J, uint4 task, c
     switch ((task.x >> TASK_PRED_SHIFT) & TASK_PRED_MASK) {
         case PRED_NONE: triangle_task_fast<PRED_NONE, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i); break;
         case PRED_DDR: triangle_task_fast<PRED_DDR, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i); break;
+        case PRED_RDD: triangle_task_fast<PRED_RDD, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i); break;
         case PRED_SAME: triangle_task_fast<PRED_SAME, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i); break;
         default: triangle_task_fast<PRED_ONE, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i); break;
     }
