@@ -821,11 +821,17 @@ AcosTable acos_table(tpcf_ctx* ctx) {
 struct PlannedJob {
     std::shared_ptr<View> v[3];
     uint64_t loop_units = 0;
-    // loop ONE with roles A == B (the D-D-R nest): counted in the role order
-    // (C, A, A), the single-array point first, so that points of C out of
-    // reach of a tile pair are skipped whole (guarded kernel, PRED_RDD)
-    bool swap = false;
-    const View* role(int r) const { return swap ? (r == 0 ? v[2].get() : v[0].get()) : v[r].get(); }
+    // Loop ONE jobs of two arrays are counted with the point of the array that
+    // appears once in role B or C and the pair array first, so that points
+    // out of reach of a tile are skipped whole (guarded kernel only):
+    //   swap 1, the D-D-R nest (A == B): roles (C, A, A), weight PRED_RDD;
+    //   swap 2, the D-R-R nest (B == C): roles (B, B, A), unordered pairs of B first.
+    int swap = 0;
+    const View* role(int r) const {
+        if (swap == 1) return r == 0 ? v[2].get() : v[0].get();
+        if (swap == 2) return r == 2 ? v[0].get() : v[1].get();
+        return v[r].get();
+    }
 };
 
 inline bool close_enough(const View& a, int ta, const View& b, int tb, double lmax) {
@@ -972,7 +978,7 @@ struct TripletPlan {
                                            (uint32_t)c)});
         };
         const tpcf_spec& s = *sp;
-        if (pj->swap) {
+        if (pj->swap == 1) {
             // roles (C, A, A) of a D-D-R job: each point of C with every
             // unordered pair of the single array, weight [k_c >= j] + [k_c >= k]
             for (int a = a0; a < a1; a++)
@@ -981,6 +987,14 @@ struct TripletPlan {
                         if (c < b) continue;
                         add(a, b, c, PRED_RDD, b == c ? TASK_DIAG_JK : 0);
                     }
+        } else if (pj->swap == 2) {
+            // roles (B, B, A) of a D-R-R job: every unordered pair of the pair
+            // array with each point of the other
+            for (int a = a0; a < a1; a++)
+                for (int b : AB->nb[a]) {
+                    if (b < a) continue;
+                    for (int c : AC->nb[a]) add(a, b, c, PRED_NONE, a == b ? TASK_DIAG_IJ : 0);
+                }
         } else if (tri && s.loop == TPCF_LOOP_SAME && sameAB && sameBC) {
             // i <= j <= k over one array: unordered distinct triples
             for (int a = a0; a < a1; a++)
@@ -1253,8 +1267,11 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
         if (ncat == 2) pj[g].v[2] = pj[g].v[1];
         pj[g].loop_units = loop_units(jsp.kind, jsp.loop, n);
         units += pj[g].loop_units;
-        pj[g].swap = rdd && jsp.kind == TPCF_TRIANGLE && jsp.precision == TPCF_GUARDED_FP32 &&
-                     jsp.loop == TPCF_LOOP_ONE && pj[g].v[0] == pj[g].v[1] && pj[g].v[1] != pj[g].v[2];
+        pj[g].swap = 0;
+        if (rdd && jsp.kind == TPCF_TRIANGLE && jsp.precision == TPCF_GUARDED_FP32 && jsp.loop == TPCF_LOOP_ONE) {
+            if (pj[g].v[0] == pj[g].v[1] && pj[g].v[1] != pj[g].v[2]) pj[g].swap = 1;
+            else if (pj[g].v[1] == pj[g].v[2] && pj[g].v[0] != pj[g].v[1]) pj[g].swap = 2;
+        }
         for (int r = 0; r < 3; r++) {
             const View* rv = pj[g].role(r);
             dj[g].pts[r] = rv->pts.p;
