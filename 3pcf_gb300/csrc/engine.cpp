@@ -691,7 +691,6 @@ struct tpcf_ctx {
     std::string last_error;
     uint64_t next_handle = 1;
     std::map<uint64_t, std::shared_ptr<Catalog>> catalogs;
-    std::map<uint64_t, std::shared_ptr<DevBuf<float4>>> cat_dev;  // unsorted points (resident)
     // (catalog, begin, end, tile points, global loop indices) -> view
     std::map<std::tuple<uint64_t, int64_t, int64_t, int, bool>, std::shared_ptr<View>> views;
     int tile_points = TILE;  // points per spatial tile (<= TILE)
@@ -1822,7 +1821,6 @@ tpcf_status tpcf_destroy(tpcf_ctx* ctx) {
         std::lock_guard<std::recursive_mutex> vlk(ctx->view_mu);
         cudaSetDevice(ctx->device);
         ctx->views.clear();
-        ctx->cat_dev.clear();
         for (auto& L : ctx->lanes) L->release();
         ctx->acos_keys.release();
         ctx->acos_vals.release();
@@ -1864,7 +1862,6 @@ tpcf_status tpcf_catalog_release(tpcf_ctx* ctx, uint64_t handle) {
     std::lock_guard<std::recursive_mutex> vlk(ctx->view_mu);
     if (!ctx->catalogs.count(handle)) return fail(ctx, TPCF_ERR_NOT_FOUND, "unknown catalog handle");
     ctx->catalogs.erase(handle);
-    ctx->cat_dev.erase(handle);
     for (auto it = ctx->views.begin(); it != ctx->views.end();) {
         if (std::get<0>(it->first) == handle) it = ctx->views.erase(it);
         else ++it;
