@@ -111,3 +111,28 @@ def test_radecz_conversion_matches_script():
     assert ulp.max() <= 1
     assert (ulp == 0).mean() > 0.9999
     assert np.allclose(other, convert_ref.radecz_to_xyz(ra[:10], dec[:10], zr[:10], (0.0, 1000.0, 0.0)), rtol=1e-6)
+
+
+@pytest.mark.gpu
+def test_count_batch_into_mixed_kinds():
+    """Jobs of different kinds and binnings in one call (one launch each):
+    every output gets the sum of its own jobs."""
+    d = synth.blobs(900, n_blobs=3, sigma=5.0, box=50.0, seed=19)
+    r = synth.uniform(800, box=50.0, seed=20)
+    with tpcf.Engine(0) as eng:
+        hd, hr = eng.catalog(d), eng.catalog(r)
+        tp = tpcf.make_spec(tpcf.TRIANGLE, tpcf.LOOP_SAME, TP)
+        tp1 = tpcf.make_spec(tpcf.TRIANGLE, tpcf.LOOP_ONE, TP)
+        jbj = tpcf.make_spec(tpcf.TRIANGLE_JBJ, tpcf.LOOP_SAME, [(10, 1.0, 11.0), (8, 0.2, 1.0), (10, 0.0, 1.0)])
+        pr = tpcf.make_spec(tpcf.PAIR, tpcf.LOOP_SAME, [(100, 0.0, 50.0)])
+        specs = [tp, tp1, jbj, pr, pr, tp]
+        jobs = [eng.job([hd, hd, hd]), eng.job([hd, hd, hr]), eng.job([hd, hd, hd]), eng.job([hd, hd]),
+                eng.job([hr, hr]), eng.job([hr, hr, hr])]
+        outs = [0, 0, 1, 2, 2, 3]
+        got = eng.count_batch_into(specs, jobs, outs, 4)
+        single = [eng.count(s, j) for s, j in zip(specs, jobs)]
+        assert np.array_equal(got[0], single[0] + single[1])
+        assert np.array_equal(got[1], single[2])
+        assert np.array_equal(got[2], single[3] + single[4])
+        assert np.array_equal(got[3], single[5])
+        assert all(g.sum() > 0 for g in got)
