@@ -674,11 +674,14 @@ struct GroupJob {
 }  // namespace
 
 // Launch shape of a persistent kernel: warp-private histogram copies in
-// shared memory (0: count straight into the 64-bit global histogram) and
-// resident CTAs per SM (the grid is that many per SM).
+// shared memory (0: count straight into the 64-bit global histogram),
+// resident CTAs per SM (the grid is that many per SM) and, for the
+// three-side kernel, task pipelines per CTA (0: plain 8-warp CTAs; g > 0:
+// one CTA per SM of g 8-warp pipelines around one large histogram).
 struct Shape {
     int copies = 1;
     int per_sm = 1;
+    int groups = 0;
     size_t smem = 0;
 };
 
@@ -1136,9 +1139,9 @@ class HostPool {
 
 void parallel_items(size_t n, const std::function<void(size_t)>& fn) { HostPool::get().run(n, fn); }
 
-size_t shape_smem(const tpcf_spec& sp, const Binning& bin, int copies) {
+size_t shape_smem(const tpcf_spec& sp, const Binning& bin, int copies, int groups) {
     if (sp.kind == TPCF_TRIANGLE || sp.kind == TPCF_TRIANGLE_JBJ) return triangle_smem_bytes(bin.len, copies);
-    if (sp.kind == TPCF_THREE_SIDE) return three_side_smem_bytes(copies ? bin.len : 0, copies);
+    if (sp.kind == TPCF_THREE_SIDE) return three_side_smem_bytes(copies ? bin.len : 0, copies, groups);
     return pair_smem_bytes(bin.len, copies);
 }
 
@@ -1149,10 +1152,11 @@ std::vector<Shape> shape_candidates(tpcf_ctx* ctx, const tpcf_spec& sp, const Bi
     int max_smem_sm = 0, max_smem_block = 0;
     cudaDeviceGetAttribute(&max_smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx->device);
     cudaDeviceGetAttribute(&max_smem_block, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
-    auto fit = [&](int copies, int cap_per_sm) {
+    auto fit = [&](int copies, int cap_per_sm, int groups = 0) {
         Shape sh;
         sh.copies = copies;
-        sh.smem = shape_smem(sp, bin, copies);
+        sh.groups = groups;
+        sh.smem = shape_smem(sp, bin, copies, groups);
         sh.per_sm = 0;
         if (sh.smem + 1024 > (size_t)max_smem_block) return sh;  // leaves room for the kernels' static shared memory
         sh.per_sm = std::min(cap_per_sm, (int)(max_smem_sm / (sh.smem + 1024)));
@@ -1162,7 +1166,7 @@ std::vector<Shape> shape_candidates(tpcf_ctx* ctx, const tpcf_spec& sp, const Bi
     auto add = [&](Shape sh) {
         if (sh.per_sm < 1) return;
         for (const Shape& o : out)
-            if (o.copies == sh.copies && o.per_sm == sh.per_sm) return;
+            if (o.copies == sh.copies && o.per_sm == sh.per_sm && o.groups == sh.groups) return;
         out.push_back(sh);
     };
     if (sp.kind == TPCF_TRIANGLE || sp.kind == TPCF_TRIANGLE_JBJ) {
@@ -1177,8 +1181,9 @@ std::vector<Shape> shape_candidates(tpcf_ctx* ctx, const tpcf_spec& sp, const Bi
             for (int cc : {4, 2, 1}) add(fit(cc, tri_per_sm));
         if (out.empty()) throw InvalidArg{"triangle histogram too large for shared memory"};
     } else if (sp.kind == TPCF_THREE_SIDE) {
-        // default: the most copies that still leave four CTAs per SM, else the
-        // global histogram
+        // default: the most copies that still leave four 8-warp CTAs per SM,
+        // else one CTA per SM of as many pipelines (up to four) as fit
+        // around one shared histogram, else the global histogram
         Shape def;
         def.copies = -1;
         for (int cc : {4, 2, 1}) {
@@ -1188,9 +1193,13 @@ std::vector<Shape> shape_candidates(tpcf_ctx* ctx, const tpcf_spec& sp, const Bi
                 break;
             }
         }
-        if (def.copies < 0) def = fit(0, 8);
+        int groups = 4;
+        while (groups > 1 && fit(1, 1, groups).per_sm < 1) groups--;
+        if (def.copies < 0) def = fit(1, 1, groups);
+        if (def.per_sm < 1) def = fit(0, 8);
         add(def);
         for (int cc : {8, 4, 2, 1, 0}) add(fit(cc, 8));
+        add(fit(1, 1, groups));
     } else {
         Shape def;
         def.copies = -1;
@@ -1438,7 +1447,7 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
                     EQ(cudaEventRecordWithFlags(L.ev_mid, st, ev_flags));
                 } else if (sp.kind == TPCF_THREE_SIDE) {
                     EQ(launch_three_side(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.three, fp64, grid, copies,
-                                         st));
+                                         sh.groups, st));
                     EQ(cudaEventRecordWithFlags(L.ev_mid, st, ev_flags));
                 } else {
                     EQ(launch_pairs(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.pair, fp64, grid, copies, st));
@@ -1461,7 +1470,7 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
                                           (uint64_t)(uintptr_t)L.h_hist.p, (uint64_t)(uintptr_t)L.h_counters.p,
                                           (uint64_t)(uintptr_t)acos_t.keys, (uint64_t)(uintptr_t)acos_t.vals,
                                           (uint64_t)(uintptr_t)acos_t.bucket, (uint64_t)acos_t.n, queue_cap,
-                                          (uint64_t)grid, (uint64_t)copies, hist_total, ntasks};
+                                          (uint64_t)grid, (uint64_t)copies, (uint64_t)sh.groups, hist_total, ntasks};
                 gsig.insert(gsig.end(), extra, extra + sizeof(extra) / sizeof(extra[0]));
                 if (!L.graph || gsig != L.graph_sig) {
                     L.drop_graph();

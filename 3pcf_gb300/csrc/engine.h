@@ -132,7 +132,7 @@ cudaError_t launch_triangle_fp64(const DevJob* jobs, const uint4* tasks, unsigne
                                  int hist_copies, int mode, cudaStream_t st);  // mode: 0 FP64, 1 geometry, 2 JBJ
 cudaError_t launch_three_side(const DevJob* jobs, const uint4* tasks, unsigned int ntasks,
                               unsigned int* task_counter, const ThreeParams& p, int fp64, int grid,
-                              int hist_copies, cudaStream_t st);
+                              int hist_copies, int groups, cudaStream_t st);
 cudaError_t launch_pairs(const DevJob* jobs, const uint4* tasks, unsigned int ntasks,
                          unsigned int* task_counter, const PairParams& p, int fp64, int grid,
                          int hist_copies, cudaStream_t st);
@@ -143,10 +143,9 @@ cudaError_t launch_radecz_to_xyz(const double* ra, const double* dec, const doub
 
 // shared-memory bytes of a launch (for occupancy / admission)
 size_t triangle_smem_bytes(int hist_len, int hist_copies);
-size_t three_side_smem_bytes(int hist_len, int hist_copies);
+size_t three_side_smem_bytes(int hist_len, int hist_copies, int groups);
 size_t pair_smem_bytes(int hist_len, int hist_copies);
 int triangle_block_threads();
-int three_side_block_threads();
 int pair_block_threads();
 
 }  // namespace tpcf

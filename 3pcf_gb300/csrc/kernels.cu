@@ -232,13 +232,25 @@ __device__ void tp_geom(double d0, double d1, double d2, const TriParams& p, int
 constexpr unsigned int FLUSH_EVERY = 256;  // tasks between histogram flushes (u32 safety)
 constexpr uint32_t TASK_NONE = 0xFFFFFFFFu;
 
+// Swizzled shared histograms: bin b of a copy lives at word hist_pos(b), its
+// low five bits (the bank) XORed with the next two 5-bit groups, so that the
+// lanes of one atomic instruction whose bins differ only in higher digits
+// (n^2 i2 + n i1 + i0 with n = 32 puts every lane of a three-side row in one
+// bank) spread over the banks.  It permutes each aligned group of 32 words;
+// copies are hist_stride(len) words apart.
+__host__ __device__ constexpr int hist_stride(int len) { return (len + 31) & ~31; }
+__device__ __forceinline__ unsigned hist_pos(unsigned b) { return b ^ (((b >> 5) ^ (b >> 10)) & 31u); }
+
+template <bool SWZ = false>
 __device__ __forceinline__ void flush_hist(unsigned int* H, int copies, int len, unsigned long long* g) {
     __syncthreads();
+    const int stride = SWZ ? hist_stride(len) : len;
     for (int b = threadIdx.x; b < len; b += blockDim.x) {
+        const int at = SWZ ? (int)hist_pos((unsigned)b) : b;
         unsigned long long sum = 0;
         for (int c = 0; c < copies; c++) {
-            sum += H[c * len + b];
-            H[c * len + b] = 0;
+            sum += H[c * stride + at];
+            H[c * stride + at] = 0;
         }
         if (sum) atomicAdd(g + b, sum);
     }
@@ -948,11 +960,26 @@ triangle_fp64_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ 
 // Three-side histogram (src/3pcf_C_version.cc): every ordered triple, sides in
 // source order d01 -> i0, d02 -> i1, d12 -> i2, index n^2 i2 + n i1 + i0.
 
-constexpr int TS_WARPS = 8;
-constexpr int TS_THREADS = TS_WARPS * 32;
-constexpr size_t TS_SMEM_FIXED = 3 * TILE * sizeof(float4) + TILE * TILE * sizeof(uint32_t) +
-                                 TS_WARPS * TILE * sizeof(uint32_t);
+constexpr int TS_WARPS = 8;  // warps per CTA, or per group of the grouped kernel
+constexpr int TS_GROUP_THREADS = TS_WARPS * 32;
+constexpr int TS_GROUPS_MAX = 4;
 constexpr uint32_t TS_FAR = 1u << 30;
+// A copy receives at most 64^3 = 2^18 counts per task, so 8192 tasks keep
+// every 32-bit shared counter below 2^31.
+constexpr unsigned int TS_FLUSH_EVERY = 8192;
+
+// Per warp: the i-k and i-j code rows of its point i and a queue of (j, k)
+// candidates (up to 31 left over plus 64 from one j).
+constexpr int TS_QCAP = 96;
+constexpr int TS_ROW = 2 * TILE + TS_QCAP;
+
+// Shared memory of one task pipeline (an 8-warp CTA, or one group of the
+// grouped kernel): point tiles, j-k codes, per-warp rows, j-k masks, boxes.
+constexpr size_t TS_OFF_JK = 3 * TILE * sizeof(float4);
+constexpr size_t TS_OFF_ROWS = TS_OFF_JK + TILE * TILE * sizeof(uint32_t);
+constexpr size_t TS_OFF_JKM = TS_OFF_ROWS + TS_WARPS * TS_ROW * sizeof(uint32_t);
+constexpr size_t TS_OFF_BOX = TS_OFF_JKM + TILE * sizeof(unsigned long long);
+constexpr size_t TS_PIPE_BYTES = (TS_OFF_BOX + 36 * sizeof(float) + 127) & ~(size_t)127;
 
 // distance_to_bin of src/3pcf_C_version.cc:23-51, times 'scale'; sides at or
 // above hist_max give nbins+1 (reference) or, in clean mode, a value that
@@ -965,19 +992,102 @@ __device__ __forceinline__ uint32_t side_code3(float d, const ThreeParams& p, ui
     return (uint32_t)__float2int_rz(F::div(F::sub(d, p.lo), p.bw)) * scale;
 }
 
+// One task pipeline: its threads (tid in [0, 256)), and its barrier (0: the
+// CTA's, else a named barrier of its 256 threads).
+struct TsPipe {
+    int tid, warp, lane, bar;
+    __device__ __forceinline__ void sync() const {
+        if (bar == 0) __syncthreads();
+        else asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(TS_GROUP_THREADS) : "memory");
+    }
+};
+
+// Bounding boxes of the three tiles (two 32-point halves each) into BX, one
+// warp per half; the caller synchronises.
+__device__ __forceinline__ void tile_boxes(const float4* P, const TaskGeom& g, float* BX, int warp, int lane) {
+    if (warp >= 6) return;
+    const int role = warp >> 1, idx = (warp & 1) * 32 + lane;
+    const int n = role == 0 ? g.nA : (role == 1 ? g.nB : g.nC);
+    const float4 pt = P[role * TILE + idx];
+    const bool valid = idx < n;
+    float lo[3] = {valid ? pt.x : INFINITY, valid ? pt.y : INFINITY, valid ? pt.z : INFINITY};
+    float hi[3] = {valid ? pt.x : -INFINITY, valid ? pt.y : -INFINITY, valid ? pt.z : -INFINITY};
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+            hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+        }
+    if (lane == 0) {
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            BX[warp * 6 + a] = lo[a];
+            BX[warp * 6 + 3 + a] = hi[a];
+        }
+    }
+}
+
+// True if every point of tile 'role' is at least 'reach' from pt (squared
+// distance to the tile's bounding box against reach^2).
+__device__ __forceinline__ bool far_from_tile(const float* BX, float4 pt, int role, float reach2) {
+    const float* b0 = BX + role * 12;
+    float s2 = 0.f;
+    {
+        const float lo = fminf(b0[0], b0[6]), hi = fmaxf(b0[3], b0[9]);
+        const float gap = fmaxf(0.f, fmaxf(lo - pt.x, pt.x - hi));
+        s2 = fmaf(gap, gap, s2);
+    }
+    {
+        const float lo = fminf(b0[1], b0[7]), hi = fmaxf(b0[4], b0[10]);
+        const float gap = fmaxf(0.f, fmaxf(lo - pt.y, pt.y - hi));
+        s2 = fmaf(gap, gap, s2);
+    }
+    {
+        const float lo = fminf(b0[2], b0[8]), hi = fmaxf(b0[5], b0[11]);
+        const float gap = fmaxf(0.f, fmaxf(lo - pt.z, pt.z - hi));
+        s2 = fmaf(gap, gap, s2);
+    }
+    return s2 >= reach2;
+}
+
+// One task (tiles A, B, C) of the three-side histogram on one pipeline whose
+// shared memory starts at 'base'; counts go to the shared copy Hw (swizzled)
+// or, with GLOBAL_HIST, straight to the job's 64-bit histogram.
 template <bool FP64, bool GLOBAL_HIST>
-__device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& p, float4* P, uint32_t* JK,
-                                uint32_t* IJ, unsigned long long* JKM, unsigned int* Hw) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+__device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& p, unsigned char* base,
+                                unsigned int* Hw, const TsPipe& pp) {
+    float4* P = reinterpret_cast<float4*>(base);
+    uint32_t* JK = reinterpret_cast<uint32_t*>(base + TS_OFF_JK);
+    uint32_t* ROWS = reinterpret_cast<uint32_t*>(base + TS_OFF_ROWS);
+    unsigned long long* JKM = reinterpret_cast<unsigned long long*>(base + TS_OFF_JKM);
+    float* BX = reinterpret_cast<float*>(base + TS_OFF_BOX);
+    const int warp = pp.warp, lane = pp.lane;
     const TaskGeom g = task_geom(J, task);
     const uint32_t n = p.n, n2 = (uint32_t)p.n * p.n, len = (uint32_t)p.len;
-    load_points(P, J, g);
-    __syncthreads();
+    for (int t = pp.tid; t < 3 * TILE; t += TS_GROUP_THREADS) {
+        const int role = t / TILE, idx = t % TILE;
+        const int nr = role == 0 ? g.nA : (role == 1 ? g.nB : g.nC);
+        const int b0 = role == 0 ? g.a0 : (role == 1 ? g.b0 : g.c0);
+        P[t] = idx < nr ? J.pts[role][b0 + idx] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    pp.sync();
     if (p.clean) {
+        // Clean mode drops every triple with a side >= hist_max, so a point
+        // farther than that from a whole tile takes no part in the task (the
+        // 1e-5 margin covers the rounding of the bound and of the distance).
+        const bool chk_b = task.x & TASK_CHECK_B, chk_c = task.x & TASK_CHECK_C;
+        if (chk_b || chk_c) tile_boxes(P, g, BX, warp, lane);
+        pp.sync();
+        const float reach = p.hi * (1.0f + 1e-5f), reach2 = reach * reach;
         // j-k codes, one warp per row j, and JKM[j]: the k's whose side is
-        // below hist_max (clean mode drops every triple with a longer side)
+        // below hist_max
         for (int j = warp; j < g.nB; j += TS_WARPS) {
             const float4 pj = P[TILE + j];
+            if (chk_b && far_from_tile(BX, pj, 0, reach2)) {  // no i reaches j: the row is never read
+                if (lane == 0) JKM[j] = 0ull;
+                continue;
+            }
             uint32_t c0 = TS_FAR, c1 = TS_FAR;
             if (lane < g.nC) c0 = side_code3<FP64>(ref_dist<FP64>(pj, P[2 * TILE + lane]), p, n2);
             if (lane + 32 < g.nC) c1 = side_code3<FP64>(ref_dist<FP64>(pj, P[2 * TILE + lane + 32]), p, n2);
@@ -986,15 +1096,82 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
             const unsigned long long m = ballot64(c0 < TS_FAR, c1 < TS_FAR);
             if (lane == 0) JKM[j] = m;
         }
-    } else {
-        for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
-            const int j = e / TILE, k = e % TILE;
-            JK[e] = (j < g.nB && k < g.nC) ? side_code3<FP64>(ref_dist<FP64>(P[TILE + j], P[2 * TILE + k]), p, n2)
-                                           : TS_FAR;
+        pp.sync();
+        uint32_t* row_ik = ROWS + warp * TS_ROW;
+        uint32_t* row_ij = row_ik + TILE;
+        uint32_t* cq = row_ij + TILE;
+        const unsigned lt = (1u << lane) - 1u;
+        auto count_candidates = [&](const uint32_t* e, int m) {
+            if (lane < m) {
+                const uint32_t c = e[lane];
+                const int j = c & 63, k = c >> 6;
+                const uint32_t idx = JK[j * TILE + k] + row_ik[k] + row_ij[j];
+                if (idx < len) {  // a side rounded to bin nbins aliases as in the reference
+                    if (GLOBAL_HIST) atomicAdd(J.hist + idx, 1ull);
+                    else atomicAdd(Hw + hist_pos(idx), 1u);
+                }
+            }
+        };
+        for (int i = warp; i < g.nA; i += TS_WARPS) {
+            const float4 pi = P[i];
+            if ((chk_b && far_from_tile(BX, pi, 1, reach2)) || (chk_c && far_from_tile(BX, pi, 2, reach2)))
+                continue;  // warp-uniform
+            uint32_t cik[2], cij[2];
+#pragma unroll
+            for (int r = 0; r < 2; r++) {
+                const int k = lane + 32 * r;
+                cik[r] = k < g.nC ? side_code3<FP64>(ref_dist<FP64>(pi, P[2 * TILE + k]), p, n) : TS_FAR;
+            }
+            const unsigned long long mk = ballot64(cik[0] < TS_FAR, cik[1] < TS_FAR);
+            if (!mk) continue;  // warp-uniform
+            // j's with a usable i-j side and a k usable with both i and j
+            bool vj[2];
+#pragma unroll
+            for (int r = 0; r < 2; r++) {
+                const int j = lane + 32 * r;
+                cij[r] = TS_FAR;
+                vj[r] = false;
+                if (j < g.nB && (JKM[j] & mk)) {
+                    cij[r] = side_code3<FP64>(ref_dist<FP64>(pi, P[TILE + j]), p, 1u);
+                    vj[r] = cij[r] < TS_FAR;
+                }
+            }
+            unsigned long long mj = ballot64(vj[0], vj[1]);
+            // Candidates (j, k) of this i, every j in turn, queued by the
+            // whole warp and counted 32 at a time.
+            row_ik[lane] = cik[0];
+            row_ik[lane + 32] = cik[1];
+            row_ij[lane] = cij[0];
+            row_ij[lane + 32] = cij[1];
+            int qn = 0;  // warp-uniform
+            while (mj) {
+                const int j = __ffsll((long long)mj) - 1;
+                mj &= mj - 1ull;
+                const unsigned long long cm = mk & JKM[j];
+                const unsigned lo = (unsigned)cm, hi = (unsigned)(cm >> 32);
+                const int nlo = __popc(lo);
+                if ((lo >> lane) & 1u) cq[qn + __popc(lo & lt)] = (uint32_t)j | ((uint32_t)lane << 6);
+                if ((hi >> lane) & 1u) cq[qn + nlo + __popc(hi & lt)] = (uint32_t)j | ((uint32_t)(lane + 32) << 6);
+                qn += nlo + __popc(hi);
+                __syncwarp();
+                while (qn >= 32) {
+                    qn -= 32;
+                    count_candidates(cq + qn, 32);
+                    __syncwarp();
+                }
+            }
+            if (qn > 0) count_candidates(cq, qn);
+            __syncwarp();
         }
+        return;
     }
-    __syncthreads();
-    uint32_t* row = IJ + warp * TILE;
+    for (int e = pp.tid; e < TILE * TILE; e += TS_GROUP_THREADS) {
+        const int j = e / TILE, k = e % TILE;
+        JK[e] = (j < g.nB && k < g.nC) ? side_code3<FP64>(ref_dist<FP64>(P[TILE + j], P[2 * TILE + k]), p, n2)
+                                       : TS_FAR;
+    }
+    pp.sync();
+    uint32_t* row = ROWS + warp * TS_ROW;
     for (int i = warp; i < g.nA; i += TS_WARPS) {
         const float4 pi = P[i];
         uint32_t cik[2];
@@ -1003,9 +1180,6 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
             const int k = lane + 32 * r;
             cik[r] = k < g.nC ? side_code3<FP64>(ref_dist<FP64>(pi, P[2 * TILE + k]), p, n) : TS_FAR;
         }
-        // k's whose i-k side can count (clean mode drops sides >= hist_max)
-        const unsigned long long mk = p.clean ? ballot64(cik[0] < TS_FAR, cik[1] < TS_FAR) : ~0ull;
-        if (!mk) continue;  // warp-uniform
 #pragma unroll
         for (int r = 0; r < 2; r++) {
             const int k = lane + 32 * r;
@@ -1015,14 +1189,13 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
 #pragma unroll 4
         for (int j = 0; j < g.nB; j++) {
             const uint32_t cij = row[j];
-            if (p.clean && (cij >= TS_FAR || !(mk & JKM[j]))) continue;  // warp-uniform
 #pragma unroll
             for (int r = 0; r < 2; r++) {
                 const int k = lane + 32 * r;
                 const uint32_t idx = JK[j * TILE + k] + cik[r] + cij;
                 if (idx < len) {
                     if (GLOBAL_HIST) atomicAdd(J.hist + idx, 1ull);
-                    else atomicAdd(Hw + idx, 1u);
+                    else atomicAdd(Hw + hist_pos(idx), 1u);
                 }
             }
         }
@@ -1030,20 +1203,19 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
     }
 }
 
+// 8-warp CTAs, several per SM: warp-private shared histogram copies (copies
+// > 0) or the global histogram.
 template <bool FP64, bool GLOBAL_HIST>
-__global__ void __launch_bounds__(TS_THREADS)
+__global__ void __launch_bounds__(TS_GROUP_THREADS)
 three_side_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ tasks, unsigned int ntasks,
                   unsigned int* task_counter, ThreeParams p, int copies) {
     extern __shared__ __align__(16) unsigned char smem[];
-    float4* P = reinterpret_cast<float4*>(smem);
-    uint32_t* JK = reinterpret_cast<uint32_t*>(smem + 3 * TILE * sizeof(float4));
-    uint32_t* IJ = JK + TILE * TILE;
-    unsigned int* H = IJ + TS_WARPS * TILE;
-    __shared__ unsigned long long s_jkm[TILE];
+    unsigned int* H = reinterpret_cast<unsigned int*>(smem + TS_PIPE_BYTES);
     __shared__ uint4 s_task;
     if (!GLOBAL_HIST)
-        for (int b = threadIdx.x; b < copies * p.len; b += blockDim.x) H[b] = 0;
-    unsigned int* Hw = H + (GLOBAL_HIST ? 0 : ((threadIdx.x >> 5) % copies) * p.len);
+        for (int b = threadIdx.x; b < copies * hist_stride(p.len); b += blockDim.x) H[b] = 0;
+    unsigned int* Hw = H + (GLOBAL_HIST ? 0 : ((threadIdx.x >> 5) % copies) * hist_stride(p.len));
+    const TsPipe pp{(int)threadIdx.x, (int)(threadIdx.x >> 5), (int)(threadIdx.x & 31), 0};
     int cur = -1;
     unsigned int since = 0;
     for (;;) {
@@ -1055,14 +1227,71 @@ three_side_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ tas
         __syncthreads();
         const uint4 task = s_task;
         const int slot = task.x == TASK_NONE ? -1 : (int)(task.x & TASK_SLOT_MASK);
-        if (!GLOBAL_HIST && (slot != cur || since >= 64) && cur >= 0) {
-            flush_hist(H, copies, p.len, jobs[cur].hist);
+        if (!GLOBAL_HIST && (slot != cur || since >= TS_FLUSH_EVERY) && cur >= 0) {
+            flush_hist<true>(H, copies, p.len, jobs[cur].hist);
             since = 0;
         }
         cur = slot;
         if (slot < 0) break;
         since++;
-        three_side_task<FP64, GLOBAL_HIST>(jobs[slot], task, p, P, JK, IJ, s_jkm, Hw);
+        three_side_task<FP64, GLOBAL_HIST>(jobs[slot], task, p, smem, Hw, pp);
+    }
+}
+
+// One CTA per SM of 'groups' independent 8-warp task pipelines (named
+// barriers 1..groups) around one shared histogram too large for several
+// CTAs per SM.  A pipeline runs tasks of the current job until it draws a
+// task of another job (or none), or the CTA has run TS_FLUSH_EVERY tasks since
+// the last flush; then it waits for the others at a CTA barrier, where the
+// histogram is flushed and the next current job is the smallest one held.
+// Every pipeline reaches that barrier: each runs finitely many tasks of the
+// current job.  At most TS_FLUSH_EVERY + groups - 1 tasks are counted between
+// two flushes, each at most 2^18 per bin, so the 32-bit counters cannot wrap.
+template <bool FP64>
+__global__ void __launch_bounds__(TS_GROUPS_MAX * TS_GROUP_THREADS, 1)
+three_side_grouped_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ tasks, unsigned int ntasks,
+                          unsigned int* task_counter, ThreeParams p, int groups) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    unsigned int* H = reinterpret_cast<unsigned int*>(smem + (size_t)groups * TS_PIPE_BYTES);
+    __shared__ uint4 s_task[TS_GROUPS_MAX];
+    __shared__ unsigned int s_stop[TS_GROUPS_MAX];  // the pipeline leaves the job to flush
+    __shared__ unsigned int s_since;                // tasks run since the last flush
+    const int gi = threadIdx.x / TS_GROUP_THREADS, gt = threadIdx.x % TS_GROUP_THREADS;
+    const TsPipe pp{gt, gt >> 5, gt & 31, 1 + gi};
+    unsigned char* base = smem + (size_t)gi * TS_PIPE_BYTES;
+    for (int b = threadIdx.x; b < hist_stride(p.len); b += blockDim.x) H[b] = 0;
+    if (threadIdx.x == 0) s_since = 0;
+    auto draw = [&]() {
+        if (gt == 0) {
+            unsigned int t = atomicAdd(task_counter, 1u);
+            s_task[gi] = t < ntasks ? tasks[t] : make_uint4(TASK_NONE, 0, 0, 0);
+        }
+    };
+    draw();
+    int cur = -1;
+    for (;;) {
+        __syncthreads();  // every pipeline waits here with a task of another job, or none
+        if (cur >= 0) flush_hist<true>(H, 1, p.len, jobs[cur].hist);
+        uint32_t next = TASK_NONE;
+        for (int g2 = 0; g2 < groups; g2++) {
+            const uint32_t x = s_task[g2].x;
+            if (x != TASK_NONE) next = min(next, x & TASK_SLOT_MASK);
+        }
+        if (next == TASK_NONE) break;  // uniform: every thread read the same words
+        if (threadIdx.x < TS_GROUPS_MAX) s_stop[threadIdx.x] = 0;
+        if (threadIdx.x == 0) s_since = 0;
+        __syncthreads();
+        cur = (int)next;
+        for (;;) {
+            // s_task[gi] and s_stop[gi] change only between this pipeline's barriers
+            const uint4 task = s_task[gi];
+            if (task.x == TASK_NONE || (int)(task.x & TASK_SLOT_MASK) != cur || s_stop[gi]) break;
+            three_side_task<FP64, false>(jobs[cur], task, p, base, H, pp);
+            pp.sync();  // the pipeline is done with s_task[gi] and its buffers
+            if (gt == 0) s_stop[gi] = atomicAdd(&s_since, 1u) + 1 >= TS_FLUSH_EVERY;
+            draw();
+            pp.sync();
+        }
     }
 }
 
@@ -1151,10 +1380,13 @@ __global__ void acos_check_kernel(AcosTable t, uint32_t key_begin, uint32_t coun
 // Launchers
 
 size_t triangle_smem_bytes(int hist_len, int copies) { return TRI_SMEM_FIXED + (size_t)hist_len * copies * 4; }
-size_t three_side_smem_bytes(int hist_len, int copies) { return TS_SMEM_FIXED + (size_t)hist_len * copies * 4; }
+size_t three_side_smem_bytes(int hist_len, int copies, int groups) {
+    // groups > 0: the grouped kernel (one histogram); else 8-warp CTAs with 'copies' copies
+    if (groups > 0) return (size_t)groups * TS_PIPE_BYTES + (size_t)hist_stride(hist_len) * 4;
+    return TS_PIPE_BYTES + (size_t)hist_stride(hist_len) * copies * 4;
+}
 size_t pair_smem_bytes(int hist_len, int copies) { return PR_SMEM_FIXED + (size_t)hist_len * copies * 4; }
 int triangle_block_threads() { return TRI_THREADS; }
-int three_side_block_threads() { return TS_THREADS; }
 int pair_block_threads() { return PR_THREADS; }
 
 // Every counting kernel may use the device's whole opt-in shared memory per
@@ -1169,7 +1401,8 @@ cudaError_t prepare_kernels(int device) {
                          (const void*)triangle_fp64_kernel<MODE_FP64>, (const void*)triangle_fp64_kernel<MODE_GEOM>,
                          (const void*)triangle_fp64_kernel<MODE_JBJ>, (const void*)three_side_kernel<true, true>,
                          (const void*)three_side_kernel<true, false>, (const void*)three_side_kernel<false, true>,
-                         (const void*)three_side_kernel<false, false>, (const void*)pair_kernel<true>,
+                         (const void*)three_side_kernel<false, false>, (const void*)three_side_grouped_kernel<true>,
+                         (const void*)three_side_grouped_kernel<false>, (const void*)pair_kernel<true>,
                          (const void*)pair_kernel<false>};
     for (const void* f : fns) {
         cudaFuncAttributes fa;
@@ -1212,11 +1445,21 @@ cudaError_t launch_triangle_fp64(const DevJob* jobs, const uint4* tasks, unsigne
 
 cudaError_t launch_three_side(const DevJob* jobs, const uint4* tasks, unsigned int ntasks,
                               unsigned int* task_counter, const ThreeParams& p, int fp64, int grid, int copies,
-                              cudaStream_t st) {
+                              int groups, cudaStream_t st) {
+    if (groups > 0) {
+        if (groups > TS_GROUPS_MAX) return cudaErrorInvalidValue;
+        const size_t smem = three_side_smem_bytes(p.len, 1, groups);
+        const int threads = groups * TS_GROUP_THREADS;
+        if (fp64)
+            three_side_grouped_kernel<true><<<grid, threads, smem, st>>>(jobs, tasks, ntasks, task_counter, p, groups);
+        else
+            three_side_grouped_kernel<false><<<grid, threads, smem, st>>>(jobs, tasks, ntasks, task_counter, p, groups);
+        return cudaGetLastError();
+    }
     const bool global = copies == 0;
-    size_t smem = three_side_smem_bytes(global ? 0 : p.len, global ? 0 : copies);
+    const size_t smem = three_side_smem_bytes(global ? 0 : p.len, global ? 0 : copies, 0);
 #define TS_LAUNCH(FP, GL) \
-    three_side_kernel<FP, GL><<<grid, TS_THREADS, smem, st>>>(jobs, tasks, ntasks, task_counter, p, copies > 0 ? copies : 1);
+    three_side_kernel<FP, GL><<<grid, TS_GROUP_THREADS, smem, st>>>(jobs, tasks, ntasks, task_counter, p, copies > 0 ? copies : 1);
     if (fp64) {
         if (global) { TS_LAUNCH(true, true) } else { TS_LAUNCH(true, false) }
     } else {

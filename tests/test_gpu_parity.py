@@ -297,6 +297,27 @@ def test_three_side_vs_oracle(eng, overflow, axis):
     eng.release(hr)
 
 
+@pytest.mark.parametrize("axis", [(32, 0.0, 32.0), (24, 2.0, 20.0), (12, 0.0, 36.0)])
+def test_three_side_clean_spread_catalog(eng, axis):
+    """Clean three-side mode on a catalog much wider than the largest side
+    (most tile triples and most points of a tile are out of reach, 30 % of the
+    points on the integer lattice): every launch shape the autotuner tries
+    (32-warp CTAs around one large histogram, the global histogram, 8-warp
+    CTAs) and the FP64 kernel give the oracle's counts."""
+    pts = synth.lattice_mix(1500, box=150.0, frac=0.3, seed=41)
+    h = eng.catalog(pts)
+    job = eng.job([h, h, h])
+    want, n = oracle.three_side([pts, pts, pts], axis[1], axis[2], axis[0], clean=True)
+    assert want.sum() > 0
+    for prec in (tpcf.GUARDED_FP32, tpcf.PLAIN_FP64):
+        s = tpcf.make_spec(tpcf.THREE_SIDE, tpcf.LOOP_ALL, [axis], precision=prec, overflow=tpcf.OVERFLOW_CLEAN)
+        for _ in range(4):  # the repeated batch is autotuned over the candidate shapes
+            got = eng.count(s, job)
+            assert np.array_equal(got, want)
+            assert eng.stats()["loop_units"] == n
+    eng.release(h)
+
+
 @pytest.mark.parametrize("axis", [(700, 0.0, 70.0), (40, 1.0, 21.0)])
 def test_pairs_vs_oracle(eng, axis):
     d = synth.blobs(3000, n_blobs=10, sigma=5.0, box=100.0, seed=41)
