@@ -451,6 +451,45 @@ float ref_bw(float lo, float hi, int n) {
     return r;
 }
 
+// The three-side bin of a side whose squared length (as the reference sums
+// it) is d2: distance_to_bin of src/3pcf_C_version.cc:23-51 on sqrtf(d2),
+// nbins + 1 standing for d >= hist_max.  IEEE single operations, as on the
+// device.
+static int three_side_bin_of_d2(float d2, float lo, float hi, float bw, int n) {
+    volatile float d = sqrtf(d2);
+    if (d < lo) return 0;
+    if (d >= hi) return n + 1;
+    volatile float x = d - lo;
+    volatile float q = x / bw;
+    return (int)q;
+}
+
+// Thresholds u[v] (smallest float d2 >= 0 with bin >= v) by bisection over
+// the ordered bit patterns of non-negative floats; the bin is a
+// non-decreasing function of d2 (sqrt, subtraction, division and truncation
+// all are).  Returns false where the first guess inv_bw * (sqrt(d2) - lo)
+// might be off by more than one bin (very fine binnings).
+static bool three_side_thresholds(ThreeParams& p) {
+    if (p.n + 3 > TS_UMAX) return false;
+    if (std::max(fabs((double)p.lo), fabs((double)p.hi)) / (double)p.bw > 16384.0) return false;
+    p.inv_bw = 1.0f / p.bw;
+    p.u[0] = -INFINITY;
+    for (int v = 1; v <= p.n + 1; v++) {
+        uint32_t lo = 0, hi = 0x7F800000u;  // +0 .. +inf (bin nbins + 1)
+        while (lo < hi) {
+            const uint32_t mid = lo + (hi - lo) / 2;
+            float x;
+            memcpy(&x, &mid, 4);
+            if (three_side_bin_of_d2(x, p.lo, p.hi, p.bw, p.n) >= v) hi = mid;
+            else lo = mid + 1;
+        }
+        memcpy(&p.u[v], &lo, 4);
+    }
+    p.u[p.n + 2] = NAN;
+    for (int v = p.n + 3; v < TS_UMAX; v++) p.u[v] = NAN;
+    return true;
+}
+
 Binning make_binning(const tpcf_spec& sp) {
     Binning b;
     b.kind = sp.kind;
@@ -470,6 +509,8 @@ Binning make_binning(const tpcf_spec& sp) {
         p.len = p.n * p.n * p.n;
         b.len = p.len;
         if (p.clean) b.lmax = (double)p.hi * (1 + 1e-6);
+        // (compat mode counts every triple: the side codes are a small part of its work)
+        p.fast = p.clean && three_side_thresholds(p) ? 1 : 0;
     } else if (sp.kind == TPCF_TRIANGLE) {
         for (int a = 0; a < 3; a++) check_axis(sp.axis[a], "triangle axis");
         TriParams& p = b.tri;

@@ -88,11 +88,20 @@ struct TriParams {
                                  // permutation 1 needs all three below it
 };
 
+constexpr int TS_UMAX = 68;  // squared-length thresholds of up to 64 bins
+
 struct ThreeParams {
     int n;                       // nbins
     float lo, hi, bw;
     int clean;
     int len;                     // n^3
+    // Side codes from squared lengths (guarded FP32 kernel, when fast != 0):
+    // u[v] is the smallest float d2 whose reference bin sqrt(d2) -> v' has
+    // v' >= v (v' = nbins + 1 for d >= hi), u[0] = -inf, u[nbins + 2] = NaN;
+    // inv_bw ~ 1/bw gives a first guess within one bin of the answer.
+    int fast;
+    float inv_bw;
+    float u[TS_UMAX];
 };
 
 struct PairParams {

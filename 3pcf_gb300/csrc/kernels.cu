@@ -979,7 +979,8 @@ constexpr size_t TS_OFF_JK = 3 * TILE * sizeof(float4);
 constexpr size_t TS_OFF_ROWS = TS_OFF_JK + TILE * TILE * sizeof(uint32_t);
 constexpr size_t TS_OFF_JKM = TS_OFF_ROWS + TS_WARPS * TS_ROW * sizeof(uint32_t);
 constexpr size_t TS_OFF_BOX = TS_OFF_JKM + TILE * sizeof(unsigned long long);
-constexpr size_t TS_PIPE_BYTES = (TS_OFF_BOX + 36 * sizeof(float) + 127) & ~(size_t)127;
+constexpr size_t TS_OFF_NEXT = TS_OFF_BOX + 36 * sizeof(float);  // next point i of the task
+constexpr size_t TS_PIPE_BYTES = (TS_OFF_NEXT + sizeof(int) + 127) & ~(size_t)127;
 
 // distance_to_bin of src/3pcf_C_version.cc:23-51, times 'scale'; sides at or
 // above hist_max give nbins+1 (reference) or, in clean mode, a value that
@@ -990,6 +991,30 @@ __device__ __forceinline__ uint32_t side_code3(float d, const ThreeParams& p, ui
     if (d < p.lo) return 0u;
     if (d >= p.hi) return p.clean ? TS_FAR : (uint32_t)(p.n + 1) * scale;
     return (uint32_t)__float2int_rz(F::div(F::sub(d, p.lo), p.bw)) * scale;
+}
+
+// Three-side code of the side a-b.  The guarded FP32 kernel skips the square
+// root and the division: the bin is a non-decreasing step function of the
+// squared length, so a first guess from an approximate square root (within one
+// bin) is corrected against the exact thresholds U of the two neighbouring
+// steps.  The plain FP64 kernel evaluates the reference's formula.
+template <bool FP64>
+__device__ __forceinline__ uint32_t side_code3_pts(float4 a, float4 b, const ThreeParams& p, const float* U,
+                                                   uint32_t scale) {
+    if (!FP64 && p.fast) {
+        const float dx = __fsub_rn(a.x, b.x), dy = __fsub_rn(a.y, b.y), dz = __fsub_rn(a.z, b.z);
+        float d2 = __fmul_rn(dx, dx);
+        d2 = __fadd_rn(d2, __fmul_rn(dy, dy));
+        d2 = __fadd_rn(d2, __fmul_rn(dz, dz));
+        float da;
+        asm("sqrt.approx.f32 %0, %1;" : "=f"(da) : "f"(d2));
+        int v = __float2int_rz(__fmul_rn(__fsub_rn(da, p.lo), p.inv_bw));
+        v = min(max(v, 0), p.n + 1);
+        v = v - 1 + (d2 >= U[v] ? 1 : 0) + (d2 >= U[v + 1] ? 1 : 0);
+        if (v > p.n) return p.clean ? TS_FAR : (uint32_t)(p.n + 1) * scale;
+        return (uint32_t)v * scale;
+    }
+    return side_code3<FP64>(ref_dist<FP64>(a, b), p, scale);
 }
 
 // One task pipeline: its threads (tid in [0, 256)), and its barrier (0: the
@@ -1055,13 +1080,14 @@ __device__ __forceinline__ bool far_from_tile(const float* BX, float4 pt, int ro
 // shared memory starts at 'base'; counts go to the shared copy Hw (swizzled)
 // or, with GLOBAL_HIST, straight to the job's 64-bit histogram.
 template <bool FP64, bool GLOBAL_HIST>
-__device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& p, unsigned char* base,
-                                unsigned int* Hw, const TsPipe& pp) {
+__device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& p, const float* U,
+                                unsigned char* base, unsigned int* Hw, const TsPipe& pp) {
     float4* P = reinterpret_cast<float4*>(base);
     uint32_t* JK = reinterpret_cast<uint32_t*>(base + TS_OFF_JK);
     uint32_t* ROWS = reinterpret_cast<uint32_t*>(base + TS_OFF_ROWS);
     unsigned long long* JKM = reinterpret_cast<unsigned long long*>(base + TS_OFF_JKM);
     float* BX = reinterpret_cast<float*>(base + TS_OFF_BOX);
+    int* next_i = reinterpret_cast<int*>(base + TS_OFF_NEXT);
     const int warp = pp.warp, lane = pp.lane;
     const TaskGeom g = task_geom(J, task);
     const uint32_t n = p.n, n2 = (uint32_t)p.n * p.n, len = (uint32_t)p.len;
@@ -1071,6 +1097,7 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
         const int b0 = role == 0 ? g.a0 : (role == 1 ? g.b0 : g.c0);
         P[t] = idx < nr ? J.pts[role][b0 + idx] : make_float4(0.f, 0.f, 0.f, 0.f);
     }
+    if (pp.tid == 0) *next_i = 0;
     pp.sync();
     if (p.clean) {
         // Clean mode drops every triple with a side >= hist_max, so a point
@@ -1089,8 +1116,8 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
                 continue;
             }
             uint32_t c0 = TS_FAR, c1 = TS_FAR;
-            if (lane < g.nC) c0 = side_code3<FP64>(ref_dist<FP64>(pj, P[2 * TILE + lane]), p, n2);
-            if (lane + 32 < g.nC) c1 = side_code3<FP64>(ref_dist<FP64>(pj, P[2 * TILE + lane + 32]), p, n2);
+            if (lane < g.nC) c0 = side_code3_pts<FP64>(pj, P[2 * TILE + lane], p, U, n2);
+            if (lane + 32 < g.nC) c1 = side_code3_pts<FP64>(pj, P[2 * TILE + lane + 32], p, U, n2);
             JK[j * TILE + lane] = c0;
             JK[j * TILE + lane + 32] = c1;
             const unsigned long long m = ballot64(c0 < TS_FAR, c1 < TS_FAR);
@@ -1112,7 +1139,12 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
                 }
             }
         };
-        for (int i = warp; i < g.nA; i += TS_WARPS) {
+        for (;;) {
+            // points of tile A go to warps one at a time (their work is uneven)
+            int i = 0;
+            if (lane == 0) i = atomicAdd(next_i, 1);
+            i = __shfl_sync(0xffffffffu, i, 0);
+            if (i >= g.nA) break;
             const float4 pi = P[i];
             if ((chk_b && far_from_tile(BX, pi, 1, reach2)) || (chk_c && far_from_tile(BX, pi, 2, reach2)))
                 continue;  // warp-uniform
@@ -1120,7 +1152,7 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
 #pragma unroll
             for (int r = 0; r < 2; r++) {
                 const int k = lane + 32 * r;
-                cik[r] = k < g.nC ? side_code3<FP64>(ref_dist<FP64>(pi, P[2 * TILE + k]), p, n) : TS_FAR;
+                cik[r] = k < g.nC ? side_code3_pts<FP64>(pi, P[2 * TILE + k], p, U, n) : TS_FAR;
             }
             const unsigned long long mk = ballot64(cik[0] < TS_FAR, cik[1] < TS_FAR);
             if (!mk) continue;  // warp-uniform
@@ -1132,7 +1164,7 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
                 cij[r] = TS_FAR;
                 vj[r] = false;
                 if (j < g.nB && (JKM[j] & mk)) {
-                    cij[r] = side_code3<FP64>(ref_dist<FP64>(pi, P[TILE + j]), p, 1u);
+                    cij[r] = side_code3_pts<FP64>(pi, P[TILE + j], p, U, 1u);
                     vj[r] = cij[r] < TS_FAR;
                 }
             }
@@ -1167,7 +1199,7 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
     }
     for (int e = pp.tid; e < TILE * TILE; e += TS_GROUP_THREADS) {
         const int j = e / TILE, k = e % TILE;
-        JK[e] = (j < g.nB && k < g.nC) ? side_code3<FP64>(ref_dist<FP64>(P[TILE + j], P[2 * TILE + k]), p, n2)
+        JK[e] = (j < g.nB && k < g.nC) ? side_code3_pts<FP64>(P[TILE + j], P[2 * TILE + k], p, U, n2)
                                        : TS_FAR;
     }
     pp.sync();
@@ -1178,12 +1210,12 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
 #pragma unroll
         for (int r = 0; r < 2; r++) {
             const int k = lane + 32 * r;
-            cik[r] = k < g.nC ? side_code3<FP64>(ref_dist<FP64>(pi, P[2 * TILE + k]), p, n) : TS_FAR;
+            cik[r] = k < g.nC ? side_code3_pts<FP64>(pi, P[2 * TILE + k], p, U, n) : TS_FAR;
         }
 #pragma unroll
         for (int r = 0; r < 2; r++) {
             const int k = lane + 32 * r;
-            if (k < g.nB) row[k] = side_code3<FP64>(ref_dist<FP64>(pi, P[TILE + k]), p, 1u);
+            if (k < g.nB) row[k] = side_code3_pts<FP64>(pi, P[TILE + k], p, U, 1u);
         }
         __syncwarp();
 #pragma unroll 4
@@ -1212,6 +1244,8 @@ three_side_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ tas
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned int* H = reinterpret_cast<unsigned int*>(smem + TS_PIPE_BYTES);
     __shared__ uint4 s_task;
+    __shared__ float s_u[TS_UMAX];
+    for (int v = threadIdx.x; v < TS_UMAX; v += blockDim.x) s_u[v] = p.u[v];
     if (!GLOBAL_HIST)
         for (int b = threadIdx.x; b < copies * hist_stride(p.len); b += blockDim.x) H[b] = 0;
     unsigned int* Hw = H + (GLOBAL_HIST ? 0 : ((threadIdx.x >> 5) % copies) * hist_stride(p.len));
@@ -1234,7 +1268,7 @@ three_side_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ tas
         cur = slot;
         if (slot < 0) break;
         since++;
-        three_side_task<FP64, GLOBAL_HIST>(jobs[slot], task, p, smem, Hw, pp);
+        three_side_task<FP64, GLOBAL_HIST>(jobs[slot], task, p, s_u, smem, Hw, pp);
     }
 }
 
@@ -1256,6 +1290,8 @@ three_side_grouped_kernel(const DevJob* __restrict__ jobs, const uint4* __restri
     __shared__ uint4 s_task[TS_GROUPS_MAX];
     __shared__ unsigned int s_stop[TS_GROUPS_MAX];  // the pipeline leaves the job to flush
     __shared__ unsigned int s_since;                // tasks run since the last flush
+    __shared__ float s_u[TS_UMAX];
+    for (int v = threadIdx.x; v < TS_UMAX; v += blockDim.x) s_u[v] = p.u[v];
     const int gi = threadIdx.x / TS_GROUP_THREADS, gt = threadIdx.x % TS_GROUP_THREADS;
     const TsPipe pp{gt, gt >> 5, gt & 31, 1 + gi};
     unsigned char* base = smem + (size_t)gi * TS_PIPE_BYTES;
@@ -1286,7 +1322,7 @@ three_side_grouped_kernel(const DevJob* __restrict__ jobs, const uint4* __restri
             // s_task[gi] and s_stop[gi] change only between this pipeline's barriers
             const uint4 task = s_task[gi];
             if (task.x == TASK_NONE || (int)(task.x & TASK_SLOT_MASK) != cur || s_stop[gi]) break;
-            three_side_task<FP64, false>(jobs[cur], task, p, base, H, pp);
+            three_side_task<FP64, false>(jobs[cur], task, p, s_u, base, H, pp);
             pp.sync();  // the pipeline is done with s_task[gi] and its buffers
             if (gt == 0) s_stop[gi] = atomicAdd(&s_since, 1u) + 1 >= TS_FLUSH_EVERY;
             draw();
