@@ -1182,7 +1182,7 @@ void parallel_items(size_t n, const std::function<void(size_t)>& fn) { HostPool:
 
 size_t shape_smem(const tpcf_spec& sp, const Binning& bin, int copies, int groups) {
     if (sp.kind == TPCF_TRIANGLE || sp.kind == TPCF_TRIANGLE_JBJ) return triangle_smem_bytes(bin.len, copies);
-    if (sp.kind == TPCF_THREE_SIDE) return three_side_smem_bytes(copies ? bin.len : 0, copies, groups);
+    if (sp.kind == TPCF_THREE_SIDE) return three_side_smem_bytes(bin.three, copies, groups);
     return pair_smem_bytes(bin.len, copies);
 }
 

@@ -974,13 +974,22 @@ constexpr int TS_QCAP = 96;
 constexpr int TS_ROW = 2 * TILE + TS_QCAP;
 
 // Shared memory of one task pipeline (an 8-warp CTA, or one group of the
-// grouped kernel): point tiles, j-k codes, per-warp rows, j-k masks, boxes.
-constexpr size_t TS_OFF_JK = 3 * TILE * sizeof(float4);
-constexpr size_t TS_OFF_ROWS = TS_OFF_JK + TILE * TILE * sizeof(uint32_t);
-constexpr size_t TS_OFF_JKM = TS_OFF_ROWS + TS_WARPS * TS_ROW * sizeof(uint32_t);
-constexpr size_t TS_OFF_BOX = TS_OFF_JKM + TILE * sizeof(unsigned long long);
-constexpr size_t TS_OFF_NEXT = TS_OFF_BOX + 36 * sizeof(float);  // next point i of the task
-constexpr size_t TS_PIPE_BYTES = (TS_OFF_NEXT + sizeof(int) + 127) & ~(size_t)127;
+// grouped kernel): point tiles, j-k table, per-warp rows, j-k masks, boxes,
+// next point.  The j-k table holds 32-bit codes; in clean mode it holds the
+// bins alone (only sides below hist_max are ever read), one byte each up to
+// 255 bins.
+struct TsLayout {
+    size_t jk, rows, jkm, box, next, bytes;
+};
+__host__ __device__ constexpr bool ts_byte_jk(const ThreeParams& p) { return p.clean && p.n <= 255; }
+__host__ __device__ constexpr TsLayout ts_layout(bool byte_jk) {
+    const size_t jk = 3 * TILE * sizeof(float4);
+    const size_t rows = jk + (byte_jk ? TILE * TILE : TILE * TILE * sizeof(uint32_t));
+    const size_t jkm = rows + TS_WARPS * TS_ROW * sizeof(uint32_t);
+    const size_t box = jkm + TILE * sizeof(unsigned long long);
+    const size_t next = box + 36 * sizeof(float);
+    return TsLayout{jk, rows, jkm, box, next, (next + sizeof(int) + 127) & ~(size_t)127};
+}
 
 // distance_to_bin of src/3pcf_C_version.cc:23-51, times 'scale'; sides at or
 // above hist_max give nbins+1 (reference) or, in clean mode, a value that
@@ -1083,11 +1092,14 @@ template <bool FP64, bool GLOBAL_HIST>
 __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& p, const float* U,
                                 unsigned char* base, unsigned int* Hw, const TsPipe& pp) {
     float4* P = reinterpret_cast<float4*>(base);
-    uint32_t* JK = reinterpret_cast<uint32_t*>(base + TS_OFF_JK);
-    uint32_t* ROWS = reinterpret_cast<uint32_t*>(base + TS_OFF_ROWS);
-    unsigned long long* JKM = reinterpret_cast<unsigned long long*>(base + TS_OFF_JKM);
-    float* BX = reinterpret_cast<float*>(base + TS_OFF_BOX);
-    int* next_i = reinterpret_cast<int*>(base + TS_OFF_NEXT);
+    const bool byte_jk = ts_byte_jk(p);
+    const TsLayout L = ts_layout(byte_jk);
+    uint32_t* JK = reinterpret_cast<uint32_t*>(base + L.jk);
+    uint8_t* JK8 = base + L.jk;
+    uint32_t* ROWS = reinterpret_cast<uint32_t*>(base + L.rows);
+    unsigned long long* JKM = reinterpret_cast<unsigned long long*>(base + L.jkm);
+    float* BX = reinterpret_cast<float*>(base + L.box);
+    int* next_i = reinterpret_cast<int*>(base + L.next);
     const int warp = pp.warp, lane = pp.lane;
     const TaskGeom g = task_geom(J, task);
     const uint32_t n = p.n, n2 = (uint32_t)p.n * p.n, len = (uint32_t)p.len;
@@ -1116,10 +1128,15 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
                 continue;
             }
             uint32_t c0 = TS_FAR, c1 = TS_FAR;
-            if (lane < g.nC) c0 = side_code3_pts<FP64>(pj, P[2 * TILE + lane], p, U, n2);
-            if (lane + 32 < g.nC) c1 = side_code3_pts<FP64>(pj, P[2 * TILE + lane + 32], p, U, n2);
-            JK[j * TILE + lane] = c0;
-            JK[j * TILE + lane + 32] = c1;
+            if (lane < g.nC) c0 = side_code3_pts<FP64>(pj, P[2 * TILE + lane], p, U, 1u);
+            if (lane + 32 < g.nC) c1 = side_code3_pts<FP64>(pj, P[2 * TILE + lane + 32], p, U, 1u);
+            if (byte_jk) {  // bins <= nbins <= 255 where read
+                JK8[j * TILE + lane] = (uint8_t)c0;
+                JK8[j * TILE + lane + 32] = (uint8_t)c1;
+            } else {
+                JK[j * TILE + lane] = c0;
+                JK[j * TILE + lane + 32] = c1;
+            }
             const unsigned long long m = ballot64(c0 < TS_FAR, c1 < TS_FAR);
             if (lane == 0) JKM[j] = m;
         }
@@ -1132,7 +1149,8 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
             if (lane < m) {
                 const uint32_t c = e[lane];
                 const int j = c & 63, k = c >> 6;
-                const uint32_t idx = JK[j * TILE + k] + row_ik[k] + row_ij[j];
+                const uint32_t jk = byte_jk ? (uint32_t)JK8[j * TILE + k] : JK[j * TILE + k];
+                const uint32_t idx = jk * n2 + row_ik[k] + row_ij[j];
                 if (idx < len) {  // a side rounded to bin nbins aliases as in the reference
                     if (GLOBAL_HIST) atomicAdd(J.hist + idx, 1ull);
                     else atomicAdd(Hw + hist_pos(idx), 1u);
@@ -1242,7 +1260,7 @@ __global__ void __launch_bounds__(TS_GROUP_THREADS)
 three_side_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ tasks, unsigned int ntasks,
                   unsigned int* task_counter, ThreeParams p, int copies) {
     extern __shared__ __align__(16) unsigned char smem[];
-    unsigned int* H = reinterpret_cast<unsigned int*>(smem + TS_PIPE_BYTES);
+    unsigned int* H = reinterpret_cast<unsigned int*>(smem + ts_layout(ts_byte_jk(p)).bytes);
     __shared__ uint4 s_task;
     __shared__ float s_u[TS_UMAX];
     for (int v = threadIdx.x; v < TS_UMAX; v += blockDim.x) s_u[v] = p.u[v];
@@ -1286,7 +1304,8 @@ __global__ void __launch_bounds__(TS_GROUPS_MAX * TS_GROUP_THREADS, 1)
 three_side_grouped_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ tasks, unsigned int ntasks,
                           unsigned int* task_counter, ThreeParams p, int groups) {
     extern __shared__ __align__(16) unsigned char smem[];
-    unsigned int* H = reinterpret_cast<unsigned int*>(smem + (size_t)groups * TS_PIPE_BYTES);
+    const size_t pipe_bytes = ts_layout(ts_byte_jk(p)).bytes;
+    unsigned int* H = reinterpret_cast<unsigned int*>(smem + (size_t)groups * pipe_bytes);
     __shared__ uint4 s_task[TS_GROUPS_MAX];
     __shared__ unsigned int s_stop[TS_GROUPS_MAX];  // the pipeline leaves the job to flush
     __shared__ unsigned int s_since;                // tasks run since the last flush
@@ -1294,7 +1313,7 @@ three_side_grouped_kernel(const DevJob* __restrict__ jobs, const uint4* __restri
     for (int v = threadIdx.x; v < TS_UMAX; v += blockDim.x) s_u[v] = p.u[v];
     const int gi = threadIdx.x / TS_GROUP_THREADS, gt = threadIdx.x % TS_GROUP_THREADS;
     const TsPipe pp{gt, gt >> 5, gt & 31, 1 + gi};
-    unsigned char* base = smem + (size_t)gi * TS_PIPE_BYTES;
+    unsigned char* base = smem + (size_t)gi * pipe_bytes;
     for (int b = threadIdx.x; b < hist_stride(p.len); b += blockDim.x) H[b] = 0;
     if (threadIdx.x == 0) s_since = 0;
     auto draw = [&]() {
@@ -1416,10 +1435,13 @@ __global__ void acos_check_kernel(AcosTable t, uint32_t key_begin, uint32_t coun
 // Launchers
 
 size_t triangle_smem_bytes(int hist_len, int copies) { return TRI_SMEM_FIXED + (size_t)hist_len * copies * 4; }
-size_t three_side_smem_bytes(int hist_len, int copies, int groups) {
-    // groups > 0: the grouped kernel (one histogram); else 8-warp CTAs with 'copies' copies
-    if (groups > 0) return (size_t)groups * TS_PIPE_BYTES + (size_t)hist_stride(hist_len) * 4;
-    return TS_PIPE_BYTES + (size_t)hist_stride(hist_len) * copies * 4;
+size_t three_side_smem_bytes(const ThreeParams& p, int copies, int groups) {
+    // groups > 0: the grouped kernel (one histogram); else 8-warp CTAs with
+    // 'copies' copies (0: the global histogram)
+    const size_t pipe = ts_layout(ts_byte_jk(p)).bytes;
+    const int hist_len = groups > 0 || copies > 0 ? p.len : 0;
+    if (groups > 0) return (size_t)groups * pipe + (size_t)hist_stride(hist_len) * 4;
+    return pipe + (size_t)hist_stride(hist_len) * copies * 4;
 }
 size_t pair_smem_bytes(int hist_len, int copies) { return PR_SMEM_FIXED + (size_t)hist_len * copies * 4; }
 int triangle_block_threads() { return TRI_THREADS; }
@@ -1484,7 +1506,7 @@ cudaError_t launch_three_side(const DevJob* jobs, const uint4* tasks, unsigned i
                               int groups, cudaStream_t st) {
     if (groups > 0) {
         if (groups > TS_GROUPS_MAX) return cudaErrorInvalidValue;
-        const size_t smem = three_side_smem_bytes(p.len, 1, groups);
+        const size_t smem = three_side_smem_bytes(p, 1, groups);
         const int threads = groups * TS_GROUP_THREADS;
         if (fp64)
             three_side_grouped_kernel<true><<<grid, threads, smem, st>>>(jobs, tasks, ntasks, task_counter, p, groups);
@@ -1493,7 +1515,7 @@ cudaError_t launch_three_side(const DevJob* jobs, const uint4* tasks, unsigned i
         return cudaGetLastError();
     }
     const bool global = copies == 0;
-    const size_t smem = three_side_smem_bytes(global ? 0 : p.len, global ? 0 : copies, 0);
+    const size_t smem = three_side_smem_bytes(p, global ? 0 : copies, 0);
 #define TS_LAUNCH(FP, GL) \
     three_side_kernel<FP, GL><<<grid, TS_GROUP_THREADS, smem, st>>>(jobs, tasks, ntasks, task_counter, p, copies > 0 ? copies : 1);
     if (fp64) {
