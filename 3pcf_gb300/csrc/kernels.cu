@@ -979,7 +979,7 @@ constexpr int TS_ROW = 2 * TILE + TS_QCAP;
 // bins alone (only sides below hist_max are ever read), one byte each up to
 // 255 bins.
 struct TsLayout {
-    size_t jk, rows, jkm, box, next, bytes;
+    size_t jk, rows, jkm, box, flags, next, bytes;
 };
 __host__ __device__ constexpr bool ts_byte_jk(const ThreeParams& p) { return p.clean && p.n <= 255; }
 __host__ __device__ constexpr TsLayout ts_layout(bool byte_jk) {
@@ -987,8 +987,9 @@ __host__ __device__ constexpr TsLayout ts_layout(bool byte_jk) {
     const size_t rows = jk + (byte_jk ? TILE * TILE : TILE * TILE * sizeof(uint32_t));
     const size_t jkm = rows + TS_WARPS * TS_ROW * sizeof(uint32_t);
     const size_t box = jkm + TILE * sizeof(unsigned long long);
-    const size_t next = box + 36 * sizeof(float);
-    return TsLayout{jk, rows, jkm, box, next, (next + sizeof(int) + 127) & ~(size_t)127};
+    const size_t flags = box + 36 * sizeof(float);  // reach flags of the points of tiles B and A
+    const size_t next = flags + 2 * TILE;
+    return TsLayout{jk, rows, jkm, box, flags, next, (next + sizeof(int) + 127) & ~(size_t)127};
 }
 
 // distance_to_bin of src/3pcf_C_version.cc:23-51, times 'scale'; sides at or
@@ -1062,27 +1063,14 @@ __device__ __forceinline__ void tile_boxes(const float4* P, const TaskGeom& g, f
     }
 }
 
-// True if every point of tile 'role' is at least 'reach' from pt (squared
-// distance to the tile's bounding box against reach^2).
-__device__ __forceinline__ bool far_from_tile(const float* BX, float4 pt, int role, float reach2) {
-    const float* b0 = BX + role * 12;
-    float s2 = 0.f;
-    {
-        const float lo = fminf(b0[0], b0[6]), hi = fmaxf(b0[3], b0[9]);
-        const float gap = fmaxf(0.f, fmaxf(lo - pt.x, pt.x - hi));
-        s2 = fmaf(gap, gap, s2);
-    }
-    {
-        const float lo = fminf(b0[1], b0[7]), hi = fmaxf(b0[4], b0[10]);
-        const float gap = fmaxf(0.f, fmaxf(lo - pt.y, pt.y - hi));
-        s2 = fmaf(gap, gap, s2);
-    }
-    {
-        const float lo = fminf(b0[2], b0[8]), hi = fmaxf(b0[5], b0[11]);
-        const float gap = fmaxf(0.f, fmaxf(lo - pt.z, pt.z - hi));
-        s2 = fmaf(gap, gap, s2);
-    }
-    return s2 >= reach2;
+// True if every point of half-tile box 'b' (role * 2 + half) is at least
+// 'reach' from pt; an empty half (inverted box) is far from everything.
+__device__ __forceinline__ bool far_from_box(const float* BX, float4 pt, int b, float reach2) {
+    const float* b0 = BX + b * 6;
+    const float gx = fmaxf(0.f, fmaxf(b0[0] - pt.x, pt.x - b0[3]));
+    const float gy = fmaxf(0.f, fmaxf(b0[1] - pt.y, pt.y - b0[4]));
+    const float gz = fmaxf(0.f, fmaxf(b0[2] - pt.z, pt.z - b0[5]));
+    return fmaf(gz, gz, fmaf(gy, gy, gx * gx)) >= reach2;
 }
 
 // One task (tiles A, B, C) of the three-side histogram on one pipeline whose
@@ -1094,6 +1082,8 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
     float4* P = reinterpret_cast<float4*>(base);
     const bool byte_jk = ts_byte_jk(p);
     const TsLayout L = ts_layout(byte_jk);
+    uint8_t* FJ = base + L.flags;  // per j of tile B: 1 reaches tile A, 2 / 4 reaches half 0 / 1 of tile C
+    uint8_t* FI = FJ + TILE;       // per i of tile A: 1 / 2 reaches half 0 / 1 of B, 4 / 8 of C
     uint32_t* JK = reinterpret_cast<uint32_t*>(base + L.jk);
     uint8_t* JK8 = base + L.jk;
     uint32_t* ROWS = reinterpret_cast<uint32_t*>(base + L.rows);
@@ -1115,21 +1105,50 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
         // Clean mode drops every triple with a side >= hist_max, so a point
         // farther than that from a whole tile takes no part in the task (the
         // 1e-5 margin covers the rounding of the bound and of the distance).
+        // (The planner flags tile pairs A-B and A-C that are not wholly within
+        // reach; B-C pairs are checked here on the half-tile boxes.)
         const bool chk_b = task.x & TASK_CHECK_B, chk_c = task.x & TASK_CHECK_C;
-        if (chk_b || chk_c) tile_boxes(P, g, BX, warp, lane);
+        tile_boxes(P, g, BX, warp, lane);
         pp.sync();
         const float reach = p.hi * (1.0f + 1e-5f), reach2 = reach * reach;
+        // reach flags of every point against the half-tile boxes, lane-parallel
+        if (warp == 0) {
+#pragma unroll
+            for (int r = 0; r < 2; r++) {
+                const int j = lane + 32 * r;
+                const float4 pj = P[TILE + j];
+                unsigned f = 0;
+                if (!chk_b || !far_from_box(BX, pj, 0, reach2) || !far_from_box(BX, pj, 1, reach2)) f |= 1u;
+                if (!far_from_box(BX, pj, 4, reach2)) f |= 2u;
+                if (!far_from_box(BX, pj, 5, reach2)) f |= 4u;
+                FJ[j] = (uint8_t)f;
+            }
+        } else if (warp == 1) {
+#pragma unroll
+            for (int r = 0; r < 2; r++) {
+                const int i = lane + 32 * r;
+                const float4 pi = P[i];
+                unsigned f = 0;
+                if (!chk_b || !far_from_box(BX, pi, 2, reach2)) f |= 1u;
+                if (!chk_b || !far_from_box(BX, pi, 3, reach2)) f |= 2u;
+                if (!chk_c || !far_from_box(BX, pi, 4, reach2)) f |= 4u;
+                if (!chk_c || !far_from_box(BX, pi, 5, reach2)) f |= 8u;
+                FI[i] = (uint8_t)f;
+            }
+        }
+        pp.sync();
         // j-k codes, one warp per row j, and JKM[j]: the k's whose side is
-        // below hist_max
+        // below hist_max (halves of tile C out of reach of j are skipped)
         for (int j = warp; j < g.nB; j += TS_WARPS) {
             const float4 pj = P[TILE + j];
-            if (chk_b && far_from_tile(BX, pj, 0, reach2)) {  // no i reaches j: the row is never read
+            const unsigned f = FJ[j];
+            if (!(f & 1u) || !(f & 6u)) {  // no i, or no k, reaches j: the row is never read
                 if (lane == 0) JKM[j] = 0ull;
                 continue;
             }
             uint32_t c0 = TS_FAR, c1 = TS_FAR;
-            if (lane < g.nC) c0 = side_code3_pts<FP64>(pj, P[2 * TILE + lane], p, U, 1u);
-            if (lane + 32 < g.nC) c1 = side_code3_pts<FP64>(pj, P[2 * TILE + lane + 32], p, U, 1u);
+            if ((f & 2u) && lane < g.nC) c0 = side_code3_pts<FP64>(pj, P[2 * TILE + lane], p, U, 1u);
+            if ((f & 4u) && lane + 32 < g.nC) c1 = side_code3_pts<FP64>(pj, P[2 * TILE + lane + 32], p, U, 1u);
             if (byte_jk) {  // bins <= nbins <= 255 where read
                 JK8[j * TILE + lane] = (uint8_t)c0;
                 JK8[j * TILE + lane + 32] = (uint8_t)c1;
@@ -1164,13 +1183,14 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
             i = __shfl_sync(0xffffffffu, i, 0);
             if (i >= g.nA) break;
             const float4 pi = P[i];
-            if ((chk_b && far_from_tile(BX, pi, 1, reach2)) || (chk_c && far_from_tile(BX, pi, 2, reach2)))
-                continue;  // warp-uniform
+            const unsigned fi = FI[i];
+            if (!(fi & 3u) || !(fi & 12u)) continue;  // out of reach of tile B or tile C (warp-uniform)
             uint32_t cik[2], cij[2];
 #pragma unroll
             for (int r = 0; r < 2; r++) {
                 const int k = lane + 32 * r;
-                cik[r] = k < g.nC ? side_code3_pts<FP64>(pi, P[2 * TILE + k], p, U, n) : TS_FAR;
+                cik[r] = ((fi >> (2 + r)) & 1u) && k < g.nC ? side_code3_pts<FP64>(pi, P[2 * TILE + k], p, U, n)
+                                                             : TS_FAR;
             }
             const unsigned long long mk = ballot64(cik[0] < TS_FAR, cik[1] < TS_FAR);
             if (!mk) continue;  // warp-uniform
@@ -1181,7 +1201,7 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
                 const int j = lane + 32 * r;
                 cij[r] = TS_FAR;
                 vj[r] = false;
-                if (j < g.nB && (JKM[j] & mk)) {
+                if (((fi >> r) & 1u) && j < g.nB && (JKM[j] & mk)) {
                     cij[r] = side_code3_pts<FP64>(pi, P[TILE + j], p, U, 1u);
                     vj[r] = cij[r] < TS_FAR;
                 }
