@@ -983,6 +983,7 @@ struct TripletPlan {
     const Binning* bin = nullptr;
     uint32_t slot = 0;
     bool empty = true, prune = false, tri = false, sameAB = false, sameBC = false;
+    bool sym_three = true;  // TPCF_SYM3=0: ordered three-side tasks
     const PairTable *AB = nullptr, *AC = nullptr, *BC = nullptr;
 
     void init(const tpcf_spec& s, const PlannedJob& p, uint32_t sl, const Binning& b, const PairTable* ab,
@@ -997,6 +998,8 @@ struct TripletPlan {
         tri = s.kind == TPCF_TRIANGLE || s.kind == TPCF_TRIANGLE_JBJ;
         sameAB = p.role(0) == p.role(1);
         sameBC = p.role(1) == p.role(2);
+        const char* e3 = getenv("TPCF_SYM3");
+        sym_three = !(e3 && e3[0] == '0');
         AB = ab;
         AC = ac;
         BC = bc;
@@ -1021,6 +1024,10 @@ struct TripletPlan {
                                            (uint32_t)c)});
         };
         const tpcf_spec& s = *sp;
+        // three-side histogram of one catalog in all roles, clean mode: the
+        // kernel counts each multiset {i, j, k} for all its orderings
+        const bool sym3 = s.kind == TPCF_THREE_SIDE && s.loop == TPCF_LOOP_ALL &&
+                          s.overflow == TPCF_OVERFLOW_CLEAN && sym_three && sameAB && sameBC;
         if (pj->swap == 1) {
             // roles (C, A, A) of a D-D-R job: each point of C with every
             // unordered pair of the single array, weight [k_c >= j] + [k_c >= k]
@@ -1038,15 +1045,17 @@ struct TripletPlan {
                     if (b < a) continue;
                     for (int c : AC->nb[a]) add(a, b, c, PRED_NONE, a == b ? TASK_DIAG_IJ : 0);
                 }
-        } else if (tri && s.loop == TPCF_LOOP_SAME && sameAB && sameBC) {
-            // i <= j <= k over one array: unordered distinct triples
+        } else if ((tri && s.loop == TPCF_LOOP_SAME || sym3) && sameAB && sameBC) {
+            // i <= j <= k over one array: unordered distinct triples (triangle
+            // programs), or every multiset of three points counted for each of
+            // its orderings (three-side clean mode: PRED_SAME marks the task)
             for (int a = a0; a < a1; a++)
                 for (int b : AB->nb[a]) {
                     if (b < a) continue;
                     for (int c : AC->nb[a]) {
                         if (c < b) continue;
                         uint32_t f = (a == b ? TASK_DIAG_IJ : 0) | (b == c ? TASK_DIAG_JK : 0);
-                        add(a, b, c, PRED_NONE, f);
+                        add(a, b, c, sym3 ? PRED_SAME : PRED_NONE, f);
                     }
                 }
         } else if (tri && s.loop == TPCF_LOOP_ONE && sameBC) {

@@ -1108,6 +1108,12 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
         // (The planner flags tile pairs A-B and A-C that are not wholly within
         // reach; B-C pairs are checked here on the half-tile boxes.)
         const bool chk_b = task.x & TASK_CHECK_B, chk_c = task.x & TASK_CHECK_C;
+        // Symmetric tasks (one catalog in all three roles): tiles a <= b <= c
+        // and, on diagonal tile pairs, positions i <= j <= k, so that every
+        // multiset {i, j, k} is visited once and counted for each of its
+        // distinct orderings.
+        const bool sym = ((task.x >> TASK_PRED_SHIFT) & TASK_PRED_MASK) == PRED_SAME;
+        const bool diag_ij = task.x & TASK_DIAG_IJ, diag_jk = task.x & TASK_DIAG_JK;
         tile_boxes(P, g, BX, warp, lane);
         pp.sync();
         const float reach = p.hi * (1.0f + 1e-5f), reach2 = reach * reach;
@@ -1156,7 +1162,8 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
                 JK[j * TILE + lane] = c0;
                 JK[j * TILE + lane + 32] = c1;
             }
-            const unsigned long long m = ballot64(c0 < TS_FAR, c1 < TS_FAR);
+            unsigned long long m = ballot64(c0 < TS_FAR, c1 < TS_FAR);
+            if (sym && diag_jk) m &= ~0ull << j;  // k >= j
             if (lane == 0) JKM[j] = m;
         }
         pp.sync();
@@ -1164,21 +1171,39 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
         uint32_t* row_ij = row_ik + TILE;
         uint32_t* cq = row_ij + TILE;
         const unsigned lt = (1u << lane) - 1u;
+        auto add = [&](uint32_t idx) {
+            if (idx < len) {  // a side rounded to bin nbins aliases as in the reference
+                if (GLOBAL_HIST) atomicAdd(J.hist + idx, 1ull);
+                else atomicAdd(Hw + hist_pos(idx), 1u);
+            }
+        };
+        int i = 0;
         auto count_candidates = [&](const uint32_t* e, int m) {
             if (lane < m) {
                 const uint32_t c = e[lane];
                 const int j = c & 63, k = c >> 6;
-                const uint32_t jk = byte_jk ? (uint32_t)JK8[j * TILE + k] : JK[j * TILE + k];
-                const uint32_t idx = jk * n2 + row_ik[k] + row_ij[j];
-                if (idx < len) {  // a side rounded to bin nbins aliases as in the reference
-                    if (GLOBAL_HIST) atomicAdd(J.hist + idx, 1ull);
-                    else atomicAdd(Hw + hist_pos(idx), 1u);
+                const uint32_t vjk = byte_jk ? (uint32_t)JK8[j * TILE + k] : JK[j * TILE + k];
+                const uint32_t vik = row_ik[k], vij = row_ij[j];
+                if (!sym) {
+                    add(vjk * n2 + vik * n + vij);
+                } else {
+                    // sides (d01, d02, d12) of the orderings of {i, j, k}:
+                    // (i,j,k) (ij,ik,jk), (i,k,j) (ik,ij,jk), (j,i,k) (ij,jk,ik),
+                    // (j,k,i) (jk,ij,ik), (k,i,j) (ik,jk,ij), (k,j,i) (jk,ik,ij);
+                    // with i == j or j == k only three of them are distinct
+                    const bool eij = diag_ij && i == j, ejk = diag_jk && j == k;
+                    add(vjk * n2 + vik * n + vij);
+                    if (!ejk) add(vjk * n2 + vij * n + vik);
+                    if (!eij) add(vik * n2 + vjk * n + vij);
+                    if (!eij) add(vik * n2 + vij * n + vjk);
+                    if (!ejk) add(vij * n2 + vjk * n + vik);
+                    if (!eij && !ejk) add(vij * n2 + vik * n + vjk);
                 }
             }
         };
         for (;;) {
             // points of tile A go to warps one at a time (their work is uneven)
-            int i = 0;
+            i = 0;
             if (lane == 0) i = atomicAdd(next_i, 1);
             i = __shfl_sync(0xffffffffu, i, 0);
             if (i >= g.nA) break;
@@ -1189,7 +1214,7 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
 #pragma unroll
             for (int r = 0; r < 2; r++) {
                 const int k = lane + 32 * r;
-                cik[r] = ((fi >> (2 + r)) & 1u) && k < g.nC ? side_code3_pts<FP64>(pi, P[2 * TILE + k], p, U, n)
+                cik[r] = ((fi >> (2 + r)) & 1u) && k < g.nC ? side_code3_pts<FP64>(pi, P[2 * TILE + k], p, U, 1u)
                                                              : TS_FAR;
             }
             const unsigned long long mk = ballot64(cik[0] < TS_FAR, cik[1] < TS_FAR);
@@ -1201,7 +1226,7 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
                 const int j = lane + 32 * r;
                 cij[r] = TS_FAR;
                 vj[r] = false;
-                if (((fi >> r) & 1u) && j < g.nB && (JKM[j] & mk)) {
+                if (((fi >> r) & 1u) && j < g.nB && (JKM[j] & mk) && !(sym && diag_ij && j < i)) {
                     cij[r] = side_code3_pts<FP64>(pi, P[TILE + j], p, U, 1u);
                     vj[r] = cij[r] < TS_FAR;
                 }

@@ -318,6 +318,29 @@ def test_three_side_clean_spread_catalog(eng, axis):
     eng.release(h)
 
 
+@pytest.mark.parametrize("sym", ["1", "0"])
+def test_three_side_clean_duplicates(eng, monkeypatch, sym):
+    """Clean three-side mode on a catalog where every point appears three
+    times (zero-length sides between distinct indices) beside the repeated
+    indices of the ordered loop (i == j, j == k, i == j == k): the symmetric
+    tasks (each multiset of three points counted for its distinct orderings)
+    and the ordered ones (TPCF_SYM3=0) give the oracle's counts."""
+    monkeypatch.setenv("TPCF_SYM3", sym)
+    base = synth.lattice_mix(70, box=30.0, frac=0.5, seed=43)
+    pts = np.concatenate([base, base, base])[np.random.default_rng(44).permutation(210)]
+    h = eng.catalog(pts)
+    for axis in ((16, 0.0, 24.0), (10, 1.0, 11.0)):
+        s = tpcf.make_spec(tpcf.THREE_SIDE, tpcf.LOOP_ALL, [axis], overflow=tpcf.OVERFLOW_CLEAN)
+        want, n = oracle.three_side([pts, pts, pts], axis[1], axis[2], axis[0], clean=True)
+        got = eng.count(s, eng.job([h, h, h]))
+        assert np.array_equal(got, want), axis
+        # a sub-range of the catalog (tiles of a range view) and two roles alike
+        r = [(13, 190)] * 3
+        want_r, _ = oracle.three_side([pts[13:190]] * 3, axis[1], axis[2], axis[0], clean=True)
+        assert np.array_equal(eng.count(s, eng.job([h, h, h], r)), want_r), axis
+    eng.release(h)
+
+
 @pytest.mark.parametrize("axis", [(700, 0.0, 70.0), (40, 1.0, 21.0)])
 def test_pairs_vs_oracle(eng, axis):
     d = synth.blobs(3000, n_blobs=10, sigma=5.0, box=100.0, seed=41)
