@@ -1413,7 +1413,9 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
             total += part[i].size();
         }
         std::vector<uint4> h_tasks(total);
-        if (total <= (size_t)ctx->num_sms * 3 * 64) {
+        // (three-side histograms above 8192 bins keep job order: their CTAs
+        // flush, and the task pipelines of one CTA meet, at every job change)
+        if (total <= (size_t)ctx->num_sms * 3 * 64 && !(sp.kind == TPCF_THREE_SIDE && bin.len > 8192)) {
             // few tasks per CTA: largest first, so that the dynamic fetch
             // balances the tail (a stable counting pass over 64 size classes)
             auto cls = [](uint64_t u) { return 63 - (u ? 63 - __builtin_clzll(u) : 0); };

@@ -318,6 +318,31 @@ def test_three_side_clean_spread_catalog(eng, axis):
     eng.release(h)
 
 
+def test_three_side_clean_batch_of_jobs(eng):
+    """Several clean three-side jobs with a 32^3-bin histogram in one launch
+    (one CTA per SM of task pipelines that meet to flush at every change of
+    job), symmetric and ordered tasks mixed, two jobs summed into one output:
+    each output equals the oracle's."""
+    d = synth.blobs(700, n_blobs=5, sigma=6.0, box=90.0, seed=45)
+    r = synth.lattice_mix(600, box=90.0, frac=0.3, seed=46)
+    hd, hr = eng.catalog(d), eng.catalog(r)
+    axis = (32, 0.0, 32.0)
+    s = tpcf.make_spec(tpcf.THREE_SIDE, tpcf.LOOP_ALL, [axis], overflow=tpcf.OVERFLOW_CLEAN)
+    combos = [([hd, hd, hd], [d, d, d]), ([hd, hr, hr], [d, r, r]), ([hr, hr, hr], [r, r, r]),
+              ([hr, hd, hr], [r, d, r])]
+    want = [oracle.three_side(c, axis[1], axis[2], axis[0], clean=True)[0] for _, c in combos]
+    jobs = [eng.job(h) for h, _ in combos]
+    for _ in range(3):  # the repeated batch is autotuned, then replayed
+        got = eng.count_batch([s] * 4, jobs)
+        for g, w in zip(got, want):
+            assert np.array_equal(g, w)
+    got = eng.count_batch_into([s] * 4, jobs, [0, 1, 0, 1], 2)
+    assert np.array_equal(got[0], want[0] + want[2])
+    assert np.array_equal(got[1], want[1] + want[3])
+    eng.release(hd)
+    eng.release(hr)
+
+
 @pytest.mark.parametrize("sym", ["1", "0"])
 def test_three_side_clean_duplicates(eng, monkeypatch, sym):
     """Clean three-side mode on a catalog where every point appears three
