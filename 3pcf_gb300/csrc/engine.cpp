@@ -511,6 +511,7 @@ Binning make_binning(const tpcf_spec& sp) {
         if (p.clean) b.lmax = (double)p.hi * (1 + 1e-6);
         // (compat mode counts every triple: the side codes are a small part of its work)
         p.fast = p.clean && three_side_thresholds(p) ? 1 : 0;
+        p.zcode = three_side_bin_of_d2(0.0f, p.lo, p.hi, p.bw, p.n);
     } else if (sp.kind == TPCF_TRIANGLE) {
         for (int a = 0; a < 3; a++) check_axis(sp.axis[a], "triangle axis");
         TriParams& p = b.tri;
@@ -1024,10 +1025,9 @@ struct TripletPlan {
                                            (uint32_t)c)});
         };
         const tpcf_spec& s = *sp;
-        // three-side histogram of one catalog in all roles, clean mode: the
-        // kernel counts each multiset {i, j, k} for all its orderings
-        const bool sym3 = s.kind == TPCF_THREE_SIDE && s.loop == TPCF_LOOP_ALL &&
-                          s.overflow == TPCF_OVERFLOW_CLEAN && sym_three && sameAB && sameBC;
+        // three-side histogram of one catalog in all roles: the kernel counts
+        // each multiset {i, j, k} once for all its orderings
+        const bool sym3 = s.kind == TPCF_THREE_SIDE && s.loop == TPCF_LOOP_ALL && sym_three && sameAB && sameBC;
         if (pj->swap == 1) {
             // roles (C, A, A) of a D-D-R job: each point of C with every
             // unordered pair of the single array, weight [k_c >= j] + [k_c >= k]
@@ -1048,7 +1048,7 @@ struct TripletPlan {
         } else if ((tri && s.loop == TPCF_LOOP_SAME || sym3) && sameAB && sameBC) {
             // i <= j <= k over one array: unordered distinct triples (triangle
             // programs), or every multiset of three points counted for each of
-            // its orderings (three-side clean mode: PRED_SAME marks the task)
+            // its orderings (three-side: PRED_SAME marks the task)
             for (int a = a0; a < a1; a++)
                 for (int b : AB->nb[a]) {
                     if (b < a) continue;

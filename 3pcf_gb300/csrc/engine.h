@@ -102,6 +102,7 @@ struct ThreeParams {
     int fast;
     float inv_bw;
     float u[TS_UMAX];
+    int zcode;  // bin of a zero-length side (nbins + 1 at or above hist_max)
 };
 
 struct PairParams {

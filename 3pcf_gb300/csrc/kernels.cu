@@ -1027,6 +1027,87 @@ __device__ __forceinline__ uint32_t side_code3_pts(float4 a, float4 b, const Thr
     return side_code3<FP64>(ref_dist<FP64>(a, b), p, scale);
 }
 
+// Symmetric three-side tasks (one catalog in all roles) visit each multiset
+// {i <= j <= k} once.  With a shared histogram they count it once in a
+// multiset accumulator (m = nbins + 2 codes per side, so no index aliases):
+//   U[v_jk m^2 + v_ik m + v_ij]   three distinct points,
+//   U2[v]                         two equal indices (sides 0, v, v),
+//   U6                            i == j == k,
+// which ts_flush expands into the reference's ordered histogram.  The
+// accumulator is ts_acc_words(p) words, U2 from word ts_u2(p).
+__host__ __device__ inline int ts_u2(const ThreeParams& p) {
+    const int m = p.n + 2;
+    return hist_stride(m * m * m);
+}
+__host__ __device__ inline int ts_acc_words(const ThreeParams& p) {
+    const int acc = ts_u2(p) + p.n + 3;
+    return acc > p.len ? acc : p.len;
+}
+
+// Adds one ordering (sides d01, d02, d12 with codes x0, x1, x2) of a triple
+// to the reference's histogram (an index at or past its end is dropped).
+__device__ __forceinline__ void ts_put(unsigned long long* g, uint32_t x0, uint32_t x1, uint32_t x2,
+                                       const ThreeParams& p, unsigned long long u) {
+    const uint32_t t = x2 * (uint32_t)p.n * (uint32_t)p.n + x1 * (uint32_t)p.n + x0;
+    if (t < (uint32_t)p.len) atomicAdd(g + t, u);
+}
+
+// The distinct orderings of a multiset with side codes (v_ij, v_ik, v_jk):
+// (i,j,k) (ij,ik,jk), (i,k,j) (ik,ij,jk), (j,i,k) (ij,jk,ik), (j,k,i) (jk,ij,ik),
+// (k,i,j) (ik,jk,ij), (k,j,i) (jk,ik,ij); with i == j or j == k three of them.
+__device__ __forceinline__ void ts_put_orderings(unsigned long long* g, uint32_t vij, uint32_t vik, uint32_t vjk,
+                                                 bool eij, bool ejk, const ThreeParams& p, unsigned long long u) {
+    ts_put(g, vij, vik, vjk, p, u);
+    if (!ejk) ts_put(g, vik, vij, vjk, p, u);
+    if (!eij) ts_put(g, vij, vjk, vik, p, u);
+    if (!eij) ts_put(g, vjk, vij, vik, p, u);
+    if (!ejk) ts_put(g, vik, vjk, vij, p, u);
+    if (!eij && !ejk) ts_put(g, vjk, vik, vij, p, u);
+}
+
+// Flushes 'copies' shared copies (hist_stride(ts_acc_words(p)) words apart)
+// into the job's 64-bit histogram: the swizzled ordered histogram, or the
+// multiset accumulator of a symmetric job expanded into its orderings.
+__device__ void ts_flush(unsigned int* H, int copies, const ThreeParams& p, unsigned long long* g, bool sym) {
+    const int stride = hist_stride(ts_acc_words(p));
+    __syncthreads();
+    if (!sym) {
+        for (int b = threadIdx.x; b < p.len; b += blockDim.x) {
+            const int at = (int)hist_pos((unsigned)b);
+            unsigned long long u = 0;
+            for (int c = 0; c < copies; c++) {
+                u += H[c * stride + at];
+                H[c * stride + at] = 0;
+            }
+            if (u) atomicAdd(g + b, u);
+        }
+    } else {
+        const int m = p.n + 2, m3 = m * m * m, u2 = ts_u2(p);
+        const uint32_t z = (uint32_t)p.zcode;
+        for (int b = threadIdx.x; b < m3 + m + 1; b += blockDim.x) {
+            const int at = b < m3 ? (int)hist_pos((unsigned)b) : u2 + (b - m3);
+            unsigned long long u = 0;
+            for (int c = 0; c < copies; c++) {
+                u += H[c * stride + at];
+                H[c * stride + at] = 0;
+            }
+            if (!u) continue;
+            if (b < m3) {
+                const uint32_t vij = b % m, vik = (b / m) % m, vjk = b / (m * m);
+                ts_put_orderings(g, vij, vik, vjk, false, false, p, u);
+            } else if (b < m3 + m) {
+                const uint32_t v = b - m3;  // (i, i, k) or (i, k, k): sides 0, v, v
+                ts_put(g, z, v, v, p, u);
+                ts_put(g, v, z, v, p, u);
+                ts_put(g, v, v, z, p, u);
+            } else {
+                ts_put(g, z, z, z, p, u);
+            }
+        }
+    }
+    __syncthreads();
+}
+
 // One task pipeline: its threads (tid in [0, 256)), and its barrier (0: the
 // CTA's, else a named barrier of its 256 threads).
 struct TsPipe {
@@ -1093,6 +1174,9 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
     const int warp = pp.warp, lane = pp.lane;
     const TaskGeom g = task_geom(J, task);
     const uint32_t n = p.n, n2 = (uint32_t)p.n * p.n, len = (uint32_t)p.len;
+    const uint32_t m = n + 2, mm = m * m, u2 = (uint32_t)ts_u2(p);  // multiset accumulator
+    const bool sym = ((task.x >> TASK_PRED_SHIFT) & TASK_PRED_MASK) == PRED_SAME;
+    const bool diag_ij = task.x & TASK_DIAG_IJ, diag_jk = task.x & TASK_DIAG_JK;
     for (int t = pp.tid; t < 3 * TILE; t += TS_GROUP_THREADS) {
         const int role = t / TILE, idx = t % TILE;
         const int nr = role == 0 ? g.nA : (role == 1 ? g.nB : g.nC);
@@ -1112,8 +1196,6 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
         // and, on diagonal tile pairs, positions i <= j <= k, so that every
         // multiset {i, j, k} is visited once and counted for each of its
         // distinct orderings.
-        const bool sym = ((task.x >> TASK_PRED_SHIFT) & TASK_PRED_MASK) == PRED_SAME;
-        const bool diag_ij = task.x & TASK_DIAG_IJ, diag_jk = task.x & TASK_DIAG_JK;
         tile_boxes(P, g, BX, warp, lane);
         pp.sync();
         const float reach = p.hi * (1.0f + 1e-5f), reach2 = reach * reach;
@@ -1178,8 +1260,8 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
             }
         };
         int i = 0;
-        auto count_candidates = [&](const uint32_t* e, int m) {
-            if (lane < m) {
+        auto count_candidates = [&](const uint32_t* e, int cnt) {
+            if (lane < cnt) {
                 const uint32_t c = e[lane];
                 const int j = c & 63, k = c >> 6;
                 const uint32_t vjk = byte_jk ? (uint32_t)JK8[j * TILE + k] : JK[j * TILE + k];
@@ -1187,17 +1269,10 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
                 if (!sym) {
                     add(vjk * n2 + vik * n + vij);
                 } else {
-                    // sides (d01, d02, d12) of the orderings of {i, j, k}:
-                    // (i,j,k) (ij,ik,jk), (i,k,j) (ik,ij,jk), (j,i,k) (ij,jk,ik),
-                    // (j,k,i) (jk,ij,ik), (k,i,j) (ik,jk,ij), (k,j,i) (jk,ik,ij);
-                    // with i == j or j == k only three of them are distinct
                     const bool eij = diag_ij && i == j, ejk = diag_jk && j == k;
-                    add(vjk * n2 + vik * n + vij);
-                    if (!ejk) add(vjk * n2 + vij * n + vik);
-                    if (!eij) add(vik * n2 + vjk * n + vij);
-                    if (!eij) add(vik * n2 + vij * n + vjk);
-                    if (!ejk) add(vij * n2 + vjk * n + vik);
-                    if (!eij && !ejk) add(vij * n2 + vik * n + vjk);
+                    if (GLOBAL_HIST) ts_put_orderings(J.hist, vij, vik, vjk, eij, ejk, p, 1ull);
+                    else if (!eij && !ejk) atomicAdd(Hw + hist_pos(vjk * mm + vik * m + vij), 1u);
+                    else atomicAdd(Hw + u2 + (eij && ejk ? m : (eij ? vik : vij)), 1u);
                 }
             }
         };
@@ -1260,6 +1335,42 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
         }
         return;
     }
+    if (sym) {
+        // every multiset {i <= j <= k} of the task (codes 0 .. nbins + 1)
+        for (int e = pp.tid; e < TILE * TILE; e += TS_GROUP_THREADS) {
+            const int j = e / TILE, k = e % TILE;
+            JK[e] = (j < g.nB && k < g.nC) ? side_code3_pts<FP64>(P[TILE + j], P[2 * TILE + k], p, U, 1u) : 0u;
+        }
+        pp.sync();
+        uint32_t* row = ROWS + warp * TS_ROW;
+        for (int i = warp; i < g.nA; i += TS_WARPS) {
+            const float4 pi = P[i];
+            uint32_t vik[2];
+#pragma unroll
+            for (int r = 0; r < 2; r++) {
+                const int k = lane + 32 * r;
+                vik[r] = k < g.nC ? side_code3_pts<FP64>(pi, P[2 * TILE + k], p, U, 1u) : 0u;
+                if (lane + 32 * r < g.nB) row[lane + 32 * r] = side_code3_pts<FP64>(pi, P[TILE + lane + 32 * r], p, U, 1u);
+            }
+            __syncwarp();
+            for (int j = diag_ij ? i : 0; j < g.nB; j++) {
+                const uint32_t vij = row[j];
+                const bool eij = diag_ij && j == i;
+#pragma unroll
+                for (int r = 0; r < 2; r++) {
+                    const int k = lane + 32 * r;
+                    if (k >= g.nC || (diag_jk && k < j)) continue;
+                    const bool ejk = diag_jk && k == j;
+                    const uint32_t vjk = JK[j * TILE + k];
+                    if (GLOBAL_HIST) ts_put_orderings(J.hist, vij, vik[r], vjk, eij, ejk, p, 1ull);
+                    else if (!eij && !ejk) atomicAdd(Hw + hist_pos(vjk * mm + vik[r] * m + vij), 1u);
+                    else atomicAdd(Hw + u2 + (eij && ejk ? m : (eij ? vik[r] : vij)), 1u);
+                }
+            }
+            __syncwarp();
+        }
+        return;
+    }
     for (int e = pp.tid; e < TILE * TILE; e += TS_GROUP_THREADS) {
         const int j = e / TILE, k = e % TILE;
         JK[e] = (j < g.nB && k < g.nC) ? side_code3_pts<FP64>(P[TILE + j], P[2 * TILE + k], p, U, n2)
@@ -1309,9 +1420,11 @@ three_side_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ tas
     __shared__ uint4 s_task;
     __shared__ float s_u[TS_UMAX];
     for (int v = threadIdx.x; v < TS_UMAX; v += blockDim.x) s_u[v] = p.u[v];
+    const int stride = hist_stride(ts_acc_words(p));
     if (!GLOBAL_HIST)
-        for (int b = threadIdx.x; b < copies * hist_stride(p.len); b += blockDim.x) H[b] = 0;
-    unsigned int* Hw = H + (GLOBAL_HIST ? 0 : ((threadIdx.x >> 5) % copies) * hist_stride(p.len));
+        for (int b = threadIdx.x; b < copies * stride; b += blockDim.x) H[b] = 0;
+    unsigned int* Hw = H + (GLOBAL_HIST ? 0 : ((threadIdx.x >> 5) % copies) * stride);
+    bool cur_sym = false;
     const TsPipe pp{(int)threadIdx.x, (int)(threadIdx.x >> 5), (int)(threadIdx.x & 31), 0};
     int cur = -1;
     unsigned int since = 0;
@@ -1325,10 +1438,11 @@ three_side_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ tas
         const uint4 task = s_task;
         const int slot = task.x == TASK_NONE ? -1 : (int)(task.x & TASK_SLOT_MASK);
         if (!GLOBAL_HIST && (slot != cur || since >= TS_FLUSH_EVERY) && cur >= 0) {
-            flush_hist<true>(H, copies, p.len, jobs[cur].hist);
+            ts_flush(H, copies, p, jobs[cur].hist, cur_sym);
             since = 0;
         }
         cur = slot;
+        cur_sym = ((task.x >> TASK_PRED_SHIFT) & TASK_PRED_MASK) == PRED_SAME;
         if (slot < 0) break;
         since++;
         three_side_task<FP64, GLOBAL_HIST>(jobs[slot], task, p, s_u, smem, Hw, pp);
@@ -1359,7 +1473,7 @@ three_side_grouped_kernel(const DevJob* __restrict__ jobs, const uint4* __restri
     const int gi = threadIdx.x / TS_GROUP_THREADS, gt = threadIdx.x % TS_GROUP_THREADS;
     const TsPipe pp{gt, gt >> 5, gt & 31, 1 + gi};
     unsigned char* base = smem + (size_t)gi * pipe_bytes;
-    for (int b = threadIdx.x; b < hist_stride(p.len); b += blockDim.x) H[b] = 0;
+    for (int b = threadIdx.x; b < hist_stride(ts_acc_words(p)); b += blockDim.x) H[b] = 0;
     if (threadIdx.x == 0) s_since = 0;
     auto draw = [&]() {
         if (gt == 0) {
@@ -1369,15 +1483,21 @@ three_side_grouped_kernel(const DevJob* __restrict__ jobs, const uint4* __restri
     };
     draw();
     int cur = -1;
+    bool cur_sym = false;
     for (;;) {
         __syncthreads();  // every pipeline waits here with a task of another job, or none
-        if (cur >= 0) flush_hist<true>(H, 1, p.len, jobs[cur].hist);
+        if (cur >= 0) ts_flush(H, 1, p, jobs[cur].hist, cur_sym);
         uint32_t next = TASK_NONE;
         for (int g2 = 0; g2 < groups; g2++) {
             const uint32_t x = s_task[g2].x;
             if (x != TASK_NONE) next = min(next, x & TASK_SLOT_MASK);
         }
         if (next == TASK_NONE) break;  // uniform: every thread read the same words
+        for (int g2 = 0; g2 < groups; g2++) {  // all tasks of a job are alike
+            const uint32_t x = s_task[g2].x;
+            if (x != TASK_NONE && (x & TASK_SLOT_MASK) == next)
+                cur_sym = ((x >> TASK_PRED_SHIFT) & TASK_PRED_MASK) == PRED_SAME;
+        }
         if (threadIdx.x < TS_GROUPS_MAX) s_stop[threadIdx.x] = 0;
         if (threadIdx.x == 0) s_since = 0;
         __syncthreads();
@@ -1484,9 +1604,9 @@ size_t three_side_smem_bytes(const ThreeParams& p, int copies, int groups) {
     // groups > 0: the grouped kernel (one histogram); else 8-warp CTAs with
     // 'copies' copies (0: the global histogram)
     const size_t pipe = ts_layout(ts_byte_jk(p)).bytes;
-    const int hist_len = groups > 0 || copies > 0 ? p.len : 0;
-    if (groups > 0) return (size_t)groups * pipe + (size_t)hist_stride(hist_len) * 4;
-    return pipe + (size_t)hist_stride(hist_len) * copies * 4;
+    const int words = groups > 0 || copies > 0 ? hist_stride(ts_acc_words(p)) : 0;
+    if (groups > 0) return (size_t)groups * pipe + (size_t)words * 4;
+    return pipe + (size_t)words * copies * 4;
 }
 size_t pair_smem_bytes(int hist_len, int copies) { return PR_SMEM_FIXED + (size_t)hist_len * copies * 4; }
 int triangle_block_threads() { return TRI_THREADS; }
