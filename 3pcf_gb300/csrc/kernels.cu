@@ -1412,7 +1412,7 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
 // 8-warp CTAs, several per SM: warp-private shared histogram copies (copies
 // > 0) or the global histogram.
 template <bool FP64, bool GLOBAL_HIST>
-__global__ void __launch_bounds__(TS_GROUP_THREADS)
+__global__ void __launch_bounds__(TS_GROUP_THREADS, 4)
 three_side_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ tasks, unsigned int ntasks,
                   unsigned int* task_counter, ThreeParams p, int copies) {
     extern __shared__ __align__(16) unsigned char smem[];
