@@ -1353,6 +1353,19 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
                 if (lane + 32 * r < g.nB) row[lane + 32 * r] = side_code3_pts<FP64>(pi, P[TILE + lane + 32 * r], p, U, 1u);
             }
             __syncwarp();
+            if (!GLOBAL_HIST && !diag_ij && !diag_jk) {
+                // three tiles apart: every (j, k) is a multiset of distinct points
+                const uint32_t vikm0 = vik[0] * m, vikm1 = vik[1] * m;
+                const bool k0 = lane < g.nC, k1 = lane + 32 < g.nC;
+#pragma unroll 4
+                for (int j = 0; j < g.nB; j++) {
+                    const uint32_t vij = row[j];
+                    if (k0) atomicAdd(Hw + hist_pos(JK[j * TILE + lane] * mm + vikm0 + vij), 1u);
+                    if (k1) atomicAdd(Hw + hist_pos(JK[j * TILE + lane + 32] * mm + vikm1 + vij), 1u);
+                }
+                __syncwarp();
+                continue;
+            }
             for (int j = diag_ij ? i : 0; j < g.nB; j++) {
                 const uint32_t vij = row[j];
                 const bool eij = diag_ij && j == i;
