@@ -110,6 +110,17 @@ def spatial_jobs(kind, d_range, r_range, grid):
     global_index) with roles 'D'/'R' per position and loop one of
     "same", "one", "all"."""
     grid = tuple(int(x) for x in grid)
+    return [j[:4] for j in cell_jobs(kind, d_range, r_range, lambda v, occ: _neighbours(v, grid, occ),
+                                     lambda a, b: _adjacent(a, b, grid))]
+
+
+def cell_jobs(kind, d_range, r_range, neighbours, near):
+    """Jobs of one histogram kind over the cells of cell-ordered catalogs.
+    neighbours(v, occupied) lists the occupied cells (v included) whose
+    points may lie within the longest counted side of a point of cell v, and
+    near(a, b) says the same of two cells; every counted triangle then falls
+    in exactly one job.  Returns (roles, ranges, loop, global_index, cells)
+    with the cell of each role."""
     ds, de = d_range
     rs, rend = r_range
     occ_d = de > ds
@@ -120,37 +131,106 @@ def spatial_jobs(kind, d_range, r_range, grid):
         X = kind[0]
         occ = occ_d if X == "D" else occ_r
         for a in np.nonzero(occ)[0]:
-            nb = _neighbours(a, grid, occ)
-            jobs.append(((X, X, X), [rng(X, a)] * 3, "same", False))
+            a = int(a)
+            nb = neighbours(a, occ)
+            jobs.append(((X, X, X), [rng(X, a)] * 3, "same", False, (a, a, a)))
             for b in nb:
                 if b <= a:
                     continue
-                jobs.append(((X, X, X), [rng(X, b), rng(X, a), rng(X, a)], "one", False))  # a=a<b
-                jobs.append(((X, X, X), [rng(X, a), rng(X, b), rng(X, b)], "one", False))  # a<b=b
+                jobs.append(((X, X, X), [rng(X, b), rng(X, a), rng(X, a)], "one", False, (b, a, a)))  # a=a<b
+                jobs.append(((X, X, X), [rng(X, a), rng(X, b), rng(X, b)], "one", False, (a, b, b)))  # a<b=b
                 for c in nb:
-                    if c > b and _adjacent(b, c, grid):
-                        jobs.append(((X, X, X), [rng(X, a), rng(X, b), rng(X, c)], "all", False))
+                    if c > b and near(b, c):
+                        jobs.append(((X, X, X), [rng(X, a), rng(X, b), rng(X, c)], "all", False, (a, b, c)))
     elif kind == "DRR":
         for u in np.nonzero(occ_d)[0]:
-            nb = _neighbours(u, grid, occ_r)
+            u = int(u)
+            nb = neighbours(u, occ_r)
             for v in nb:
-                jobs.append((("D", "R", "R"), [rng("D", u), rng("R", v), rng("R", v)], "one", False))
+                jobs.append((("D", "R", "R"), [rng("D", u), rng("R", v), rng("R", v)], "one", False, (u, v, v)))
                 for w in nb:
-                    if w > v and _adjacent(v, w, grid):
-                        jobs.append((("D", "R", "R"), [rng("D", u), rng("R", v), rng("R", w)], "all", False))
+                    if w > v and near(v, w):
+                        jobs.append((("D", "R", "R"), [rng("D", u), rng("R", v), rng("R", w)], "all", False,
+                                     (u, v, w)))
     elif kind == "DDR":
         for u in np.nonzero(occ_d)[0]:
-            nbd = _neighbours(u, grid, occ_d)
-            nbr = _neighbours(u, grid, occ_r)
+            u = int(u)
+            nbd = neighbours(u, occ_d)
+            nbr = neighbours(u, occ_r)
             for w in nbr:
-                jobs.append((("D", "D", "R"), [rng("D", u), rng("D", u), rng("R", w)], "one", True))
+                jobs.append((("D", "D", "R"), [rng("D", u), rng("D", u), rng("R", w)], "one", True, (u, u, w)))
             for v in nbd:
                 if v <= u:
                     continue
                 for w in nbr:
-                    if _adjacent(v, w, grid):
-                        jobs.append((("D", "D", "R"), [rng("D", u), rng("D", v), rng("R", w)], "one", True))
-                        jobs.append((("D", "D", "R"), [rng("D", v), rng("D", u), rng("R", w)], "one", True))
+                    if near(v, w):
+                        jobs.append((("D", "D", "R"), [rng("D", u), rng("D", v), rng("R", w)], "one", True,
+                                     (u, v, w)))
+                        jobs.append((("D", "D", "R"), [rng("D", v), rng("D", u), rng("R", w)], "one", True,
+                                     (v, u, w)))
     else:
         raise ValueError(kind)
     return jobs
+
+
+# ---------------------------------------------------------------------------
+# Jackknife subsamples from one decomposition.
+#
+# With the catalogs ordered by jackknife region (cells), every counted
+# triangle falls in exactly one cell job, so the subsample without region r
+# (points of r removed from both catalogs) is the sum of the jobs that involve
+# no point of r: JK_r = F - sum of the jobs whose cells include r, F the sum
+# of all jobs.  Jobs are grouped by their set of distinct cells; the engine
+# sums each group on the device and the subsamples are sums of groups.
+
+def cell_boxes(points_by_cat, starts_by_cat, ends_by_cat, ncell):
+    """Bounding box (lo, hi; float64) of each cell over every catalog."""
+    lo = np.full((ncell, 3), np.inf)
+    hi = np.full((ncell, 3), -np.inf)
+    for pts, st, en in zip(points_by_cat, starts_by_cat, ends_by_cat):
+        pts = np.asarray(pts, dtype=np.float64)
+        for c in range(ncell):
+            if en[c] > st[c]:
+                seg = pts[st[c]:en[c]]
+                lo[c] = np.minimum(lo[c], seg.min(0))
+                hi[c] = np.maximum(hi[c], seg.max(0))
+    return lo, hi
+
+
+def box_near(lo, hi, reach):
+    """near(a, b): the boxes of cells a and b are closer than reach (a
+    conservative test: the true distance of two points is at least it)."""
+    def near(a, b):
+        gap = np.maximum(0.0, np.maximum(lo[a] - hi[b], lo[b] - hi[a]))
+        return bool(np.sqrt((gap ** 2).sum()) < reach)
+
+    def neighbours(v, occ):
+        return [int(c) for c in np.nonzero(occ)[0] if near(v, int(c))]
+    return neighbours, near
+
+
+def jackknife_groups(kind, d_range, r_range, neighbours, near):
+    """Cell jobs of one kind and their groups: returns (jobs, group of each
+    job, cell set of each group)."""
+    jobs = cell_jobs(kind, d_range, r_range, neighbours, near)
+    groups, key_of = [], {}
+    gid = []
+    for j in jobs:
+        key = frozenset(j[4])
+        if key not in key_of:
+            key_of[key] = len(groups)
+            groups.append(key)
+        gid.append(key_of[key])
+    return jobs, gid, groups
+
+
+def jackknife_from_groups(group_hists, groups, nregions):
+    """(full histogram, [JK_r for r in range(nregions)]) from the summed
+    histogram of each group (uint64 arrays)."""
+    full = np.zeros_like(group_hists[0])
+    touch = [np.zeros_like(group_hists[0]) for _ in range(nregions)]
+    for h, g in zip(group_hists, groups):
+        full += h
+        for r in g:
+            touch[r] += h
+    return full, [full - t for t in touch]

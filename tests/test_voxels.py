@@ -33,6 +33,35 @@ def test_spatial_jobs_cover_each_canonical_triple_once():
     assert seen == want
 
 
+def test_cell_jobs_cover_every_cell_multiset_once():
+    """With every pair of cells near, the DDD cell jobs cover each multiset of
+    cells once, and the DDR/DRR jobs each ordered role pattern once."""
+    n = 5
+    rng_ = (np.arange(n) * 10, np.arange(n) * 10 + 10)
+    allnb = lambda v, occ: [int(c) for c in np.nonzero(occ)[0]]
+    near = lambda a, b: True
+    seen = [tuple(sorted(j[4])) for j in voxels.cell_jobs("DDD", rng_, rng_, allnb, near)]
+    assert len(seen) == len(set(seen))
+    assert set(seen) == {(a, b, c) for a in range(n) for b in range(a, n) for c in range(b, n)}
+    drr = [(j[4][0],) + tuple(sorted(j[4][1:])) for j in voxels.cell_jobs("DRR", rng_, rng_, allnb, near)]
+    assert len(drr) == len(set(drr)) == n * n * (n + 1) // 2
+    ddr = [j[4] for j in voxels.cell_jobs("DDR", rng_, rng_, allnb, near)]
+    # ordered data-cell pairs (u, v) with u == v once, u != v both ways, each with every random cell
+    assert len(ddr) == len(set(ddr)) == n * n * n
+    for j in voxels.cell_jobs("DDD", rng_, rng_, allnb, near):
+        for (lo, hi), c in zip(j[1], j[4]):
+            assert lo == c * 10 and hi == c * 10 + 10
+
+
+def test_jackknife_from_groups_arithmetic():
+    """JK_r = full - (groups touching r), on made-up group histograms."""
+    groups = [frozenset({0}), frozenset({0, 1}), frozenset({1, 2}), frozenset({2})]
+    hs = [np.full(4, v, dtype=np.uint64) for v in (1, 10, 100, 1000)]
+    full, jk = voxels.jackknife_from_groups(hs, groups, 3)
+    assert (full == 1111).all()
+    assert (jk[0] == 1100).all() and (jk[1] == 1001).all() and (jk[2] == 11).all()
+
+
 def _setup(seed):
     d = synth.blobs(2500, n_blobs=12, sigma=5.0, box=130.0, seed=seed)
     r = synth.uniform(2000, box=130.0, seed=seed + 1)
@@ -136,3 +165,50 @@ def test_count_batch_into_mixed_kinds():
         assert np.array_equal(got[2], single[3] + single[4])
         assert np.array_equal(got[3], single[5])
         assert all(g.sum() > 0 for g in got)
+
+
+@pytest.mark.gpu
+def test_jackknife_by_cells_equals_subsample_counts():
+    """Jackknife subsamples (one region of points removed from both catalogs)
+    from one cell decomposition equal the direct counts of the subsamples,
+    for the histograms whose loop compares indices of one catalog only (DDD,
+    DRR, RRR; the D-D-R loop compares a data index with a random index, so
+    removing points shifts that comparison and its subsamples are counted
+    directly)."""
+    d = synth.lightcone(3000, clustered=True, seed=21)
+    r = synth.lightcone(3000, seed=22)
+    # 2 x 2 angular regions of the flat-sky slab, as region ids 0..3; the
+    # catalogs in region order
+    reg = lambda x: (np.clip(((x[:, 0] / x[:, 2] + np.deg2rad(10)) / np.deg2rad(20) * 2).astype(int), 0, 1) * 2
+                     + np.clip(((x[:, 1] / x[:, 2] + np.deg2rad(10)) / np.deg2rad(20) * 2).astype(int), 0, 1))
+    d, r = d[np.argsort(reg(d), kind="stable")], r[np.argsort(reg(r), kind="stable")]
+    rd, rr = reg(d), reg(r)
+    sd = np.searchsorted(rd, np.arange(4), "left"), np.searchsorted(rd, np.arange(4), "right")
+    sr = np.searchsorted(rr, np.arange(4), "left"), np.searchsorted(rr, np.arange(4), "right")
+    lo, hi = voxels.cell_boxes([d, r], [sd[0], sr[0]], [sd[1], sr[1]], 4)
+    neighbours, near = voxels.box_near(lo, hi, 40.0 * 1.001)
+    kinds = {"DDD": tpcf.LOOP_SAME, "DRR": tpcf.LOOP_ONE, "RRR": tpcf.LOOP_SAME}
+    with tpcf.Engine(0) as eng:
+        hd, hr = eng.catalog(d), eng.catalog(r)
+        cat = {"D": hd, "R": hr}
+        specs, jobs, outs, per_kind = [], [], [], {}
+        for k in kinds:
+            cj, gid, groups = voxels.jackknife_groups(k, sd, sr, neighbours, near)
+            base = max(outs) + 1 if outs else 0
+            for j, g in zip(cj, gid):
+                specs.append(tpcf.make_spec(tpcf.TRIANGLE, LOOP[j[2]], TP))
+                jobs.append(eng.job([cat[x] for x in j[0]], j[1], global_index=j[3]))
+                outs.append(base + g)
+            per_kind[k] = (base, groups)
+        got = eng.count_batch_into(specs, jobs, outs, max(outs) + 1)
+        for k, loop in kinds.items():
+            base, groups = per_kind[k]
+            full, jk = voxels.jackknife_from_groups(got[base:base + len(groups)], groups, 4)
+            sp = tpcf.make_spec(tpcf.TRIANGLE, loop, TP)
+            assert np.array_equal(full, eng.count(sp, eng.job([cat[x] for x in k]))), k
+            for rg in range(4):
+                sub = {"D": eng.catalog(d[rd != rg]), "R": eng.catalog(r[rr != rg])}
+                assert jk[rg].sum() > 0
+                assert np.array_equal(jk[rg], eng.count(sp, eng.job([sub[x] for x in k]))), (k, rg)
+                for h in sub.values():
+                    eng.release(h)
