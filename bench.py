@@ -558,8 +558,15 @@ def run_voxel(args):
     longest counted side, 40); the catalogs are ordered by voxel.  One step is
     ONE launch of: the four full histograms (DDD, DDR, DRR, RRR), every
     canonical neighbour-voxel job of each (summed on the device into one
-    histogram per kind, which must equal the full one exactly), and the 16
-    jackknife subsamples (one 4x4 angular cell left out) x 4 histograms."""
+    histogram per kind, which must equal the full one exactly), and the jobs
+    of the 16 jackknife subsamples (one 4x4 angular cell left out) x 4
+    histograms: DDR subsamples as jobs of their own (its loop compares data
+    and random indices, so removing points changes that comparison), the
+    DDD, DRR and RRR subsamples from one decomposition of the region-ordered
+    catalogs into jobs grouped by the regions they touch (summed on the
+    device per group; a subsample is the full count minus the groups that
+    touch its region).  The first call also counts those subsamples directly
+    and checks that they are identical."""
     import tpcf
     import synth
     import voxels
@@ -595,34 +602,75 @@ def run_voxel(args):
         for rl, rg, loop, glob in voxels.spatial_jobs(k, (sd, ed), (sr, er), grid):
             add(spec[loops[loop]], eng.job([cat[x] for x in rl], rg, global_index=glob), 4 + o)
             nvox += 1
-    for reg in range(16):  # outputs 8-71: jackknife subsamples
+    sub = []
+    for reg in range(16):  # outputs 8-23: DDR jackknife subsamples
         jd, jr = eng.catalog(d[rd != reg]), eng.catalog(r[rr != reg])
-        jc = {"D": jd, "R": jr}
-        for o, (k, lp) in enumerate(kinds):
-            add(spec[lp], eng.job([jc[x] for x in roles[k]]), 8 + 4 * reg + o)
-    n_out = 8 + 64
+        sub.append({"D": jd, "R": jr})
+        add(spec[tpcf.LOOP_ONE], eng.job([sub[reg][x] for x in "DDR"]), 8 + reg)
+    # DDD, DRR, RRR subsamples from one decomposition of the region-ordered catalogs
+    gd, gr = np.argsort(rd, kind="stable"), np.argsort(rr, kind="stable")
+    dg, rg_, rdg, rrg = d[gd], r[gr], rd[gd], rr[gr]
+    cd = np.searchsorted(rdg, np.arange(16), "left"), np.searchsorted(rdg, np.arange(16), "right")
+    cr = np.searchsorted(rrg, np.arange(16), "left"), np.searchsorted(rrg, np.arange(16), "right")
+    blo, bhi = voxels.cell_boxes([dg, rg_], [cd[0], cr[0]], [cd[1], cr[1]], 16)
+    neighbours, near = voxels.box_near(blo, bhi, 40.0 * 1.001)  # longest counted side < 40
+    hdg, hrg = eng.catalog(dg), eng.catalog(rg_)
+    gcat = {"D": hdg, "R": hrg}
+    group_base, n_out = {}, 24
+    for k, lp in kinds:
+        if k == "DDR":
+            continue
+        cj, gid, groups = voxels.jackknife_groups(k, cd, cr, neighbours, near)
+        for j, g in zip(cj, gid):
+            add(spec[loops[j[2]]], eng.job([gcat[x] for x in j[0]], j[1], global_index=j[3]), n_out + g)
+        group_base[k] = (n_out, groups)
+        n_out += len(groups)
+
+    def jackknife(hs):
+        """16 x 4 subsample histograms (region-major, DDD DDR DRR RRR)."""
+        out = {}
+        for k, (base, groups) in group_base.items():
+            out[k] = voxels.jackknife_from_groups(hs[base:base + len(groups)], groups, 16)[1]
+        out["DDR"] = [hs[8 + reg] for reg in range(16)]
+        return [out[k][reg] for reg in range(16) for k, _ in kinds]
+
     batch = eng.prepare(specs, jobs, outs, n_out)
     t0 = time.perf_counter()
     hs = eng.count_prepared(batch)
     first_s = time.perf_counter() - t0  # includes views and planning of every job
+    # the subsamples counted as jobs of their own, once, for the identity check
+    direct = eng.count_batch([spec[lp] for reg in range(16) for k, lp in kinds],
+                             [eng.job([sub[reg][x] for x in roles[k]]) for reg in range(16) for k, _ in kinds])
+    jk_exact = all(np.array_equal(a, b) for a, b in zip(jackknife(hs), direct))
+    # the reference-loop triangles of the histograms a step delivers: the full
+    # and voxel jobs, and every subsample as its own loop (the region
+    # decomposition jobs are the means, not outputs)
+    n_region = len(jobs) - 4 - nvox - 16
+    units = (sum(eng.loop_units(sp, jb) for sp, jb in zip(specs[:4 + nvox + 16], jobs[:4 + nvox + 16]))
+             + sum(eng.loop_units(spec[lp], eng.job([sub[reg][x] for x in roles[k]]))
+                   for reg in range(16) for k, lp in kinds if k != "DDR"))
     for _ in range(max(0, args.warmup - 1)):
         eng.count_prepared(batch)
     ms, wall, st = [], [], None
     for _ in range(args.steps):
         t0 = time.perf_counter()
         hs = eng.count_prepared(batch)
+        jk = jackknife(hs)
         wall.append((time.perf_counter() - t0) * 1e3)
         st = eng.stats()
         ms.append(st["kernel_ms"])
     exact = [bool(np.array_equal(hs[o], hs[4 + o])) for o in range(4)]
     mean = statistics.mean(ms) / 1e3
-    _line("triangles/s (bit-exact histos)", st["loop_units"] / mean, "triangles/s", args,
+    _line("triangles/s (bit-exact histos)", units / mean, "triangles/s", args,
           {"workload": "light cone 100k clustered + 100k uniform, TP s8 q8 t16; one launch of 4 full histograms "
                        "+ %d canonical neighbour-voxel jobs (10x10x10 voxels, summed per kind on the device) "
-                       "+ 16x4 jackknife jobs" % nvox, "jobs": len(jobs),
+                       "+ 16 jackknife subsamples x 4 histograms (DDR: 16 jobs; DDD, DRR, RRR: %d jobs of the "
+                       "region decomposition in %d groups)" % (nvox, n_region, n_out - 24),
+           "jobs": len(jobs), "jackknife_equals_subsample_counts": jk_exact,
            "voxel_jobs": nvox, "occupied_voxels": [int((ed > sd).sum()), int((er > sr).sum())],
            "voxel_sum_equals_full": exact, "counted_full": [int(hs[o].sum()) for o in range(4)],
-           "triangles_per_step": st["loop_units"], "evaluated_triangles_per_step": st["evaluated_units"],
+           "triangles_per_step": units, "launched_loop_triangles_per_step": st["loop_units"],
+           "evaluated_triangles_per_step": st["evaluated_units"],
            "binned_triangles_per_step": st["binned_units"], "tasks": st["tasks"],
            "first_call_s": first_s, "launch_shape": {"hist_copies": st["hist_copies"], "ctas_per_sm": st["ctas_per_sm"]}},
           ms_per_step=mean * 1e3, wall_ms_per_step=statistics.mean(wall), p50_ms=statistics.median(ms),
@@ -631,8 +679,8 @@ def run_voxel(args):
           roofline={"bound": "issue", "achieved": W_TP * st["binned_units"] / (st["main_kernel_ms"] / 1e3) / 1e12,
                     "unit": "Tinst/s", "per_unit": "58 lane-instructions per binned triangle"})
     eng.close()
-    if not all(exact):
-        print("voxel sums differ from the full histograms", exact, file=sys.stderr)
+    if not all(exact) or not jk_exact:
+        print("voxel sums or jackknife subsamples differ", exact, jk_exact, file=sys.stderr)
         return 1
     return 0
 
