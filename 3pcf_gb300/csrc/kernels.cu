@@ -1175,6 +1175,9 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
     const TaskGeom g = task_geom(J, task);
     const uint32_t n = p.n, n2 = (uint32_t)p.n * p.n, len = (uint32_t)p.len;
     const uint32_t m = n + 2, mm = m * m, u2 = (uint32_t)ts_u2(p);  // multiset accumulator
+    // Symmetric tasks (one catalog in all three roles): tiles a <= b <= c and,
+    // on diagonal tile pairs, positions i <= j <= k, so that every multiset
+    // {i, j, k} is visited once and counted for all its orderings.
     const bool sym = ((task.x >> TASK_PRED_SHIFT) & TASK_PRED_MASK) == PRED_SAME;
     const bool diag_ij = task.x & TASK_DIAG_IJ, diag_jk = task.x & TASK_DIAG_JK;
     for (int t = pp.tid; t < 3 * TILE; t += TS_GROUP_THREADS) {
@@ -1192,10 +1195,6 @@ __device__ void three_side_task(const DevJob& J, uint4 task, const ThreeParams& 
         // (The planner flags tile pairs A-B and A-C that are not wholly within
         // reach; B-C pairs are checked here on the half-tile boxes.)
         const bool chk_b = task.x & TASK_CHECK_B, chk_c = task.x & TASK_CHECK_C;
-        // Symmetric tasks (one catalog in all three roles): tiles a <= b <= c
-        // and, on diagonal tile pairs, positions i <= j <= k, so that every
-        // multiset {i, j, k} is visited once and counted for each of its
-        // distinct orderings.
         tile_boxes(P, g, BX, warp, lane);
         pp.sync();
         const float reach = p.hi * (1.0f + 1e-5f), reach2 = reach * reach;
