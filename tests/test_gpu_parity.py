@@ -318,6 +318,30 @@ def test_three_side_clean_spread_catalog(eng, axis):
     eng.release(h)
 
 
+@pytest.mark.parametrize("overflow", [tpcf.OVERFLOW_COMPAT, tpcf.OVERFLOW_CLEAN])
+@pytest.mark.parametrize("axis", [(16, 0.0, 40.0), (50, 0.0, 30.0)])
+def test_three_side_every_launch_shape(eng, overflow, axis):
+    """One catalog in all roles (multiset counting) and two catalogs (ordered
+    tasks) in one batch, counted repeatedly so that the autotuner runs every
+    launch shape (histogram copies per CTA, the grouped kernel, the global
+    histogram; 50 bins do not fit shared memory at all): the oracle's counts
+    every time."""
+    d = synth.blobs(300, n_blobs=4, sigma=5.0, box=60.0, seed=47)
+    r = synth.lattice_mix(260, box=60.0, frac=0.4, seed=48)
+    hd, hr = eng.catalog(d), eng.catalog(r)
+    s = tpcf.make_spec(tpcf.THREE_SIDE, tpcf.LOOP_ALL, [axis], overflow=overflow)
+    clean = overflow == tpcf.OVERFLOW_CLEAN
+    combos = [([hd, hd, hd], [d, d, d]), ([hr, hr, hr], [r, r, r]), ([hd, hr, hr], [d, r, r])]
+    want = [oracle.three_side(c, axis[1], axis[2], axis[0], clean=clean)[0] for _, c in combos]
+    jobs = [eng.job(h) for h, _ in combos]
+    for _ in range(4):
+        got = eng.count_batch([s] * 3, jobs)
+        for g, w in zip(got, want):
+            assert np.array_equal(g, w)
+    eng.release(hd)
+    eng.release(hr)
+
+
 def test_three_side_clean_batch_of_jobs(eng):
     """Several clean three-side jobs with a 32^3-bin histogram in one launch
     (one CTA per SM of task pipelines that meet to flush at every change of
