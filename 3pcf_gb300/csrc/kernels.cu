@@ -232,25 +232,24 @@ __device__ void tp_geom(double d0, double d1, double d2, const TriParams& p, int
 constexpr unsigned int FLUSH_EVERY = 256;  // tasks between histogram flushes (u32 safety)
 constexpr uint32_t TASK_NONE = 0xFFFFFFFFu;
 
-// Swizzled shared histograms: bin b of a copy lives at word hist_pos(b), its
-// low five bits (the bank) XORed with the next two 5-bit groups, so that the
-// lanes of one atomic instruction whose bins differ only in higher digits
-// (n^2 i2 + n i1 + i0 with n = 32 puts every lane of a three-side row in one
-// bank) spread over the banks.  It permutes each aligned group of 32 words;
-// copies are hist_stride(len) words apart.
+// Swizzled shared histograms (three-side kernels): bin b of a copy lives at
+// word hist_pos(b), its low five bits (the bank) XORed with the next two 5-bit
+// groups, so that the lanes of one atomic instruction whose bins differ only
+// in higher digits (n^2 i2 + n i1 + i0 with n = 32 puts every lane of a
+// three-side row in one bank) spread over the banks.  It permutes each
+// aligned group of 32 words, so a copy takes hist_stride(words) words.
 __host__ __device__ constexpr int hist_stride(int len) { return (len + 31) & ~31; }
 __device__ __forceinline__ unsigned hist_pos(unsigned b) { return b ^ (((b >> 5) ^ (b >> 10)) & 31u); }
 
-template <bool SWZ = false>
+// Adds 'copies' shared histograms of len bins (len words apart) into the
+// job's 64-bit histogram and clears them.
 __device__ __forceinline__ void flush_hist(unsigned int* H, int copies, int len, unsigned long long* g) {
     __syncthreads();
-    const int stride = SWZ ? hist_stride(len) : len;
     for (int b = threadIdx.x; b < len; b += blockDim.x) {
-        const int at = SWZ ? (int)hist_pos((unsigned)b) : b;
         unsigned long long sum = 0;
         for (int c = 0; c < copies; c++) {
-            sum += H[c * stride + at];
-            H[c * stride + at] = 0;
+            sum += H[c * len + b];
+            H[c * len + b] = 0;
         }
         if (sum) atomicAdd(g + b, sum);
     }
