@@ -474,7 +474,8 @@ def impl_ours(args):
 
 
 # ---------------------------------------------------------------------------
-# Other workloads (python bench.py --config NAME); the default is configs[1].
+# Other workloads (python bench.py --config NAME); the default is the 10k + 10k
+# triangle-parametrization workload above.
 
 def _line(metric, value, unit, args, config, **kw):
     d = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
@@ -485,7 +486,7 @@ def _line(metric, value, unit, args, config, **kw):
 
 
 def run_three_side(args):
-    """configs[0]: three-side DDD + RRR, 1000 clustered + 1000 uniform points in a
+    """Three-side DDD + RRR, 1000 clustered + 1000 uniform points in a
     100^3 cube, 16 bins on [0,40) (reference overflow aliasing), 2e9 triangles."""
     import tpcf
     import synth
@@ -552,7 +553,7 @@ def _jackknife_region(xyz):
 
 
 def run_voxel(args):
-    """configs[2]: 100k clustered + 100k uniform points in a 20x20 degree
+    """100k clustered + 100k uniform points in a 20x20 degree
     light-cone slab (depth 500-1500, density falling as r^-2).  The common
     bounding box is cut into 10x10x10 voxels (~53x54x103, each edge above the
     longest counted side, 40); the catalogs are ordered by voxel.  One step is
@@ -686,7 +687,7 @@ def run_voxel(args):
 
 
 def run_lattice(args):
-    """configs[3]: 500k points uniform in a 500^3 box with 30 % on the integer
+    """500k points uniform in a 500^3 box with 30 % on the integer
     lattice; three-side 32 bins on [0,32) restricted to triples whose sides are
     all below 32; FP32 path vs all-FP64 kernel, counts identical."""
     import tpcf
@@ -731,9 +732,9 @@ def run_lattice(args):
 
 
 def run_serving(args):
-    """configs[4]: 2000 jobs with Poisson arrivals (rate --rate per second, seed
+    """Serving: 2000 jobs with Poisson arrivals (rate --rate per second, seed
     2) on resident catalogs whose sizes are log-uniform in [500, 50000], drawn
-    from the clustered-cube (configs[0]) and light-cone (configs[2]) generators;
+    from the clustered-cube and light-cone generators;
     70 % triangle jobs (DDD/DDR/DRR/RRR), 30 % pair jobs (DD/DR/RR, 700 bins on
     [0,70)); p50/p99 latency from arrival to histogram and throughput."""
     import tpcf
