@@ -692,7 +692,8 @@ def run_lattice(args):
     all below 32; FP32 path vs all-FP64 kernel, counts identical."""
     import tpcf
     import synth
-    pts = synth.lattice_mix(500000, box=500.0, frac=0.3, seed=3)
+    npts = args.lattice_points  # 500k; fewer at the same density for profiling
+    pts = synth.lattice_mix(npts, box=500.0 * (npts / 500000.0) ** (1.0 / 3.0), frac=0.3, seed=3)
     eng = tpcf.Engine(0)
     h = eng.catalog(pts)
     job = eng.job([h, h, h])
@@ -716,8 +717,9 @@ def run_lattice(args):
     h32s = h32 if full else eng.count(s32, js)
     mean = statistics.mean(ms) / 1e3
     _line("triangles/s (bit-exact histos)", st["loop_units"] / mean, "triangles/s", args,
-          {"workload": "500k points, 500^3 box, 30 % on the integer lattice, three-side 32 bins on [0,32), "
-                       "sides < 32 only", "triangles_per_step": st["loop_units"],
+          {"workload": "%dk points, %.4g^3 box, 30 %% on the integer lattice, three-side 32 bins on [0,32), "
+                       "sides < 32 only" % (npts // 1000, 500.0 * (npts / 500000.0) ** (1.0 / 3.0)),
+           "triangles_per_step": st["loop_units"],
            "evaluated_triangles_per_step": st["evaluated_units"], "tasks": st["tasks"],
            "counted": int(h32.sum())},
           ms_per_step=mean * 1e3, wall_ms_per_step=st["total_ms"],
@@ -817,6 +819,8 @@ def main():
     ap.add_argument("--jobs", type=int, default=2000, help="serving: number of jobs")
     ap.add_argument("--rate", type=float, default=25.0, help="serving: Poisson arrival rate (jobs/s)")
     ap.add_argument("--fp64-slab", action="store_true", help="lattice500k: FP64 comparison on the slab x < 100 only")
+    ap.add_argument("--lattice-points", type=int, default=500000,
+                    help="lattice500k: number of points (same density; smaller cases for profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
