@@ -464,6 +464,46 @@ static int three_side_bin_of_d2(float d2, float lo, float hi, float bw, int n) {
     return (int)q;
 }
 
+// The pair code of a squared separation d2 (ref_bin_tp of the pair program,
+// src/2pcf_C_version.cc:57-86, on sqrtf(d2)): 0 below lo, bin + 1 inside,
+// nbins + 2 at or above hi.  IEEE single operations, as on the device.
+static int pair_code_of_d2(float d2, float lo, float hi, float bw, int n) {
+    volatile float d = sqrtf(d2);
+    if (d < lo) return 0;
+    if (d >= hi) return n + 2;
+    volatile float x = d - lo;
+    volatile float q = x / bw;
+    return (int)q + 1;
+}
+
+// Smallest non-negative float d2 whose code (a non-decreasing function of
+// d2) is >= v, by bisection over the ordered bit patterns of floats.
+template <class Code>
+static float smallest_d2_with_code(int v, Code code) {
+    uint32_t lo = 0, hi = 0x7F800000u;  // +0 .. +inf (the largest code)
+    while (lo < hi) {
+        const uint32_t mid = lo + (hi - lo) / 2;
+        float x;
+        memcpy(&x, &mid, 4);
+        if (code(x) >= v) hi = mid;
+        else lo = mid + 1;
+    }
+    float r;
+    memcpy(&r, &lo, 4);
+    return r;
+}
+
+static bool pair_thresholds(PairParams& p) {
+    if (p.n + 4 > PR_UMAX) return false;
+    if (std::max(fabs((double)p.lo), fabs((double)p.hi)) / (double)p.bw > 16384.0) return false;
+    p.inv_bw = 1.0f / p.bw;
+    p.u[0] = -INFINITY;
+    for (int v = 1; v <= p.n + 2; v++)
+        p.u[v] = smallest_d2_with_code(v, [&](float x) { return pair_code_of_d2(x, p.lo, p.hi, p.bw, p.n); });
+    for (int v = p.n + 3; v < PR_UMAX; v++) p.u[v] = NAN;
+    return true;
+}
+
 // Thresholds u[v] (smallest float d2 >= 0 with bin >= v) by bisection over
 // the ordered bit patterns of non-negative floats; the bin is a
 // non-decreasing function of d2 (sqrt, subtraction, division and truncation
@@ -593,6 +633,7 @@ Binning make_binning(const tpcf_spec& sp) {
         p.lo = sp.axis[0].lo;
         p.hi = sp.axis[0].hi;
         p.bw = ref_bw(p.lo, p.hi, p.n);
+        p.fast = pair_thresholds(p) ? 1 : 0;
         b.len = p.n;
         b.lmax = (double)p.hi * (1 + 1e-6) + 1e-6;
     } else {

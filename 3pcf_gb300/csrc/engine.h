@@ -105,9 +105,18 @@ struct ThreeParams {
     int zcode;  // bin of a zero-length side (nbins + 1 at or above hist_max)
 };
 
+constexpr int PR_UMAX = 704;  // squared-length thresholds of up to 700 pair bins
+
 struct PairParams {
     int n;
     float lo, hi, bw;
+    // Bins from squared lengths (guarded FP32 kernel, when fast != 0): the
+    // code of a separation d is 0 below lo, bin + 1 inside (up to nbins + 1
+    // where rounding gives bin nbins), nbins + 2 at or above hi; u[v] is the
+    // smallest float d2 whose code is >= v, u[0] = -inf, u[nbins + 3] = NaN.
+    int fast = 0;
+    float inv_bw = 0.f;
+    float u[PR_UMAX];
 };
 
 // Exact glibc-acosf exception table on the device.

@@ -1533,8 +1533,32 @@ constexpr int PR_WARPS = 8;
 constexpr int PR_THREADS = PR_WARPS * 32;
 constexpr size_t PR_SMEM_FIXED = 2 * TILE * sizeof(float4);
 
+// Pair bin of the separation a-b, -1 if not counted.  The guarded FP32
+// kernel works on the squared separation: a first guess from an approximate
+// square root (within one step) corrected against the exact thresholds U of
+// the neighbouring steps of the code (0 below lo, bin + 1, nbins + 2 at or
+// above hi); the plain FP64 kernel evaluates the reference's formula.
+template <bool FP64>
+__device__ __forceinline__ int pair_bin(float4 a, float4 b, const PairParams& p, const float* U) {
+    if (!FP64 && p.fast) {
+        const float dx = __fsub_rn(a.x, b.x), dy = __fsub_rn(a.y, b.y), dz = __fsub_rn(a.z, b.z);
+        float d2 = __fmul_rn(dx, dx);
+        d2 = __fadd_rn(d2, __fmul_rn(dy, dy));
+        d2 = __fadd_rn(d2, __fmul_rn(dz, dz));
+        float da;
+        asm("sqrt.approx.f32 %0, %1;" : "=f"(da) : "f"(d2));
+        int v = __float2int_rz(__fmul_rn(__fsub_rn(da, p.lo), p.inv_bw)) + 1;
+        v = min(max(v, 0), p.n + 2);
+        v = v - 1 + (d2 >= U[v] ? 1 : 0) + (d2 >= U[v + 1] ? 1 : 0);
+        return v >= 1 && v <= p.n ? v - 1 : -1;
+    }
+    const int bn = ref_bin_tp<FP64>(ref_dist<FP64>(a, b), p.lo, p.hi, p.n, 0);
+    return bn >= 0 && bn < p.n ? bn : -1;
+}
+
 template <bool FP64, int PRED>
-__device__ void pair_task(const DevJob& J, uint4 task, const PairParams& p, float4* P, unsigned int* Hw) {
+__device__ void pair_task(const DevJob& J, uint4 task, const PairParams& p, const float* U, float4* P,
+                          unsigned int* Hw) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int a0 = J.tile_start[0][task.y], nA = J.tile_start[0][task.y + 1] - a0;
     const int b0 = J.tile_start[1][task.z], nB = J.tile_start[1][task.z + 1] - b0;
@@ -1555,8 +1579,8 @@ __device__ void pair_task(const DevJob& J, uint4 task, const PairParams& p, floa
             if (diag && j < i) continue;  // self pairs (j == i) are counted, as the reference's j >= i
             const float4 pj = P[TILE + j];
             if (PRED == PRED_SAME && pkey(pj) < ki) continue;
-            const int b = ref_bin_tp<FP64>(ref_dist<FP64>(pi, pj), p.lo, p.hi, p.n, 0);
-            if (b >= 0 && b < p.n) atomicAdd(Hw + b, 1u);
+            const int b = pair_bin<FP64>(pi, pj, p, U);
+            if (b >= 0) atomicAdd(Hw + b, 1u);
         }
     }
     __syncthreads();
@@ -1570,6 +1594,9 @@ pair_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ tasks, un
     float4* P = reinterpret_cast<float4*>(smem);
     unsigned int* H = reinterpret_cast<unsigned int*>(smem + PR_SMEM_FIXED);
     __shared__ uint4 s_task;
+    __shared__ float s_u[PR_UMAX];
+    if (!FP64 && p.fast)
+        for (int v = threadIdx.x; v < PR_UMAX; v += blockDim.x) s_u[v] = p.u[v];
     for (int b = threadIdx.x; b < copies * p.n; b += blockDim.x) H[b] = 0;
     unsigned int* Hw = H + ((threadIdx.x >> 5) % copies) * p.n;
     int cur = -1;
@@ -1590,8 +1617,10 @@ pair_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ tasks, un
         cur = slot;
         if (slot < 0) break;
         since++;
-        if (((task.x >> TASK_PRED_SHIFT) & TASK_PRED_MASK) == PRED_SAME) pair_task<FP64, PRED_SAME>(jobs[slot], task, p, P, Hw);
-        else pair_task<FP64, PRED_NONE>(jobs[slot], task, p, P, Hw);
+        if (((task.x >> TASK_PRED_SHIFT) & TASK_PRED_MASK) == PRED_SAME)
+            pair_task<FP64, PRED_SAME>(jobs[slot], task, p, s_u, P, Hw);
+        else
+            pair_task<FP64, PRED_NONE>(jobs[slot], task, p, s_u, P, Hw);
     }
 }
 
@@ -1833,8 +1862,8 @@ pair_kernel_noalloc(unsigned int* task_counter, int ntA, int ntB, int same, int 
         const unsigned int a = t / (unsigned int)ntB, b = t % (unsigned int)ntB;
         if (same && b < a) continue;
         uint4 task = make_uint4((same && a == b ? TASK_DIAG_IJ : 0u), a, b, 0u);
-        if (pred_same) pair_task<FP64, PRED_SAME>(J, task, p, P, Hw);
-        else pair_task<FP64, PRED_NONE>(J, task, p, P, Hw);
+        if (pred_same) pair_task<FP64, PRED_SAME>(J, task, p, nullptr, P, Hw);
+        else pair_task<FP64, PRED_NONE>(J, task, p, nullptr, P, Hw);
     }
     flush_hist(H, copies, p.n, J.hist);
 }

@@ -409,6 +409,23 @@ def test_pairs_vs_oracle(eng, axis):
     eng.release(hr)
 
 
+@pytest.mark.parametrize("axis", [(10, 0.0, 10.0), (7, 1.5, 12.0), (2000, 0.0, 40.0)])
+def test_pairs_bin_edges(eng, axis):
+    """Lattice points (separations exactly on bin edges, zero separations
+    between duplicates): the squared-length thresholds of the guarded kernel
+    (up to 700 bins; 2000 bins take the reference formula) and the FP64
+    kernel give the oracle's counts."""
+    pts = synth.lattice_mix(2500, box=40.0, frac=0.8, seed=49)
+    pts = np.concatenate([pts, pts[:300]])
+    h = eng.catalog(pts)
+    for prec in (tpcf.GUARDED_FP32, tpcf.PLAIN_FP64):
+        got = eng.count(tpcf.make_spec(tpcf.PAIR, tpcf.LOOP_SAME, [axis], precision=prec), eng.job([h, h]))
+        want, _ = oracle.pair([pts, pts], 0, axis[1], axis[2], axis[0])
+        assert got.sum() > 0
+        assert np.array_equal(got, want), prec
+    eng.release(h)
+
+
 def test_empty_and_tiny_catalogs(eng):
     spec = ((8, 2.0, 10.0), (8, 1.0, 3.0), (16, 0.0, 1.0))
     one = np.array([[1.0, 2.0, 3.0]], dtype=np.float32)
