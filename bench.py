@@ -75,7 +75,9 @@ def issue_peak(device=0):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 50 ms, each sample
+    stamped with the host time it arrived (summary() keeps those inside a
+    window, e.g. the timed region)."""
 
     def __init__(self, index):
         self.index = index
@@ -88,7 +90,7 @@ class ClockSampler:
                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -96,7 +98,7 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.time(), line.strip()))
 
     def __exit__(self, *a):
         if self.proc:
@@ -106,10 +108,12 @@ class ClockSampler:
             except Exception:
                 self.proc.kill()
 
-    def summary(self):
+    def summary(self, window=None):
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for t, ln in self.lines:
+            if window is not None and not (window[0] <= t <= window[1]):
+                continue
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -338,15 +342,16 @@ def impl_ours(args):
     jobs = [eng.job([hd, hd, hd]), eng.job([hd, hd, hr]), eng.job([hd, hr, hr]), eng.job([hr, hr, hr])]
     sp32 = specs(tpcf.GUARDED_FP32)
     flush = L2Flush(local)
-    for _ in range(args.warmup):
-        eng.count_batch(sp32, jobs)
-    eng.stats()
     dev_ms, main_ms, wall_ms = [], [], []
     launches = 0
     units = evaluated = recheck = binned = 0
     ref_hists = None
-    with ClockSampler(local) as clocks:
+    with ClockSampler(local) as clocks:  # running during the warm-up already
+        for _ in range(args.warmup):
+            eng.count_batch(sp32, jobs)
+        eng.stats()
         barrier(dist)
+        t_timed = time.time()
         for _ in range(args.steps):
             flush()
             t0 = time.perf_counter()
@@ -363,6 +368,7 @@ def impl_ours(args):
             elif any(not np.array_equal(a, b) for a, b in zip(hists, ref_hists)):
                 raise RuntimeError("histograms differ between steps")
         barrier(dist)
+        t_timed_end = time.time()
     total_s = max_over_ranks(dist, sum(dev_ms) / 1e3)
     all_units = sum_over_ranks(dist, units * args.steps)
     value = all_units / total_s
@@ -441,7 +447,7 @@ def impl_ours(args):
         lane_inst = kc["smsp__inst_executed.sum"] * kc.get("smsp__thread_inst_executed_per_inst_executed.ratio", 32.0)
         issue_frac = lane_inst / (statistics.mean(main_ms) / 1e3) / 1e12 / peak
     cpu = None if args.no_cpu_baseline else cpu_baseline_single(d)
-    csum = clocks.summary()
+    csum = clocks.summary(window=(t_timed, t_timed_end))
     line = {
         "metric": METRIC, "value": value, "unit": "triangles/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
