@@ -164,8 +164,6 @@ cudaError_t launch_radecz_to_xyz(const double* ra, const double* dec, const doub
 size_t triangle_smem_bytes(int hist_len, int hist_copies);
 size_t three_side_smem_bytes(const ThreeParams& p, int hist_copies, int groups);
 size_t pair_smem_bytes(int hist_len, int hist_copies);
-int triangle_block_threads();
-int pair_block_threads();
 
 }  // namespace tpcf
 #endif

@@ -1649,8 +1649,6 @@ size_t three_side_smem_bytes(const ThreeParams& p, int copies, int groups) {
     return pipe + (size_t)words * copies * 4;
 }
 size_t pair_smem_bytes(int hist_len, int copies) { return PR_SMEM_FIXED + (size_t)hist_len * copies * 4; }
-int triangle_block_threads() { return TRI_THREADS; }
-int pair_block_threads() { return PR_THREADS; }
 
 // Every counting kernel may use the device's whole opt-in shared memory per
 // block.  Set once per device, before any launch or graph capture, and never
