@@ -1017,7 +1017,10 @@ __device__ __forceinline__ uint32_t side_code3_pts(float4 a, float4 b, const Thr
         d2 = __fadd_rn(d2, __fmul_rn(dz, dz));
         float da;
         asm("sqrt.approx.f32 %0, %1;" : "=f"(da) : "f"(d2));
-        int v = __float2int_rz(__fmul_rn(__fsub_rn(da, p.lo), p.inv_bw));
+        // the guess rounds to nearest: where d reaches hi the code jumps over
+        // nbins (unless rounding gives bin nbins), and a truncated guess just
+        // below hi would be two steps short
+        int v = __float2int_rn(__fmul_rn(__fsub_rn(da, p.lo), p.inv_bw));
         v = min(max(v, 0), p.n + 1);
         v = v - 1 + (d2 >= U[v] ? 1 : 0) + (d2 >= U[v + 1] ? 1 : 0);
         if (v > p.n) return p.clean ? TS_FAR : (uint32_t)(p.n + 1) * scale;
@@ -1547,7 +1550,9 @@ __device__ __forceinline__ int pair_bin(float4 a, float4 b, const PairParams& p,
         d2 = __fadd_rn(d2, __fmul_rn(dz, dz));
         float da;
         asm("sqrt.approx.f32 %0, %1;" : "=f"(da) : "f"(d2));
-        int v = __float2int_rz(__fmul_rn(__fsub_rn(da, p.lo), p.inv_bw)) + 1;
+        // rounded guess (as for the three-side codes: the code jumps over
+        // nbins + 1 where d reaches hi)
+        int v = __float2int_rn(__fmul_rn(__fsub_rn(da, p.lo), p.inv_bw)) + 1;
         v = min(max(v, 0), p.n + 2);
         v = v - 1 + (d2 >= U[v] ? 1 : 0) + (d2 >= U[v + 1] ? 1 : 0);
         return v >= 1 && v <= p.n ? v - 1 : -1;

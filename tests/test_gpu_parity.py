@@ -342,6 +342,18 @@ def test_three_side_every_launch_shape(eng, overflow, axis):
     eng.release(hr)
 
 
+@pytest.mark.parametrize("axis", [(32, 0.0, 32.0), (10, 0.0, 10.0), (12, 2.0, 14.0)])
+def test_three_side_clean_sides_on_hist_max(eng, axis):
+    """Integer lattice points: many sides exactly at hist_max (d = hi drops the
+    triple; the code jumps over nbins there) and on every bin edge."""
+    pts = synth.lattice_mix(500, box=36.0, frac=1.0, seed=50)
+    h = eng.catalog(pts)
+    s = tpcf.make_spec(tpcf.THREE_SIDE, tpcf.LOOP_ALL, [axis], overflow=tpcf.OVERFLOW_CLEAN)
+    want, _ = oracle.three_side([pts, pts, pts], axis[1], axis[2], axis[0], clean=True)
+    assert np.array_equal(eng.count(s, eng.job([h, h, h])), want)
+    eng.release(h)
+
+
 def test_three_side_clean_batch_of_jobs(eng):
     """Several clean three-side jobs with a 32^3-bin histogram in one launch
     (one CTA per SM of task pipelines that meet to flush at every change of
