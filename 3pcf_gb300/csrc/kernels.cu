@@ -1574,6 +1574,8 @@ __device__ void pair_task(const DevJob& J, uint4 task, const PairParams& p, cons
         P[t] = idx < nn ? J.pts[role][base + idx] : make_float4(0.f, 0.f, 0.f, 0.f);
     }
     __syncthreads();
+    // each lane keeps its two points of tile B in registers for the whole task
+    const float4 pj[2] = {P[TILE + lane], P[TILE + lane + 32]};
     for (int i = warp; i < nA; i += PR_WARPS) {
         const float4 pi = P[i];
         const int ki = pkey(pi);
@@ -1582,9 +1584,8 @@ __device__ void pair_task(const DevJob& J, uint4 task, const PairParams& p, cons
             const int j = lane + 32 * r;
             if (j >= nB) continue;
             if (diag && j < i) continue;  // self pairs (j == i) are counted, as the reference's j >= i
-            const float4 pj = P[TILE + j];
-            if (PRED == PRED_SAME && pkey(pj) < ki) continue;
-            const int b = pair_bin<FP64>(pi, pj, p, U);
+            if (PRED == PRED_SAME && pkey(pj[r]) < ki) continue;
+            const int b = pair_bin<FP64>(pi, pj[r], p, U);
             if (b >= 0) atomicAdd(Hw + b, 1u);
         }
     }
