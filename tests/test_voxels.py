@@ -53,6 +53,30 @@ def test_cell_jobs_cover_every_cell_multiset_once():
             assert lo == c * 10 and hi == c * 10 + 10
 
 
+def test_cell_jobs_with_a_sparse_neighbour_relation():
+    """A random symmetric neighbour relation: the DDD jobs cover exactly the
+    cell multisets whose cells are pairwise near, once each; DRR jobs every
+    (data cell, unordered random pair) within reach, DDR jobs every ordered
+    (data cell pair, random cell) within reach, each once."""
+    rng = np.random.default_rng(7)
+    n = 9
+    m = rng.random((n, n)) < 0.45
+    near_m = m | m.T | np.eye(n, dtype=bool)
+    rng_ = (np.arange(n) * 10, np.arange(n) * 10 + 10)
+    neighbours = lambda v, occ: [int(c) for c in np.nonzero(occ)[0] if near_m[v, c]]
+    near = lambda a, b: bool(near_m[a, b])
+    ok = lambda cells: all(near_m[x, y] for x in cells for y in cells)
+    ddd = [tuple(sorted(j[4])) for j in voxels.cell_jobs("DDD", rng_, rng_, neighbours, near)]
+    assert len(ddd) == len(set(ddd))
+    assert set(ddd) == {(a, b, c) for a in range(n) for b in range(a, n) for c in range(b, n) if ok((a, b, c))}
+    drr = [(j[4][0],) + tuple(sorted(j[4][1:])) for j in voxels.cell_jobs("DRR", rng_, rng_, neighbours, near)]
+    assert len(drr) == len(set(drr))
+    assert set(drr) == {(u, v, w) for u in range(n) for v in range(n) for w in range(v, n) if ok((u, v, w))}
+    ddr = [j[4] for j in voxels.cell_jobs("DDR", rng_, rng_, neighbours, near)]
+    assert len(ddr) == len(set(ddr))
+    assert set(ddr) == {(u, v, w) for u in range(n) for v in range(n) for w in range(n) if ok((u, v, w))}
+
+
 def test_jackknife_from_groups_arithmetic():
     """JK_r = full - (groups touching r), on made-up group histograms."""
     groups = [frozenset({0}), frozenset({0, 1}), frozenset({1, 2}), frozenset({2})]
