@@ -77,6 +77,29 @@ def test_cell_jobs_with_a_sparse_neighbour_relation():
     assert set(ddr) == {(u, v, w) for u in range(n) for v in range(n) for w in range(n) if ok((u, v, w))}
 
 
+def test_box_near_is_conservative():
+    """Two cells whose points come within the reach of each other are always
+    near (the box gap never exceeds a point distance)."""
+    rng = np.random.default_rng(8)
+    pts = rng.uniform(0, 100, size=(3000, 3)).astype(np.float32)
+    cell = (pts[:, 0] // 25).astype(int) * 4 + (pts[:, 1] // 25).astype(int)
+    order = np.argsort(cell, kind="stable")
+    pts, cell = pts[order], cell[order]
+    st = np.searchsorted(cell, np.arange(16), "left")
+    en = np.searchsorted(cell, np.arange(16), "right")
+    lo, hi = voxels.cell_boxes([pts], [st], [en], 16)
+    reach = 12.0
+    neighbours, near = voxels.box_near(lo, hi, reach)
+    sample = rng.choice(len(pts), 400, replace=False)
+    for i in sample:
+        dd = np.sqrt(((pts - pts[i]) ** 2).sum(1))
+        for c in np.unique(cell[dd < reach]):
+            assert near(int(cell[i]), int(c)) and near(int(c), int(cell[i]))
+    occ = en > st
+    for v in range(16):
+        assert v in neighbours(v, occ)
+
+
 def test_jackknife_from_groups_arithmetic():
     """JK_r = full - (groups touching r), on made-up group histograms."""
     groups = [frozenset({0}), frozenset({0, 1}), frozenset({1, 2}), frozenset({2})]
