@@ -25,11 +25,14 @@ def build_oracle():
     return LIB
 
 
-def build_all():
+def build_all(reference=None):
+    """reference: the reference checkout, if this machine has one (else
+    TPCF_REFERENCE_DIR; without either, the configured copies already in
+    oracle/_ref/src are compiled)."""
     sys.path.insert(0, HERE)
     import ref_build
     build_oracle()
-    ref_build.write_configured()
+    ref_build.write_configured(reference)
     ref_build.compile_all()
 
 

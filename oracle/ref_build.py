@@ -36,7 +36,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 SRC_OUT = os.path.join(OUT, "src")
 BIN_OUT = os.path.join(OUT, "bin")
-REFERENCE = os.environ.get("TPCF_REFERENCE_DIR", "/root/reference")
+# the reference checkout: TPCF_REFERENCE_DIR, or the argument of write_configured
+REFERENCE = os.environ.get("TPCF_REFERENCE_DIR")
 
 # name -> (program, parameters).  Parameters are the macro values as the
 # reference writes them (double literals).
@@ -106,8 +107,13 @@ def configure(program, params, text):
     raise ValueError(program)
 
 
-def write_configured(reference=REFERENCE):
-    """Step 1: write configured copies (needs the reference checkout)."""
+def write_configured(reference=None):
+    """Step 1: write configured copies (needs the reference checkout, given
+    as the argument or by TPCF_REFERENCE_DIR; without one nothing is written
+    and False is returned)."""
+    reference = reference or REFERENCE
+    if not reference:
+        return False
     src_dir = os.path.join(reference, "src")
     if not os.path.isdir(src_dir):
         return False
@@ -181,7 +187,11 @@ def binary(name):
 
 
 def main():
-    wrote = write_configured()
+    ref = sys.argv[1] if len(sys.argv) > 1 else REFERENCE
+    if not ref and not os.path.isdir(SRC_OUT):
+        print("ref_build: give the reference checkout (argument or TPCF_REFERENCE_DIR)")
+        return 1
+    wrote = write_configured(ref)
     names = compile_all()
     print("reference variants: configured=%s built=%d" % (wrote, len(names)))
     return 0

@@ -32,7 +32,8 @@ import numpy as np  # noqa: E402
 import synth  # noqa: E402
 import ref_build  # noqa: E402
 
-REFERENCE = os.environ.get("TPCF_REFERENCE_DIR", "/root/reference")
+# the reference checkout (required): TPCF_REFERENCE_DIR or the first argument
+REFERENCE = os.environ.get("TPCF_REFERENCE_DIR") or (sys.argv[1] if len(sys.argv) > 1 else None)
 
 SANDBOX_INPUTS = [
     "MICE_5degx5deg_1k_randomized.dat",
@@ -161,8 +162,9 @@ def reference_outputs():
 
 
 def main():
-    if not os.path.isdir(REFERENCE):
-        print("reference checkout not found; fixtures unchanged")
+    if not REFERENCE or not os.path.isdir(REFERENCE):
+        print("make_fixtures: give the reference checkout (TPCF_REFERENCE_DIR or the first argument);"
+              " fixtures unchanged")
         return 1
     sandbox()
     reference_outputs()

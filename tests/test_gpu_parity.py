@@ -185,11 +185,33 @@ def test_sandbox_full_sets(eng_x86, tmp_path, setname, histo):
         got = _earlier_revision_ddr(eng, hd, hr, len(d), len(r), spec)
     eng.release(hd)
     eng.release(hr)
-    _, _, want = rf.parse_triangle(rf.read_bytes(os.path.join(SANDBOX, h["file"] + ".gz")))
+    if "compare" in h:
+        # the golden file came from another build (compare_note): the
+        # reference compiled here, summed over the same chunk runs, is the pin
+        want = np.array(rf.read_bytes(os.path.join(rf.GOLDEN, h["compare"])).split(), dtype=np.uint64)
+    else:
+        _, _, want = rf.parse_triangle(rf.read_bytes(os.path.join(SANDBOX, h["file"] + ".gz")))
     got = (got & np.uint64(0xFFFFFFFF)).astype(np.int64)
-    for idx, dv in h.get("residual", {}).items():  # pinned, see residual_note
-        got[int(idx)] += dv
     assert np.array_equal(got, want.astype(np.int64)), int((got != want.astype(np.int64)).sum())
+
+
+@pytest.mark.parametrize("chunks", ["002000008", "000005009"])
+def test_lrg_rrr_chunk_jobs(eng_x86, tmp_path, chunks):
+    """Two -X 10 chunk jobs of the LRG randoms run by the reference binary
+    compiled here (tests/golden/make_lrg_rrr.py): 002000008 holds the
+    triangle whose ratio rounds to exactly Q_HI, 000005009 the triangle of
+    bin (33, 12, 17) closest to its q edge.  Byte-identical output files in
+    both precisions."""
+    eng = eng_x86
+    cat = _sandbox_cat(tmp_path, "flat_MICE_LRGs_10degx10deg.dat")
+    h = eng.catalog(cat)
+    idx = rf.voxel_indices(int(chunks), 3)
+    ranges = [rf.vox2gal(10, idx[a], len(cat)) for a in range(3)]
+    want = rf.read_bytes(os.path.join(rf.GOLDEN, "ref", "lrg_rrr_x10_%s.dat.gz" % chunks))
+    for prec in (tpcf.GUARDED_FP32, tpcf.PLAIN_FP64):
+        got = eng.count(_tp_spec(SANDBOX_SPEC, tpcf.LOOP_SAME, prec), eng.job([h, h, h], ranges))
+        assert rf.format_triangle(got, [len(cat)] * 3, SANDBOX_SPEC) == want, prec
+    eng.release(h)
 
 
 def _random_case(seed, n_d=220, n_r=200):

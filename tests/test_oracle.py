@@ -162,3 +162,16 @@ def test_geometry_fp64_oracle_matches_python_restatement():
     assert n == count
     assert np.array_equal(got, want)
     assert want.sum() > 0
+
+
+def test_lrg_rrr_chunk_job_matches_compiled_reference(tmp_path):
+    """The oracle on one -X 10 chunk job of the LRG randoms (1.56e9 triangles)
+    against the output file of the reference binary compiled here for the
+    same job: the job holding the triangle whose ratio m/s rounds to exactly
+    Q_HI (tests/golden/make_lrg_rrr.py)."""
+    cat = sandbox_catalog(tmp_path, "flat_MICE_LRGs_10degx10deg.dat")
+    idx = rf.voxel_indices(2000008, 3)
+    subs = [cat[slice(*rf.vox2gal(10, idx[a], len(cat)))] for a in range(3)]
+    hist, _ = oracle.triangle(subs, 0, SANDBOX_SPEC)
+    got = rf.format_triangle(hist, [len(cat)] * 3, SANDBOX_SPEC)
+    assert got == rf.read_bytes(os.path.join(rf.GOLDEN, "ref", "lrg_rrr_x10_002000008.dat.gz"))
