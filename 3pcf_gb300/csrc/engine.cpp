@@ -1497,8 +1497,12 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
     const bool graphs = L.graphs_ok && !(genv && genv[0] == '0');
     L.h_hist.reserve(hist_total);
     L.h_counters.reserve(8);
-    unsigned int queue_cap = (unsigned int)std::max<size_t>(L.d_queue.n, (size_t)1 << 22);
-    uint64_t dev_evaluated = 0, dev_binned = 0, replays = 0;
+    // recheck queue: at least 4M entries; TPCF_RECHECK_CAP lowers the floor
+    // (tests use it to run the overflow path: grow the queue, count again)
+    size_t queue_floor = (size_t)1 << 22;
+    if (const char* qc = getenv("TPCF_RECHECK_CAP")) queue_floor = (size_t)std::max(1L, std::atol(qc));
+    unsigned int queue_cap = (unsigned int)std::max<size_t>(L.d_queue.n, queue_floor);
+    uint64_t dev_evaluated = 0, dev_binned = 0, replays = 0, regrows = 0;
 
     // One complete count of the group with launch shape sh: zero, count,
     // recheck, copy back (replayed from a captured graph when allowed and
@@ -1602,6 +1606,7 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
                 // the recheck queue overflowed: grow it and count again
                 queue_cap =
                     (unsigned int)std::min<uint64_t>((uint64_t)counters[1] + (counters[1] >> 2) + 1024, 0xF0000000ull);
+                regrows++;
                 continue;
             }
             break;
@@ -1676,6 +1681,7 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
     L.stats.binned_units = (sp.kind == TPCF_TRIANGLE && !fp64) ? dev_binned : evaluated;
     L.stats.tasks = ntasks;
     L.stats.kernel_launches = launches * std::max<uint64_t>(1, tuned_runs);
+    L.stats.recheck_regrows = regrows;
     L.stats.total_ms =
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_wall0).count();
 }
@@ -2053,6 +2059,7 @@ tpcf_status count_jobs(tpcf_ctx* ctx, const tpcf_spec* specs, const tpcf_job* jo
             acc.loop_units += L.stats.loop_units;
             acc.evaluated_units += L.stats.evaluated_units;
             acc.recheck_units += L.stats.recheck_units;
+            acc.recheck_regrows += L.stats.recheck_regrows;
             acc.tasks += L.stats.tasks;
             acc.kernel_launches += L.stats.kernel_launches;
             acc.graph_replays += L.stats.graph_replays;

@@ -60,7 +60,7 @@ class Stats(ctypes.Structure):
                 ("main_kernel_ms", ctypes.c_double), ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
                 ("binned_units", ctypes.c_uint64), ("graph_replays", ctypes.c_uint64),
                 ("tuned_shapes", ctypes.c_uint64), ("hist_copies", ctypes.c_uint64), ("ctas_per_sm", ctypes.c_uint64),
-                ("plan_ms", ctypes.c_double)]
+                ("plan_ms", ctypes.c_double), ("recheck_regrows", ctypes.c_uint64)]
 
 
 _LIB = None

@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define TPCF_ABI_VERSION 2
+#define TPCF_ABI_VERSION 3
 
 typedef int32_t tpcf_status;
 enum {
@@ -155,6 +155,8 @@ typedef struct {
     uint64_t ctas_per_sm;        /* ... and resident CTAs per SM */
     double plan_ms;              /* host time of views, planning and the task upload
                                     (near 0 when a repeated batch reuses its plan) */
+    uint64_t recheck_regrows;    /* times the guard-band recheck queue overflowed and the
+                                    count was repeated with a larger queue */
 } tpcf_stats;
 
 typedef struct tpcf_ctx tpcf_ctx;

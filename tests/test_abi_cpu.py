@@ -29,7 +29,7 @@ def test_library_exports_every_declared_symbol():
     L = ctypes.CDLL(tpcf.LIB_PATH)
     for name in declared_symbols():
         assert hasattr(L, name), name
-    assert L.tpcf_abi_version() == 2
+    assert L.tpcf_abi_version() == 3
 
 
 def _has_gpu():
