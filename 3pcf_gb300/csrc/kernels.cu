@@ -1874,17 +1874,11 @@ pair_kernel_noalloc(unsigned int* task_counter, int ntA, int ntB, int same, int 
 
 }  // namespace tpcf
 
-namespace {
-struct NoAllocDevice {
-    bool ready = false;
-    void* scratch = nullptr;
-};
-NoAllocDevice g_noalloc_dev[64];
-}  // namespace
-
-// Declared in include/tpcf.h.  The first call on a device resolves the device
-// address of the scratch array (cudaGetSymbolAddress) with that device
-// current; make that first call outside any stream capture.
+// Declared in include/tpcf.h.  Every call looks up the device address of the
+// scratch array (cudaGetSymbolAddress) with the caller's device current: a
+// host call, so the address is never stale (a device reset reloads the
+// module).  The first call on a device may load the library's device code:
+// make it outside any stream capture.
 extern "C" int32_t tpcf_pair_count_noalloc(const float* x0, const float* y0, const float* z0, int64_t n0,
                                            const float* x1, const float* y1, const float* z1, int64_t n1,
                                            int32_t loop, float lo, float hi, int32_t nbins, uint64_t* hist_out,
@@ -1898,21 +1892,21 @@ extern "C" int32_t tpcf_pair_count_noalloc(const float* x0, const float* y0, con
     int copies = 8;
     while (copies > 1 && pair_smem_bytes(nbins, copies) > 200 * 1024) copies /= 2;
     if (pair_smem_bytes(nbins, copies) > 227 * 1024) return TPCF_ERR_INVALID;
+    // an error left by the caller's earlier work is reported, not consumed
+    if (cudaPeekAtLastError() != cudaSuccess) return TPCF_ERR_CUDA;
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return TPCF_ERR_NO_DEVICE;
-    NoAllocDevice& D = g_noalloc_dev[dev];
-    if (!D.ready) {
-        if (cudaGetSymbolAddress(&D.scratch, g_noalloc) != cudaSuccess || !D.scratch) {
-            cudaGetLastError();
-            return TPCF_ERR_CUDA;
-        }
-        D.ready = true;
+    if (cudaGetDevice(&dev) != cudaSuccess) return TPCF_ERR_NO_DEVICE;
+    void* scratch = nullptr;
+    if (cudaGetSymbolAddress(&scratch, g_noalloc) != cudaSuccess || !scratch) {
+        (void)cudaGetLastError();
+        return TPCF_ERR_CUDA;
     }
     cudaStream_t st = (cudaStream_t)stream;
-    NoAllocScratch* S = (NoAllocScratch*)D.scratch;
+    NoAllocScratch* S = (NoAllocScratch*)scratch;
     unsigned int* counter = &S->task_counter;
     if (cudaMemsetAsync(hist, 0, sizeof(unsigned long long) * (size_t)nbins, st) != cudaSuccess) return TPCF_ERR_CUDA;
     noalloc_prepare<<<256, 256, 0, st>>>(x0, y0, z0, (int)n0, x1, y1, z1, (int)n1, hist);
+    if (cudaGetLastError() != cudaSuccess) return TPCF_ERR_CUDA;
     const bool same = loop == TPCF_LOOP_SAME && x0 == x1 && y0 == y1 && z0 == z1 && n0 == n1;
     const int pred_same = loop == TPCF_LOOP_SAME && !same;
     const int ntA = (int)((n0 + TILE - 1) / TILE), ntB = (int)((n1 + TILE - 1) / TILE);
@@ -1924,14 +1918,20 @@ extern "C" int32_t tpcf_pair_count_noalloc(const float* x0, const float* y0, con
         volatile float span = hi - lo;
         p.bw = span / (float)nbins;
         size_t smem = pair_smem_bytes(nbins, copies);
-        if (cudaFuncSetAttribute(pair_kernel_noalloc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        // the kernel's dynamic shared memory limit: always the device's opt-in
+        // maximum, never lowered (a lower per-call value would invalidate
+        // launches recorded earlier with a larger size)
+        int smem_max = 0, sms = 0;
+        if (cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || (size_t)smem_max < smem)
+            return TPCF_ERR_CUDA;
+        if (cudaFuncSetAttribute(pair_kernel_noalloc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max) !=
             cudaSuccess)
             return TPCF_ERR_CUDA;
-        int sms = 0;
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         long long tasks = (long long)ntA * ntB;
         int grid = (int)std::min<long long>(tasks, (long long)sms * 4);
         pair_kernel_noalloc<false><<<grid, PR_THREADS, smem, st>>>(counter, ntA, ntB, same ? 1 : 0, pred_same, p, copies);
+        if (cudaGetLastError() != cudaSuccess) return TPCF_ERR_CUDA;
     }
-    return cudaGetLastError() == cudaSuccess ? TPCF_OK : TPCF_ERR_CUDA;
+    return TPCF_OK;
 }

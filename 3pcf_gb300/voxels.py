@@ -198,11 +198,18 @@ def cell_boxes(points_by_cat, starts_by_cat, ends_by_cat, ncell):
 
 
 def box_near(lo, hi, reach):
-    """near(a, b): the boxes of cells a and b are closer than reach (a
-    conservative test: the true distance of two points is at least it)."""
+    """near(a, b): the boxes of cells a and b are closer than reach, with
+    reach the largest side that can be counted (the upper bin edge).  The
+    kernels decide with the reference's float32 side length, which can round
+    below the edge for points whose exact distance is at or slightly above
+    it, so the test uses reach * (1 + 1e-5) + 1e-6: a float32 length is within
+    a few units in the last place (~2.4e-7 relative) of the exact one.  The
+    box gap never exceeds the exact distance of two of their points."""
+    limit = float(reach) * (1.0 + 1e-5) + 1e-6
+
     def near(a, b):
         gap = np.maximum(0.0, np.maximum(lo[a] - hi[b], lo[b] - hi[a]))
-        return bool(np.sqrt((gap ** 2).sum()) < reach)
+        return bool(np.sqrt((gap ** 2).sum()) < limit)
 
     def neighbours(v, occ):
         return [int(c) for c in np.nonzero(occ)[0] if near(v, int(c))]

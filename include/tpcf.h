@@ -108,7 +108,8 @@ typedef struct {
     int32_t kind;       /* TPCF_THREE_SIDE / TPCF_TRIANGLE / TPCF_PAIR */
     int32_t loop;       /* TPCF_LOOP_* */
     int32_t precision;  /* TPCF_GUARDED_FP32 / TPCF_PLAIN_FP64 */
-    int32_t nan_policy; /* TPCF_NAN_* (triangle only) */
+    int32_t nan_policy; /* TPCF_NAN_* (triangle only; pair counts always follow
+                           x86-64: a NaN separation is not counted) */
     int32_t overflow;   /* TPCF_OVERFLOW_* (three-side and JBJ) */
     int32_t prune;      /* 1: skip point tiles that provably cannot contribute
                            (exact); 0: visit every tile of the loop nest */
@@ -256,10 +257,16 @@ tpcf_status tpcf_convert_radecz(tpcf_ctx* ctx, const double* ra, const double* d
  *   - at most 262144 points per catalog (TPCF_ERR_INVALID beyond);
  *   - loop TPCF_LOOP_SAME with identical pointers and sizes counts j >= i of
  *     one catalog; with different arrays it compares loop indices;
- *   - the first call on a device looks up that array's device address, with
- *     the device current; make that first call before any stream capture;
+ *   - each call looks up that array's device address with the caller's device
+ *     current (a host call; valid after a device reset too); the first call on
+ *     a device may load the library's device code, so make it before any
+ *     stream capture;
  *   - calls share the array: calls that overlap on the GPU (other streams or
  *     host threads) race; the call clears the counter and hist it needs;
+ *   - returns TPCF_ERR_CUDA without launching when a CUDA error is already
+ *     pending on the calling thread (left pending for its owner);
+ *   - a NaN separation is not counted (as the x86-64 build of the reference,
+ *     whose int(NaN) is INT_MIN; tpcf_count's pair kernels do the same);
  *   - asynchronous on 'stream' (a cudaStream_t, or NULL for the default stream). */
 tpcf_status tpcf_pair_count_noalloc(const float* x0, const float* y0, const float* z0, int64_t n0,
                                     const float* x1, const float* y1, const float* z1, int64_t n1,

@@ -76,3 +76,74 @@ def test_zeta_error_summary():
     assert abs(e["max_abs"] - 2e-3) < 1e-15
     assert abs(e["rms"] - np.sqrt((1e-6 + 4e-6) / 3)) < 1e-15
     assert abs(e["max_rel"] - 2e-3) < 1e-12
+
+
+# ---- pins: the reference's own scripts run on committed histogram files ----
+# (tests/golden/make_estimator_pins.py executes examples/plot_MICE_2pcf.py and
+# examples/plot_MICE_3pcf.py under Python 3, matplotlib replaced by a recorder)
+
+import os  # noqa: E402
+
+import refformat as rf  # noqa: E402
+
+PINS = np.load(os.path.join(rf.GOLDEN, "estimator_pins.npz"))
+LRG = "Debbie_LRG_CPU_10degx10deg_LRG_binning_SLAC_1k.dat"
+
+
+def _triangle_files(paths):
+    hs, ns = [], []
+    for p in paths:
+        ngal, nb, counts = rf.parse_triangle(rf.read_bytes(p))
+        hs.append(counts)
+        ns.append(tuple(ngal))
+    return hs, ns, nb
+
+
+def _pair_file(path):
+    vals = rf.read_bytes(path).split()
+    ngal = (int(vals[0]), int(vals[1]))
+    lo, hi = float(vals[3]), float(vals[4])
+    return np.array([int(v) for v in vals[6:]], dtype=np.uint64), ngal, int(vals[2]), lo, hi
+
+
+def _same(a, b):
+    """Identical float64 values (NaN never occurs: the scripts set it to 0)."""
+    a, b = np.asarray(a, dtype=np.float64).ravel(), np.asarray(b, dtype=np.float64).ravel()
+    return a.shape == b.shape and np.array_equal(a, b)
+
+
+def test_zeta_pinned_to_the_reference_script():
+    for var in ("tp_s8_q8_t16", "tp_default"):
+        hs, ns, nb = _triangle_files([os.path.join(rf.GOLDEN, "ref", "%s_%s.dat.gz" % (var, h))
+                                      for h in ("DDD", "DDR", "DRR", "RRR")])
+        z = estimators.zeta(*hs, *ns)
+        assert _same(z, PINS["zeta_" + var]), var
+    hs, ns, nb = _triangle_files([os.path.join(rf.GOLDEN, "sandbox", "%s_%s.gz" % (h, LRG))
+                                  for h in ("DDD", "DDR", "DRR", "RRR")])
+    z = estimators.zeta(*hs, *ns)
+    assert _same(z, PINS["zeta_lrg"])
+    assert np.count_nonzero(z) > 1000
+
+
+def test_xi_and_table_pinned_to_the_reference_script():
+    for var in ("2pcf_default", "2pcf_s40_1_21"):
+        files = [_pair_file(os.path.join(rf.GOLDEN, "ref", "%s_%s.dat.gz" % (var, h))) for h in ("DD", "DR", "RR")]
+        (dd, ndd, nbins, lo, hi), (dr, ndr, _, _, _), (rr, nrr, _, _, _) = files
+        x = estimators.xi(dd, dr, rr, ndd, ndr, nrr)
+        assert _same(x, PINS["xi_" + var]), var
+        # the script's table: x + width with the width as the file prints it
+        text = estimators.format_xi_table(estimators.xi_table(x, lo, hi, nbins))
+        assert text == str(PINS["table_" + var]), var
+
+
+def test_reduced_zeta_pinned_to_the_reference_script():
+    """LRG golden files (25 theta bins) with the xi table of 2pcf_default."""
+    hs, ns, nb = _triangle_files([os.path.join(rf.GOLDEN, "sandbox", "%s_%s.gz" % (h, LRG))
+                                  for h in ("DDD", "DDR", "DRR", "RRR")])
+    z = estimators.zeta(*hs, *ns)
+    table = np.array([[float(v) for v in line.split()] for line in str(PINS["table_2pcf_default"]).splitlines()])
+    spec = ((50, 2.0, 12.0), (16, 0.9, 4.1), (25, 0.0, 1.0))
+    q = estimators.reduced_zeta(z, spec, int(PINS["sbin"]), [int(v) for v in PINS["qbins"]], table)
+    want = PINS["reduced_lrg"]
+    assert q.shape == want.shape
+    assert np.allclose(q, want, rtol=1e-12, atol=0, equal_nan=True)

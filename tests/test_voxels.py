@@ -100,6 +100,36 @@ def test_box_near_is_conservative():
         assert v in neighbours(v, occ)
 
 
+def _ref_dist32(a, b):
+    """The reference's float side length: sqrt((dx*dx + dy*dy) + dz*dz) in float32."""
+    d = (a - b).astype(np.float32)
+    s = np.float32(d[0] * d[0]) + np.float32(d[1] * d[1])
+    s = np.float32(s) + np.float32(d[2] * d[2])
+    return np.float32(np.sqrt(np.float32(s)))
+
+
+def test_box_near_keeps_pairs_that_round_below_the_edge():
+    """Pairs of points in two cells whose exact distance is at or just above
+    the edge hi, but whose float32 length (as the kernels compute it) is below
+    hi, must still make the two cells near."""
+    rng = np.random.default_rng(9)
+    hi = np.float32(12.0)
+    found = 0
+    for _ in range(4000):
+        a = rng.uniform(0, 30, size=3).astype(np.float32)
+        u = rng.normal(size=3)
+        u /= np.linalg.norm(u)
+        b = (a.astype(np.float64) + u * float(hi) * (1 + rng.uniform(0, 2e-7))).astype(np.float32)
+        exact = np.linalg.norm(a.astype(np.float64) - b.astype(np.float64))
+        if exact < hi or _ref_dist32(a, b) >= hi:
+            continue
+        found += 1
+        lo_ = np.stack([a, b]).astype(np.float64)
+        neighbours, near = voxels.box_near(lo_, lo_, float(hi))
+        assert near(0, 1) and near(1, 0)
+    assert found > 0
+
+
 def test_jackknife_from_groups_arithmetic():
     """JK_r = full - (groups touching r), on made-up group histograms."""
     groups = [frozenset({0}), frozenset({0, 1}), frozenset({1, 2}), frozenset({2})]

@@ -6,7 +6,8 @@ passes (here: torch tensors); the entry point's own working buffers are a fixed
 per-device array inside the library.
 
 Checked through the C ABI against the allocating entry point (tpcf_count with
-a pair spec) on two calls in a row; integer counts must be identical.  This file
+a pair spec) and against the oracle's pair loop (src/2pcf_C_version.cc:358-387
+restated) on two calls in a row; integer counts must be identical.  This file
 is collected last so that a run stopping at its first failure has already run
 every other test."""
 import ctypes
@@ -14,6 +15,7 @@ import ctypes
 import numpy as np
 import pytest
 
+import oracle
 import synth
 import tpcf
 
@@ -57,9 +59,11 @@ def test_noalloc_matches_allocating_entry_point(axis):
     for xyz0, xyz1, loop, same in ((d, d, tpcf.LOOP_SAME, True), (d, r, tpcf.LOOP_ONE, False),
                                    (r, d, tpcf.LOOP_SAME, False)):
         want = _allocating(xyz0, xyz1, loop, axis, same)
+        ref, _ = oracle.pair([xyz0, xyz1], 1 if loop == tpcf.LOOP_ONE else 0, axis[1], axis[2], axis[0])
         first = _noalloc(xyz0, xyz1, loop, axis, same)
         second = _noalloc(xyz0, xyz1, loop, axis, same)  # the shared array keeps the first call's contents
         assert want.sum() > 0
+        assert np.array_equal(want, ref)
         assert np.array_equal(first, want)
         assert np.array_equal(second, want)
 
