@@ -13,6 +13,13 @@ Mirrors the reference's post-processing scripts:
       norms  DD: (N0^2 - N0)/2,  DR: N0 N1,  RR: (N0^2 - N0)/2
       xi = (DD/n - 2 DR/n + RR/n) / (RR/n); NaN -> 0, +inf -> 0
     and the table file master_2pcf_reference.dat ("%f %f" of x + w and xi), :128-132.
+  * jackknife covariance of zeta (no counterpart in the reference, whose
+    estimator ends at zeta): for N subsamples, subsample r being the catalogs
+    with the points of region r removed and zeta_r its zeta (norms from the
+    subsample's own catalog sizes),
+      mean_b  = (1/N) sum_r zeta_r[b]
+      C[a, b] = (N - 1)/N sum_r (zeta_r[a] - mean_a) (zeta_r[b] - mean_b)
+    and sigma_b = sqrt(C[b, b]), the error bar of zeta[b] of the full sample.
 
 Histograms are the engine's uint64 counts; the reference reads the written files,
 whose triangle and pair counts are unsigned int, so counts are wrapped mod 2^32
@@ -124,3 +131,37 @@ def zeta_error(z, z_ref, rrr):
     rel = d / np.maximum(np.abs(z_ref[m]), 1e-12)
     return {"bins": int(m.sum()), "max_abs": float(d.max()), "rms": float(np.sqrt(np.mean(d * d))),
             "max_rel": float(rel.max())}
+
+
+def norms_counts(nd, nr):
+    """Header counts (N0, N1, N2) of the DDD, DDR, DRR, RRR files for nd data
+    and nr random points."""
+    return (nd, nd, nd), (nd, nd, nr), (nd, nr, nr), (nr, nr, nr)
+
+
+def jackknife_covariance(samples):
+    """(mean, covariance) of N jackknife samples (N x B): the mean over the
+    samples and (N - 1)/N times the sum of the outer products of the
+    deviations from it."""
+    x = np.asarray(samples, dtype=np.float64)
+    n = x.shape[0]
+    mean = x.mean(axis=0)
+    dev = x - mean
+    cov = (n - 1) / n * (dev.T @ dev)
+    return mean, cov
+
+
+def zeta_jackknife(full, subsamples, n_full, n_sub, bins=None):
+    """zeta of the full sample with its jackknife error.
+
+    full: (DDD, DDR, DRR, RRR) histograms of the full catalogs; subsamples:
+    one such tuple per region r, counted on the catalogs without region r;
+    n_full: (nd, nr) catalog sizes; n_sub: one (nd, nr) per region.  bins:
+    the flat bin indices the covariance is kept for (default all; a
+    covariance of B bins holds B^2 doubles).  Returns a dict with zeta (all
+    bins), the jackknife mean, covariance and sigma over the chosen bins."""
+    z = zeta(*full, *norms_counts(*n_full))
+    zs = np.stack([zeta(*h, *norms_counts(*n)) for h, n in zip(subsamples, n_sub)])
+    sel = np.arange(z.size) if bins is None else np.asarray(bins)
+    mean, cov = jackknife_covariance(zs[:, sel])
+    return {"zeta": z, "bins": sel, "mean": mean, "cov": cov, "sigma": np.sqrt(np.diag(cov))}

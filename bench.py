@@ -703,6 +703,22 @@ def run_voxel(args):
         st = eng.stats()
         ms.append(st["kernel_ms"])
     exact = [bool(np.array_equal(hs[o], hs[4 + o])) for o in range(4)]
+    # zeta of the full light cone with its jackknife error bars (16 subsamples)
+    import estimators
+    zj = estimators.zeta_jackknife(tuple(hs[:4]), [tuple(jk[4 * reg:4 * reg + 4]) for reg in range(16)],
+                                   (len(d), len(r)),
+                                   [(int((rd != reg).sum()), int((rr != reg).sum())) for reg in range(16)])
+    pop = np.nonzero(hs[3] > 0)[0]
+    top = pop[np.argsort(hs[3][pop])[::-1][:5]]
+    zeta_jk = {"estimator": "Szapudi-Szalay zeta of the full sample; jackknife covariance (N-1)/N sum_r "
+                            "(zeta_r - mean)(zeta_r - mean)^T over the 16 subsamples",
+               "populated_bins": int(len(pop)),
+               "median_sigma": float(np.median(zj["sigma"][pop])) if len(pop) else 0.0,
+               "median_abs_zeta_over_sigma": float(np.median(np.abs(zj["zeta"][pop]) /
+                                                             np.maximum(zj["sigma"][pop], 1e-300)))
+               if len(pop) else 0.0,
+               "most_populated": [{"bin": int(b), "zeta": float(zj["zeta"][b]), "sigma": float(zj["sigma"][b])}
+                                  for b in top]}
     mean = statistics.mean(ms) / 1e3
     _line("triangles/s (bit-exact histos)", units / mean, "triangles/s", args,
           {"workload": "light cone 100k clustered + 100k uniform, TP s8 q8 t16; one launch of 4 full histograms "
@@ -718,7 +734,7 @@ def run_voxel(args):
            "first_call_s": first_s, "launch_shape": {"hist_copies": st["hist_copies"], "ctas_per_sm": st["ctas_per_sm"]}},
           ms_per_step=mean * 1e3, wall_ms_per_step=statistics.mean(wall), p50_ms=statistics.median(ms),
           p99_ms=float(np.percentile(ms, 99)), gpu_launches=st["kernel_launches"] * args.steps,
-          graph_replays=st["graph_replays"],
+          graph_replays=st["graph_replays"], zeta_jackknife=zeta_jk,
           roofline={"bound": "issue", "achieved": W_TP * st["binned_units"] / (st["main_kernel_ms"] / 1e3) / 1e12,
                     "unit": "Tinst/s", "per_unit": "58 lane-instructions per binned triangle"})
     eng.close()

@@ -85,3 +85,20 @@ def reduced_zeta(z, spec, sbin, qbins, xi_x, xi_y):
             row.append(zz / den if den != 0 else (math.copysign(math.inf, zz) if zz != 0 else math.nan))
         out.append(row)
     return out
+
+
+def jackknife_covariance(samples):
+    """Element-by-element restatement of the jackknife covariance of
+    3pcf_gb300/estimators.py (no reference counterpart):
+    mean_b = (1/N) sum_r x_r[b]; C[a][b] = (N-1)/N sum_r (x_r[a]-mean_a)(x_r[b]-mean_b)."""
+    n = len(samples)
+    nb = len(samples[0])
+    mean = [sum(float(samples[r][b]) for r in range(n)) / n for b in range(nb)]
+    cov = [[0.0] * nb for _ in range(nb)]
+    for a in range(nb):
+        for b in range(nb):
+            acc = 0.0
+            for r in range(n):
+                acc += (float(samples[r][a]) - mean[a]) * (float(samples[r][b]) - mean[b])
+            cov[a][b] = (n - 1) / n * acc
+    return mean, cov

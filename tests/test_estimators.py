@@ -147,3 +147,47 @@ def test_reduced_zeta_pinned_to_the_reference_script():
     want = PINS["reduced_lrg"]
     assert q.shape == want.shape
     assert np.allclose(q, want, rtol=1e-12, atol=0, equal_nan=True)
+
+
+def test_jackknife_covariance_matches_restatement():
+    rng = np.random.default_rng(3)
+    x = rng.normal(size=(16, 12)) * rng.uniform(0.1, 3.0, size=12)
+    mean, cov = estimators.jackknife_covariance(x)
+    wmean, wcov = estimators_ref.jackknife_covariance(x.tolist())
+    assert np.allclose(mean, wmean, rtol=1e-14, atol=1e-15)
+    assert np.allclose(cov, np.array(wcov), rtol=1e-12, atol=1e-14)
+    # (N-1)/N sum of squares = (N-1) times the biased sample covariance
+    assert np.allclose(cov, 15 * np.cov(x, rowvar=False, bias=True), rtol=1e-12, atol=1e-14)
+    assert np.allclose(cov, cov.T)
+    assert np.linalg.eigvalsh(cov).min() > -1e-12
+
+
+def test_zeta_jackknife_of_identical_subsamples_has_no_spread():
+    h, n, spec, d, r = _hists(21)
+    full = (h["DDD"], h["DDR"], h["DRR"], h["RRR"])
+    out = estimators.zeta_jackknife(full, [full] * 4, (140, 150), [(140, 150)] * 4)
+    assert np.array_equal(out["mean"], out["zeta"])
+    assert np.all(out["sigma"] == 0)
+
+
+def test_zeta_jackknife_from_region_subsamples():
+    """Subsamples of the oracle's counts with one of 4 regions removed: the
+    error bars are the restated formula applied to their zetas."""
+    spec = ((8, 2.0, 10.0), (8, 1.0, 3.0), (16, 0.0, 1.0))
+    d = synth.blobs(160, n_blobs=3, sigma=4.0, box=30.0, seed=31)
+    r = synth.uniform(150, box=30.0, seed=32)
+    reg_d, reg_r = (d[:, 0] // 7.5).astype(int).clip(0, 3), (r[:, 0] // 7.5).astype(int).clip(0, 3)
+
+    def four(dd, rr):
+        return tuple(oracle.triangle(c, w, spec)[0] for c, w in (([dd, dd, dd], 0), ([dd, dd, rr], 1),
+                                                                 ([dd, rr, rr], 1), ([rr, rr, rr], 0)))
+    full = four(d, r)
+    subs = [four(d[reg_d != k], r[reg_r != k]) for k in range(4)]
+    ns = [(int((reg_d != k).sum()), int((reg_r != k).sum())) for k in range(4)]
+    bins = np.nonzero(full[3])[0][:20]
+    out = estimators.zeta_jackknife(full, subs, (len(d), len(r)), ns, bins=bins)
+    zs = [estimators_ref.zeta(*h, *estimators.norms_counts(*n)) for h, n in zip(subs, ns)]
+    wmean, wcov = estimators_ref.jackknife_covariance([[z[b] for b in bins] for z in zs])
+    assert np.allclose(out["mean"], wmean, rtol=1e-12, atol=1e-14)
+    assert np.allclose(out["cov"], np.array(wcov), rtol=1e-10, atol=1e-14)
+    assert out["sigma"].max() > 0
