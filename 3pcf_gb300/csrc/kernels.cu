@@ -1904,9 +1904,15 @@ extern "C" int32_t tpcf_pair_count_noalloc(const float* x0, const float* y0, con
     cudaStream_t st = (cudaStream_t)stream;
     NoAllocScratch* S = (NoAllocScratch*)scratch;
     unsigned int* counter = &S->task_counter;
-    if (cudaMemsetAsync(hist, 0, sizeof(unsigned long long) * (size_t)nbins, st) != cudaSuccess) return TPCF_ERR_CUDA;
+    // (an error of this call's own CUDA calls is consumed before returning, so
+    // that it does not stay pending for the caller's next CUDA call)
+    auto own_error = []() {
+        (void)cudaGetLastError();
+        return (int32_t)TPCF_ERR_CUDA;
+    };
+    if (cudaMemsetAsync(hist, 0, sizeof(unsigned long long) * (size_t)nbins, st) != cudaSuccess) return own_error();
     noalloc_prepare<<<256, 256, 0, st>>>(x0, y0, z0, (int)n0, x1, y1, z1, (int)n1, hist);
-    if (cudaGetLastError() != cudaSuccess) return TPCF_ERR_CUDA;
+    if (cudaGetLastError() != cudaSuccess) return TPCF_ERR_CUDA;  // (consumed by the check itself)
     const bool same = loop == TPCF_LOOP_SAME && x0 == x1 && y0 == y1 && z0 == z1 && n0 == n1;
     const int pred_same = loop == TPCF_LOOP_SAME && !same;
     const int ntA = (int)((n0 + TILE - 1) / TILE), ntB = (int)((n1 + TILE - 1) / TILE);
@@ -1921,13 +1927,18 @@ extern "C" int32_t tpcf_pair_count_noalloc(const float* x0, const float* y0, con
         // the kernel's dynamic shared memory limit: always the device's opt-in
         // maximum, never lowered (a lower per-call value would invalidate
         // launches recorded earlier with a larger size)
-        int smem_max = 0, sms = 0;
-        if (cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || (size_t)smem_max < smem)
-            return TPCF_ERR_CUDA;
+        // (dynamic plus the kernel's static shared memory within the opt-in limit)
+        int optin = 0, sms = 0;
+        cudaFuncAttributes fa;
+        if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            cudaFuncGetAttributes(&fa, pair_kernel_noalloc<false>) != cudaSuccess)
+            return own_error();
+        const int smem_max = optin - (int)fa.sharedSizeBytes;
+        if ((size_t)smem_max < smem) return TPCF_ERR_INVALID;
         if (cudaFuncSetAttribute(pair_kernel_noalloc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max) !=
             cudaSuccess)
-            return TPCF_ERR_CUDA;
+            return own_error();
         long long tasks = (long long)ntA * ntB;
         int grid = (int)std::min<long long>(tasks, (long long)sms * 4);
         pair_kernel_noalloc<false><<<grid, PR_THREADS, smem, st>>>(counter, ntA, ntB, same ? 1 : 0, pred_same, p, copies);
