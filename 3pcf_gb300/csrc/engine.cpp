@@ -530,6 +530,33 @@ static bool three_side_thresholds(ThreeParams& p) {
     return true;
 }
 
+// s-bin of a side d as distance_to_bin computes it for d >= s_lo
+// (src/3pcf_C_version_triangle_parametrization.cc:84-113), -1 below s_lo.
+// IEEE single operations, as on the device.
+static int tri_s_bin(float d, float lo, float bw) {
+    if (d < lo) return -1;
+    volatile float x = d - lo;
+    volatile float q = x / bw;
+    if (!(q < 1e9f)) return 1000000000;  // (beyond every bin; keeps the conversion defined)
+    return (int)q;
+}
+
+// Thresholds of the division-free s-bin: s_u[b] = smallest float side >= 0
+// whose bin is >= b (the bin is non-decreasing in d).  Off where the first
+// guess could be more than one bin away (very fine or far-offset binnings).
+static void tri_s_thresholds(TriParams& p) {
+    p.s_fast = 0;
+    if (p.S + 2 > TRI_SUMAX) return;
+    if (std::max(fabs((double)p.s_lo), fabs((double)p.s_hi)) / (double)p.s_bw > 16384.0) return;
+    p.s_inv_bw = 1.0f / p.s_bw;
+    p.s_u[0] = -INFINITY;
+    for (int b = 1; b <= p.S; b++)
+        p.s_u[b] = smallest_d2_with_code(b, [&](float x) { return tri_s_bin(x, p.s_lo, p.s_bw); });
+    p.s_u[p.S + 1] = INFINITY;
+    for (int b = p.S + 2; b < TRI_SUMAX; b++) p.s_u[b] = NAN;
+    p.s_fast = 1;
+}
+
 Binning make_binning(const tpcf_spec& sp) {
     Binning b;
     b.kind = sp.kind;
@@ -563,6 +590,7 @@ Binning make_binning(const tpcf_spec& sp) {
         p.s_lo = sp.axis[0].lo;
         p.s_hi = sp.axis[0].hi;
         p.s_bw = ref_bw(p.s_lo, p.s_hi, p.S);
+        tri_s_thresholds(p);
         p.q_lo = sp.axis[1].lo;
         p.q_hi = sp.axis[1].hi;
         p.q_bw = ref_bw(p.q_lo, p.q_hi, p.Q);
@@ -613,6 +641,7 @@ Binning make_binning(const tpcf_spec& sp) {
         p.s_lo = sp.axis[0].lo;
         p.s_hi = sp.axis[0].hi;
         p.s_bw = ref_bw(p.s_lo, p.s_hi, p.S);
+        tri_s_thresholds(p);
         p.q_lo = sp.axis[1].lo;
         p.q_hi = sp.axis[1].hi;
         p.q_bw = ref_bw(p.q_lo, p.q_hi, p.Q);
@@ -1237,7 +1266,7 @@ size_t shape_smem(const tpcf_spec& sp, const Binning& bin, int copies, int group
 }
 
 // Launch shapes worth trying for a group, the default first.  The guarded
-// triangle kernel is compiled for three CTAs per SM (its register budget);
+// triangle kernel is compiled for four CTAs per SM (its register budget);
 // the others take as many CTAs as shared memory allows, up to 8.
 std::vector<Shape> shape_candidates(tpcf_ctx* ctx, const tpcf_spec& sp, const Binning& bin, bool fp64) {
     int max_smem_sm = 0, max_smem_block = 0;
@@ -1262,14 +1291,18 @@ std::vector<Shape> shape_candidates(tpcf_ctx* ctx, const tpcf_spec& sp, const Bi
     };
     if (sp.kind == TPCF_TRIANGLE || sp.kind == TPCF_TRIANGLE_JBJ) {
         const char* bps = getenv("TPCF_TRI_BLOCKS_PER_SM");
-        const int tri_per_sm = fp64 ? 2 : (bps ? std::max(1, atoi(bps)) : 3);
-        // default: as many copies as keep three CTAs on an SM (the kernel is
-        // latency-bound and needs the warps)
+        const int tri_per_sm = fp64 ? 2 : (bps ? std::max(1, atoi(bps)) : 4);
+        // default: as many copies as keep four CTAs on an SM (the kernel
+        // needs the warps to hide the latency of its shared-memory tables);
+        // the autotuner also tries three CTAs with more copies
         int c = 8;
         while (c > 1 && fit(c, tri_per_sm).per_sm < tri_per_sm) c /= 2;
         add(fit(c, tri_per_sm));
-        if (!fp64)
+        if (!fp64) {
             for (int cc : {4, 2, 1}) add(fit(cc, tri_per_sm));
+            if (!bps)
+                for (int cc : {4, 2, 1}) add(fit(cc, 3));
+        }
         if (out.empty()) throw InvalidArg{"triangle histogram too large for shared memory"};
     } else if (sp.kind == TPCF_THREE_SIDE) {
         // default: the most copies that still leave four 8-warp CTAs per SM,
@@ -1367,7 +1400,8 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
         pj[g].loop_units = loop_units(jsp.kind, jsp.loop, n);
         units += pj[g].loop_units;
         pj[g].swap = 0;
-        if (rdd && jsp.kind == TPCF_TRIANGLE && jsp.precision == TPCF_GUARDED_FP32 && jsp.loop == TPCF_LOOP_ONE) {
+        if (rdd && (jsp.kind == TPCF_TRIANGLE || jsp.kind == TPCF_TRIANGLE_JBJ) &&
+            jsp.precision == TPCF_GUARDED_FP32 && jsp.loop == TPCF_LOOP_ONE) {
             if (pj[g].v[0] == pj[g].v[1] && pj[g].v[1] != pj[g].v[2]) pj[g].swap = 1;
             else if (pj[g].v[1] == pj[g].v[2] && pj[g].v[0] != pj[g].v[1]) pj[g].swap = 2;
         }
@@ -1489,6 +1523,7 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
     L.stats.plan_ms =
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_wall0).count();
     const bool fp64 = sp.precision != TPCF_GUARDED_FP32;
+    const bool fast_jbj = sp.kind == TPCF_TRIANGLE_JBJ && !fp64;  // the fast kernel's JBJ binning
     if (sp.kind == TPCF_TRIANGLE) ensure_acos(ctx);
     const AcosTable acos_t = sp.kind == TPCF_TRIANGLE ? acos_table(ctx) : AcosTable{};
     const unsigned int nt = (unsigned int)ntasks;
@@ -1519,6 +1554,9 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
                 q.count = L.d_counters.p + 1;
                 q.cap = queue_cap;
                 q.evaluated = reinterpret_cast<unsigned long long*>(L.d_counters.p + 2);
+            } else if (fast_jbj) {
+                q.count = L.d_counters.p + 1;  // no item is ever queued (cap 0)
+                q.evaluated = reinterpret_cast<unsigned long long*>(L.d_counters.p + 2);
             }
             auto enqueue = [&](bool capturing) -> cudaError_t {
                 const unsigned int ev_flags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
@@ -1535,9 +1573,15 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
                                             sp.precision == TPCF_GEOMETRY_FP64 ? 1 : 0, st));
                     EQ(cudaEventRecordWithFlags(L.ev_mid, st, ev_flags));
                 } else if (sp.kind == TPCF_TRIANGLE) {
-                    EQ(launch_triangle_fast(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.tri, q, grid, copies, st));
+                    EQ(launch_triangle_fast(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.tri, q, grid, copies, 0,
+                                            st));
                     EQ(cudaEventRecordWithFlags(L.ev_mid, st, ev_flags));
                     EQ(launch_triangle_recheck(L.d_jobs.p, q, bin.tri, acos_t, ctx->num_sms * 8, st));
+                } else if (fast_jbj) {
+                    // JBJ in FP32: the fast kernel, exact without a recheck
+                    EQ(launch_triangle_fast(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.tri, q, grid, copies, 1,
+                                            st));
+                    EQ(cudaEventRecordWithFlags(L.ev_mid, st, ev_flags));
                 } else if (sp.kind == TPCF_TRIANGLE_JBJ) {
                     EQ(launch_triangle_fp64(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.tri, acos_t, grid, copies,
                                             2, st));
@@ -1620,7 +1664,7 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
     // else the default.  A batch that repeats (its plan was cached) and has no
     // tuned shape yet is counted once with every candidate shape -- each count
     // is exact -- and the fastest is kept for the next calls.
-    const std::vector<Shape> cands = shape_candidates(ctx, sp, bin, fp64 || sp.kind == TPCF_TRIANGLE_JBJ);
+    const std::vector<Shape> cands = shape_candidates(ctx, sp, bin, fp64);
     uint64_t key = 1469598103934665603ull;
     for (uint64_t v : sig) key = (key ^ v) * 1099511628211ull;
     const char* tenv = getenv("TPCF_AUTOTUNE");
@@ -1677,8 +1721,9 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
     // the fast triangle kernel skips (i,j) pairs that no counted triangle can
     // contain and counts the triangles it walks; other kernels walk every
     // triangle of their tasks
-    L.stats.evaluated_units = (sp.kind == TPCF_TRIANGLE && !fp64) ? dev_evaluated : evaluated;
-    L.stats.binned_units = (sp.kind == TPCF_TRIANGLE && !fp64) ? dev_binned : evaluated;
+    const bool fast_kernel = (sp.kind == TPCF_TRIANGLE || sp.kind == TPCF_TRIANGLE_JBJ) && !fp64;
+    L.stats.evaluated_units = fast_kernel ? dev_evaluated : evaluated;
+    L.stats.binned_units = fast_kernel ? dev_binned : evaluated;
     L.stats.tasks = ntasks;
     L.stats.kernel_launches = launches * std::max<uint64_t>(1, tuned_runs);
     L.stats.recheck_regrows = regrows;

@@ -298,7 +298,8 @@ __device__ __forceinline__ int tri_side_code(float d, const TriParams& p) {
 }
 
 // Side word of the fast kernel: code * 128 + class weight (see engine.h).
-__device__ __forceinline__ int tri_side_word(float d, const TriParams& p) {
+// U: the s-bin thresholds p.s_u staged in shared memory (used when p.s_fast).
+__device__ __forceinline__ int tri_side_word(float d, const TriParams& p, const float* U) {
     int code, w;
     if (d == 0.f) {
         code = CODE_ZERO;
@@ -310,7 +311,15 @@ __device__ __forceinline__ int tri_side_word(float d, const TriParams& p) {
         code = CODE_ABOVE;
         w = CW_ABOVE;
     } else {
-        int b = __float2int_rz(__fdiv_rn(__fsub_rn(d, p.s_lo), p.s_bw));
+        int b;
+        if (p.s_fast) {
+            // the reference's trunc((d - s_lo)/s_bw) without a division: a
+            // guess within one bin, corrected against the exact thresholds
+            b = min(max(__float2int_rz(__fmul_rn(__fsub_rn(d, p.s_lo), p.s_inv_bw)), 0), p.S);
+            b += (d >= U[b + 1] ? 1 : 0) - (d < U[b] ? 1 : 0);
+        } else {
+            b = __float2int_rz(__fdiv_rn(__fsub_rn(d, p.s_lo), p.s_bw));
+        }
         code = b * (p.Q * p.T);
         w = b < p.S ? CW_IN : CW_ABOVE;  // b == S: rounding at the top edge, index past the array
     }
@@ -359,57 +368,183 @@ __device__ __forceinline__ void theta_fast(float c, const TriParams& p, float& f
 __device__ __forceinline__ unsigned weight_index(int wa, int wb, int wc) { return (unsigned)(wa + wb + wc) & 127u; }
 __device__ __forceinline__ bool mask_bit(unsigned mask, unsigned idx) { return (__funnelshift_rc(mask, 0u, idx) & 1u) != 0; }
 
-// Full fast path of one triangle (sides a, b, c with their words) whose weight
-// index 'idx' says some permutation may count.  w: multiplicity (0 = none).
-// Returns true if the triangle must be recomputed exactly (guard band).
+// Two floats in one 64-bit register for the packed FP32 instructions of
+// sm_100+ (add/sub/mul/fma .rn .f32x2: two IEEE single operations per
+// instruction, each element rounded exactly as the scalar operation).
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 pk2(float a, float b) {
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void up2(f32x2 r, float& a, float& b) { asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r)); }
+__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
+    f32x2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ f32x2 splat2(float a) { return pk2(a, a); }
+
+// magic_floor of two coordinates
+__device__ __forceinline__ void magic_floor2(f32x2 f_m, int& b0, int& b1, float& e0, float& e1) {
+    const f32x2 mg = splat2(MAGIC);
+    const f32x2 tm = add2(f_m, mg);
+    up2(sub2(f_m, sub2(tm, mg)), e0, e1);
+    float t0, t1;
+    up2(tm, t0, t1);
+    b0 = __float_as_int(t0) - MAGIC_BITS;
+    b1 = __float_as_int(t1) - MAGIC_BITS;
+}
+
+// theta_fast of two cosines
+__device__ __forceinline__ void theta_fast2(f32x2 c, const TriParams& p, f32x2& f_m, f32x2& thr) {
+    float c0, c1;
+    up2(c, c0, c1);
+    const f32x2 x = pk2(fabsf(c0), fabsf(c1));
+    const f32x2 t = sub2(splat2(1.0f), x);
+    float t0, t1;
+    up2(t, t0, t1);
+    const f32x2 y = pk2(rsqrt_approx(t0), rsqrt_approx(t1));
+    const f32x2 sq = mul2(t, y);
+    f32x2 P = splat2(p.t_coef[5]);
+    P = fma2(P, x, splat2(p.t_coef[4]));
+    P = fma2(P, x, splat2(p.t_coef[3]));
+    P = fma2(P, x, splat2(p.t_coef[2]));
+    P = fma2(P, x, splat2(p.t_coef[1]));
+    P = fma2(P, x, splat2(p.t_coef[0]));
+    float a0, a1;
+    up2(fma2(sq, P, splat2(-p.t_half)), a0, a1);  // K*acos(|c|) - K*pi/2
+    a0 = __int_as_float(__float_as_int(a0) ^ (__float_as_int(c0) & 0x80000000));  // acos(-x) = pi - acos(x)
+    a1 = __int_as_float(__float_as_int(a1) ^ (__float_as_int(c1) & 0x80000000));
+    f_m = add2(pk2(a0, a1), splat2(p.t_off0));
+    thr = fma2(splat2(-p.t_thrB), y, splat2(p.t_thrA));
+}
+
+// Full fast path of two triangles at once (each lane's two candidates): sides
+// a, b, c with their words; w: multiplicities (0 = none).  The FP32
+// arithmetic of the two runs in packed f32x2 instructions.  A triangle whose
+// weight index says some permutation may count is binned into Hw, unless a
+// permutation that could count has a coordinate inside its guard band: then
+// guard[t] is set and the triangle must be recomputed exactly.
 template <bool THETA_FULL>
-__device__ __forceinline__ bool triangle_full(float a, int wa, float b, int wb, float c, int wc, unsigned idx,
-                                              unsigned w, const TriParams& p, unsigned int* Hw) {
-    const bool v02 = w && mask_bit(VALID_02, idx);
-    const bool v1 = w && mask_bit(VALID_1, idx);
-    float lo_ab = fminf(a, b), hi_ab = fmaxf(a, b);
-    float s = fminf(lo_ab, c);
-    float l = fmaxf(hi_ab, c);
-    float m = fmaxf(lo_ab, fminf(hi_ab, c));
-    int wlo = min(wa, wb), whi = max(wa, wb);
-    int off_s = min(wlo, wc) >> 7;
-    int off_m = max(wlo, min(whi, wc)) >> 7;
-
-    float s2 = __fmul_rn(s, s), m2 = __fmul_rn(m, m), l2 = __fmul_rn(l, l);
-    float rs = rcp_approx(s), rm = rcp_approx(m);
-    float rsq = __fmul_rn(rs, p.q_scale), rmq = __fmul_rn(rm, p.q_scale);
-    GuardedBin q0 = magic_floor(__fmaf_rn(m, rsq, p.q_off));
-    GuardedBin q1 = magic_floor(__fmaf_rn(l, rmq, p.q_off));
-    GuardedBin q2 = magic_floor(__fmaf_rn(l, rsq, p.q_off));
-
-    float num0 = __fsub_rn(__fadd_rn(s2, m2), l2);
-    float num1 = __fsub_rn(__fadd_rn(m2, l2), s2);
-    float c0 = __fmul_rn(__fmul_rn(num0, rcp_approx(__fmul_rn(s, m))), 0.5f);
-    float c1 = __fmul_rn(__fmul_rn(num1, rcp_approx(__fmul_rn(m, l))), 0.5f);
-    float f0m, thr0, f1m, thr1;
-    theta_fast(c0, p, f0m, thr0);
-    theta_fast(c1, p, f1m, thr1);
-    float f2m = __fsub_rn(__fsub_rn(p.t2_off, f0m), f1m);
-    float thr2 = __fadd_rn(__fadd_rn(thr0, thr1), -0.5f - 1e-6f);
-    GuardedBin t0 = magic_floor(f0m), t1 = magic_floor(f1m), t2 = magic_floor(f2m);
-
-    // guard: a permutation that could count has a value near a bin edge
-    bool gq0 = !(fabsf(q0.err) <= p.q_thr), gq1 = !(fabsf(q1.err) <= p.q_thr), gq2 = !(fabsf(q2.err) <= p.q_thr);
-    bool gt0 = !(fabsf(t0.err) <= thr0), gt1 = !(fabsf(t1.err) <= thr1), gt2 = !(fabsf(t2.err) <= thr2);
-    bool guard = (v02 && (gq0 || gt0 || gq2 || gt2)) || (v1 && (gq1 || gt1));
-
-    bool ok0 = v02 && !guard && (unsigned)q0.bin < (unsigned)p.Q;
-    bool ok1 = v1 && !guard && (unsigned)q1.bin < (unsigned)p.Q;
-    bool ok2 = v02 && !guard && (unsigned)q2.bin < (unsigned)p.Q;
-    if (!THETA_FULL) {
-        ok0 = ok0 && (unsigned)t0.bin < (unsigned)p.T;
-        ok1 = ok1 && (unsigned)t1.bin < (unsigned)p.T;
-        ok2 = ok2 && (unsigned)t2.bin < (unsigned)p.T;
+__device__ __forceinline__ void triangle_full2(const float (&a)[2], const int (&wa)[2], const float (&b)[2],
+                                               const int (&wb)[2], const float (&c)[2], const int (&wc)[2],
+                                               const unsigned (&w)[2], const TriParams& p, unsigned int* Hw,
+                                               bool (&guard)[2]) {
+    float s[2], m[2], l[2];
+    int off_s[2], off_m[2];
+    bool v02[2], v1[2];
+#pragma unroll
+    for (int t = 0; t < 2; t++) {
+        const unsigned idx = weight_index(wa[t], wb[t], wc[t]);
+        v02[t] = w[t] && mask_bit(VALID_02, idx);
+        v1[t] = w[t] && mask_bit(VALID_1, idx);
+        const float lo_ab = fminf(a[t], b[t]), hi_ab = fmaxf(a[t], b[t]);
+        s[t] = fminf(lo_ab, c[t]);
+        l[t] = fmaxf(hi_ab, c[t]);
+        m[t] = fmaxf(lo_ab, fminf(hi_ab, c[t]));
+        const int wlo = min(wa[t], wb[t]), whi = max(wa[t], wb[t]);
+        off_s[t] = min(wlo, wc[t]) >> 7;
+        off_m[t] = max(wlo, min(whi, wc[t])) >> 7;
     }
-    if (ok0) atomicAdd(Hw + off_s + q0.bin * p.T + t0.bin, w);
-    if (ok1) atomicAdd(Hw + off_m + q1.bin * p.T + t1.bin, w);
-    if (ok2) atomicAdd(Hw + off_s + q2.bin * p.T + t2.bin, w);
-    return guard;
+    const f32x2 S = pk2(s[0], s[1]), M = pk2(m[0], m[1]), L = pk2(l[0], l[1]);
+    const f32x2 S2 = mul2(S, S), M2 = mul2(M, M), L2 = mul2(L, L);
+    const f32x2 qs = splat2(p.q_scale), qo = splat2(p.q_off);
+    const f32x2 rsq = mul2(pk2(rcp_approx(s[0]), rcp_approx(s[1])), qs);
+    const f32x2 rmq = mul2(pk2(rcp_approx(m[0]), rcp_approx(m[1])), qs);
+    int q0b[2], q1b[2], q2b[2], t0b[2], t1b[2], t2b[2];
+    float q0e[2], q1e[2], q2e[2], t0e[2], t1e[2], t2e[2];
+    magic_floor2(fma2(M, rsq, qo), q0b[0], q0b[1], q0e[0], q0e[1]);
+    magic_floor2(fma2(L, rmq, qo), q1b[0], q1b[1], q1e[0], q1e[1]);
+    magic_floor2(fma2(L, rsq, qo), q2b[0], q2b[1], q2e[0], q2e[1]);
+    const f32x2 num0 = sub2(add2(S2, M2), L2);
+    const f32x2 num1 = sub2(add2(M2, L2), S2);
+    float sm0, sm1, ml0, ml1;
+    up2(mul2(S, M), sm0, sm1);
+    up2(mul2(M, L), ml0, ml1);
+    const f32x2 half = splat2(0.5f);
+    const f32x2 c0 = mul2(mul2(num0, pk2(rcp_approx(sm0), rcp_approx(sm1))), half);
+    const f32x2 c1 = mul2(mul2(num1, pk2(rcp_approx(ml0), rcp_approx(ml1))), half);
+    f32x2 f0m, thr0, f1m, thr1;
+    theta_fast2(c0, p, f0m, thr0);
+    theta_fast2(c1, p, f1m, thr1);
+    const f32x2 f2m = sub2(sub2(splat2(p.t2_off), f0m), f1m);
+    float thr0v[2], thr1v[2], thr2v[2];
+    up2(thr0, thr0v[0], thr0v[1]);
+    up2(thr1, thr1v[0], thr1v[1]);
+    up2(add2(add2(thr0, thr1), splat2(-0.5f - 1e-6f)), thr2v[0], thr2v[1]);
+    magic_floor2(f0m, t0b[0], t0b[1], t0e[0], t0e[1]);
+    magic_floor2(f1m, t1b[0], t1b[1], t1e[0], t1e[1]);
+    magic_floor2(f2m, t2b[0], t2b[1], t2e[0], t2e[1]);
+#pragma unroll
+    for (int t = 0; t < 2; t++) {
+        // guard: a permutation that could count has a value near a bin edge
+        const bool gq0 = !(fabsf(q0e[t]) <= p.q_thr), gq1 = !(fabsf(q1e[t]) <= p.q_thr),
+                   gq2 = !(fabsf(q2e[t]) <= p.q_thr);
+        const bool gt0 = !(fabsf(t0e[t]) <= thr0v[t]), gt1 = !(fabsf(t1e[t]) <= thr1v[t]),
+                   gt2 = !(fabsf(t2e[t]) <= thr2v[t]);
+        const bool g = (v02[t] && (gq0 || gt0 || gq2 || gt2)) || (v1[t] && (gq1 || gt1));
+        bool ok0 = v02[t] && !g && (unsigned)q0b[t] < (unsigned)p.Q;
+        bool ok1 = v1[t] && !g && (unsigned)q1b[t] < (unsigned)p.Q;
+        bool ok2 = v02[t] && !g && (unsigned)q2b[t] < (unsigned)p.Q;
+        if (!THETA_FULL) {
+            ok0 = ok0 && (unsigned)t0b[t] < (unsigned)p.T;
+            ok1 = ok1 && (unsigned)t1b[t] < (unsigned)p.T;
+            ok2 = ok2 && (unsigned)t2b[t] < (unsigned)p.T;
+        }
+        if (ok0) atomicAdd(Hw + off_s[t] + q0b[t] * p.T + t0b[t], w[t]);
+        if (ok1) atomicAdd(Hw + off_m[t] + q1b[t] * p.T + t1b[t], w[t]);
+        if (ok2) atomicAdd(Hw + off_s[t] + q2b[t] * p.T + t2b[t], w[t]);
+        guard[t] = g;
+    }
+}
+
+// JBJ binning of two triangles (src/3pcf_C_version_triangle_parametrization_JBJ.cc
+// distance(), :116-229): one permutation, s = shortest, q = s/m and
+// theta = (l - m)/s in float, binned as distance_to_bin does.  These are the
+// reference's float operations done exactly (IEEE division), so no guard band
+// is needed.  The s-bin comes from the shortest side's word; a triangle whose
+// weight index says its shortest side is out of range, zero or rejected, or
+// whose multiplicity is 0, adds nothing.
+
+// distance_to_bin: -1 outside [lo, hi); the bin as the reference truncates it,
+// which rounding can make n at the top edge (the index then runs into the
+// next row, as the reference's does, or past the array)
+__device__ __forceinline__ int jbj_axis_bin(float v, float lo, float hi, float bw) {
+    if (!(v >= lo) || v >= hi) return -1;  // (v is never NaN here: no zero side reaches this)
+    return __float2int_rz(__fdiv_rn(__fsub_rn(v, lo), bw));
+}
+
+__device__ __forceinline__ void jbj_full2(const float (&a)[2], const int (&wa)[2], const float (&b)[2],
+                                          const int (&wb)[2], const float (&c)[2], const int (&wc)[2],
+                                          const unsigned (&w)[2], const TriParams& p, unsigned int* Hw) {
+#pragma unroll
+    for (int t = 0; t < 2; t++) {
+        const unsigned idx = weight_index(wa[t], wb[t], wc[t]);
+        const bool v = w[t] && mask_bit(VALID_02, idx);
+        const float lo_ab = fminf(a[t], b[t]), hi_ab = fmaxf(a[t], b[t]);
+        const float s = fminf(lo_ab, c[t]), l = fmaxf(hi_ab, c[t]), m = fmaxf(lo_ab, fminf(hi_ab, c[t]));
+        const int code = min(min(wa[t], wb[t]), wc[t]) >> 7;
+        const int i1 = jbj_axis_bin(__fdiv_rn(s, m), p.q_lo, p.q_hi, p.q_bw);
+        const int i2 = jbj_axis_bin(__fdiv_rn(__fsub_rn(l, m), s), p.t_lo, p.t_hi, p.t_bw);
+        const int x = code + i1 * p.T + i2;
+        if (v && i1 >= 0 && i2 >= 0 && x < p.len) atomicAdd(Hw + x, w[t]);
+    }
 }
 
 __device__ __forceinline__ void push_recheck(RecheckQueue& q, uint32_t slot, unsigned w, uint32_t ia, uint32_t ib,
@@ -447,9 +582,9 @@ __device__ __forceinline__ int pkey(float4 p) { return __float_as_int(p.w); }
 // Candidate triangle of the current i: j (6 bits), k (6 bits), weight (2 bits).
 __device__ __forceinline__ uint32_t pack_cand(int j, int k, unsigned w) { return (uint32_t)j | ((uint32_t)k << 6) | (w << 12); }
 
-// Runs the full binning path on n (<= 64) queued candidates, up to two per
-// lane (two independent dependency chains per lane).
-template <bool THETA_FULL>
+// Runs the full binning path on n (<= 64) queued candidates, two per lane
+// (packed into the f32x2 instructions of one binning path).
+template <bool THETA_FULL, bool JBJ>
 __device__ __forceinline__ void run_candidates(const uint32_t* cand, int n, const int2* row_ij, const int2* row_ik,
                                                const int2* JK, const TriParams& p, unsigned int* Hw, RecheckQueue& q,
                                                uint32_t slot, uint32_t ia, int b0, int c0) {
@@ -460,13 +595,18 @@ __device__ __forceinline__ void run_candidates(const uint32_t* cand, int n, cons
     const unsigned w0 = e0 >> 12, w1 = e1 >> 12;
     const int2 ij0 = row_ij[j0], ik0 = row_ik[k0], jk0 = JK[j0 * TILE + k0];
     const int2 ij1 = row_ij[j1], ik1 = row_ik[k1], jk1 = JK[j1 * TILE + k1];
-    const bool g0 = triangle_full<THETA_FULL>(__int_as_float(ij0.x), ij0.y, __int_as_float(ik0.x), ik0.y,
-                                              __int_as_float(jk0.x), jk0.y, weight_index(ij0.y, ik0.y, jk0.y), w0,
-                                              p, Hw);
-    bool g1 = false;
-    if (n > 32)  // warp-uniform
-        g1 = triangle_full<THETA_FULL>(__int_as_float(ij1.x), ij1.y, __int_as_float(ik1.x), ik1.y,
-                                       __int_as_float(jk1.x), jk1.y, weight_index(ij1.y, ik1.y, jk1.y), w1, p, Hw);
+    const float fa[2] = {__int_as_float(ij0.x), __int_as_float(ij1.x)};
+    const float fb[2] = {__int_as_float(ik0.x), __int_as_float(ik1.x)};
+    const float fc[2] = {__int_as_float(jk0.x), __int_as_float(jk1.x)};
+    const int wa[2] = {ij0.y, ij1.y}, wb[2] = {ik0.y, ik1.y}, wc[2] = {jk0.y, jk1.y};
+    const unsigned ww[2] = {w0, w1};
+    if (JBJ) {
+        jbj_full2(fa, wa, fb, wb, fc, wc, ww, p, Hw);
+        return;
+    }
+    bool guard[2];
+    triangle_full2<THETA_FULL>(fa, wa, fb, wb, fc, wc, ww, p, Hw, guard);
+    const bool g0 = guard[0], g1 = guard[1];
     if (g0) push_recheck(q, slot, w0, ia, (uint32_t)(b0 + j0), (uint32_t)(c0 + k0));
     if (g1) push_recheck(q, slot, w1, ia, (uint32_t)(b0 + j1), (uint32_t)(c0 + k1));
 }
@@ -501,11 +641,22 @@ __device__ __forceinline__ unsigned long long candidate_mask(int cij, unsigned l
     return (nI & (mI | mM)) | (nM & mI);  // cij == 1 or 4
 }
 
-template <int PRED, bool THETA_FULL>
+// The same for the JBJ parametrization: a triangle can count only if its
+// shortest side is in the s range, i.e. no side below s_lo and at least one
+// in range.
+__device__ __forceinline__ unsigned long long candidate_mask_jbj(int cij, unsigned long long nI, unsigned long long nM,
+                                                                 unsigned long long nH, unsigned long long mI,
+                                                                 unsigned long long mM, unsigned long long mH) {
+    if (cij == 1) return 0ull;
+    if (cij == 2) return (nI | nM | nH) & (mI | mM | mH);
+    return (nI & (mI | mM | mH)) | ((nM | nH) & mI);
+}
+
+template <int PRED, bool THETA_FULL, bool JBJ>
 __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams& p, float4* P, int2* JK,
                                    int2* IJ, int2* IK, uint32_t* Q, unsigned long long* JM, float* BX,
                                    unsigned int* Hw, RecheckQueue& q, unsigned long long& evaluated,
-                                   unsigned long long& binned, int* next_i) {
+                                   unsigned long long& binned, int* next_i, const float* SU) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const TaskGeom g = task_geom(J, task);
     const uint32_t slot = task.x & TASK_SLOT_MASK;
@@ -575,13 +726,13 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
         int c0 = 0, c1 = 0;
         if (lane < g.nC) {
             float d = ref_dist<false>(pj, P[2 * TILE + lane]);
-            int w = tri_side_word(d, p);
+            int w = tri_side_word(d, p, SU);
             JK[j * TILE + lane] = make_int2(__float_as_int(d), w);
             c0 = side_class(w, d, p);
         }
         if (lane + 32 < g.nC) {
             float d = ref_dist<false>(pj, P[2 * TILE + lane + 32]);
-            int w = tri_side_word(d, p);
+            int w = tri_side_word(d, p, SU);
             JK[j * TILE + lane + 32] = make_int2(__float_as_int(d), w);
             c1 = side_class(w, d, p);
         }
@@ -615,13 +766,13 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
         int c0 = 0, c1 = 0;
         if (lane < g.nC) {
             float d = ref_dist<false>(pi, P[2 * TILE + lane]);
-            int w = tri_side_word(d, p);
+            int w = tri_side_word(d, p, SU);
             row_ik[lane] = make_int2(__float_as_int(d), w);
             c0 = side_class(w, d, p);
         }
         if (lane + 32 < g.nC) {
             float d = ref_dist<false>(pi, P[2 * TILE + lane + 32]);
-            int w = tri_side_word(d, p);
+            int w = tri_side_word(d, p, SU);
             row_ik[lane + 32] = make_int2(__float_as_int(d), w);
             c1 = side_class(w, d, p);
         }
@@ -640,13 +791,14 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
             w2 = 0;
             if (j >= g.nB) return false;
             float d = ref_dist<false>(pi, P[TILE + j]);
-            int w = tri_side_word(d, p);
+            int w = tri_side_word(d, p, SU);
             row_ij[j] = make_int2(__float_as_int(d), w);
             const int c = side_class(w, d, p);
             bool ok = c != 0 && any_k && (!diag_ij || j > i);
             if (PRED == PRED_SAME) ok = ok && ki <= pkey(P[TILE + j]);
             if (!ok) return false;
-            cm = candidate_mask(c, nB, nI, nM, nH, JM[j], JM[TILE + j], JM[2 * TILE + j], JM[3 * TILE + j]);
+            cm = JBJ ? candidate_mask_jbj(c, nI, nM, nH, JM[TILE + j], JM[2 * TILE + j], JM[3 * TILE + j])
+                     : candidate_mask(c, nB, nI, nM, nH, JM[j], JM[TILE + j], JM[2 * TILE + j], JM[3 * TILE + j]);
             if (diag_jk) cm &= j >= 63 ? 0ull : (~0ull << (j + 1));
             if (PRED == PRED_RDD) {
                 // weight [key_j <= key_i] + [key_k <= key_i]
@@ -709,14 +861,14 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
                 __syncwarp();
                 if (qn >= 64) {
                     qn -= 64;
-                    run_candidates<THETA_FULL>(cand + qn, 64, row_ij, row_ik, JK, p, Hw, q, slot, ia, g.b0, g.c0);
+                    run_candidates<THETA_FULL, JBJ>(cand + qn, 64, row_ij, row_ik, JK, p, Hw, q, slot, ia, g.b0, g.c0);
                     bn += 64;
                     __syncwarp();
                 }
             }
         }
         if (qn > 0) {
-            run_candidates<THETA_FULL>(cand, qn, row_ij, row_ik, JK, p, Hw, q, slot, ia, g.b0, g.c0);
+            run_candidates<THETA_FULL, JBJ>(cand, qn, row_ij, row_ik, JK, p, Hw, q, slot, ia, g.b0, g.c0);
             bn += qn;
         }
         __syncwarp();
@@ -725,24 +877,25 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
     binned += bn;
 }
 
-template <bool THETA_FULL>
+template <bool THETA_FULL, bool JBJ>
 __device__ __forceinline__ void triangle_dispatch(const DevJob& J, uint4 task, const TriParams& p, float4* P,
                                                   int2* JK, int2* IJ, int2* IK, uint32_t* Q,
                                                   unsigned long long* JM, float* BX, unsigned int* Hw, RecheckQueue& q,
-                                                  unsigned long long& ev, unsigned long long& bn, int* next_i) {
+                                                  unsigned long long& ev, unsigned long long& bn, int* next_i,
+                                                  const float* SU) {
     switch ((task.x >> TASK_PRED_SHIFT) & TASK_PRED_MASK) {
-        case PRED_NONE: triangle_task_fast<PRED_NONE, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i); break;
-        case PRED_DDR: triangle_task_fast<PRED_DDR, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i); break;
-        case PRED_RDD: triangle_task_fast<PRED_RDD, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i); break;
-        case PRED_SAME: triangle_task_fast<PRED_SAME, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i); break;
-        default: triangle_task_fast<PRED_ONE, THETA_FULL>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i); break;
+        case PRED_NONE: triangle_task_fast<PRED_NONE, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i, SU); break;
+        case PRED_DDR: triangle_task_fast<PRED_DDR, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i, SU); break;
+        case PRED_RDD: triangle_task_fast<PRED_RDD, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i, SU); break;
+        case PRED_SAME: triangle_task_fast<PRED_SAME, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i, SU); break;
+        default: triangle_task_fast<PRED_ONE, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i, SU); break;
     }
 }
 
 #ifndef TRI_MIN_BLOCKS
-#define TRI_MIN_BLOCKS 3
+#define TRI_MIN_BLOCKS 4
 #endif
-template <bool THETA_FULL>
+template <bool THETA_FULL, bool JBJ>
 __global__ void __launch_bounds__(TRI_THREADS, TRI_MIN_BLOCKS)
 triangle_fast_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ tasks, unsigned int ntasks,
                      unsigned int* task_counter, TriParams p, RecheckQueue q, int copies) {
@@ -757,6 +910,8 @@ triangle_fast_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ 
     __shared__ uint4 s_task;
     __shared__ int s_next_i;
     __shared__ float s_box[6 * 6];  // tile bounding boxes: 6 half-tiles x {lo, hi}
+    __shared__ float s_su[TRI_SUMAX];
+    for (int b = threadIdx.x; b < TRI_SUMAX; b += blockDim.x) s_su[b] = p.s_u[b];
     for (int b = threadIdx.x; b < copies * p.len; b += blockDim.x) H[b] = 0;
     unsigned int* Hw = H + ((threadIdx.x >> 5) % copies) * p.len;
     int cur = -1;
@@ -778,7 +933,8 @@ triangle_fast_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ 
         cur = slot;
         if (slot < 0) break;
         since++;
-        triangle_dispatch<THETA_FULL>(jobs[slot], task, p, P, JK, IJ, IK, Q, JM, s_box, Hw, q, ev, bn, &s_next_i);
+        triangle_dispatch<THETA_FULL, JBJ>(jobs[slot], task, p, P, JK, IJ, IK, Q, JM, s_box, Hw, q, ev, bn, &s_next_i,
+                                           s_su);
     }
     if ((threadIdx.x & 31) == 0) {
         if (ev) atomicAdd(q.evaluated, ev);
@@ -1664,7 +1820,8 @@ cudaError_t prepare_kernels(int device) {
     int optin = 0;
     cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
     if (e != cudaSuccess) return e;
-    const void* fns[] = {(const void*)triangle_fast_kernel<true>, (const void*)triangle_fast_kernel<false>,
+    const void* fns[] = {(const void*)triangle_fast_kernel<true, false>, (const void*)triangle_fast_kernel<false, false>,
+                         (const void*)triangle_fast_kernel<false, true>,
                          (const void*)triangle_fp64_kernel<MODE_FP64>, (const void*)triangle_fp64_kernel<MODE_GEOM>,
                          (const void*)triangle_fp64_kernel<MODE_JBJ>, (const void*)three_side_kernel<true, true>,
                          (const void*)three_side_kernel<true, false>, (const void*)three_side_kernel<false, true>,
@@ -1684,12 +1841,17 @@ cudaError_t prepare_kernels(int device) {
 
 cudaError_t launch_triangle_fast(const DevJob* jobs, const uint4* tasks, unsigned int ntasks,
                                  unsigned int* task_counter, const TriParams& p, RecheckQueue q, int grid,
-                                 int copies, cudaStream_t st) {
+                                 int copies, int jbj, cudaStream_t st) {
     size_t smem = triangle_smem_bytes(p.len, copies);
-    if (p.theta_full)
-        triangle_fast_kernel<true><<<grid, TRI_THREADS, smem, st>>>(jobs, tasks, ntasks, task_counter, p, q, copies);
+    if (jbj)
+        triangle_fast_kernel<false, true><<<grid, TRI_THREADS, smem, st>>>(jobs, tasks, ntasks, task_counter, p, q,
+                                                                           copies);
+    else if (p.theta_full)
+        triangle_fast_kernel<true, false><<<grid, TRI_THREADS, smem, st>>>(jobs, tasks, ntasks, task_counter, p, q,
+                                                                           copies);
     else
-        triangle_fast_kernel<false><<<grid, TRI_THREADS, smem, st>>>(jobs, tasks, ntasks, task_counter, p, q, copies);
+        triangle_fast_kernel<false, false><<<grid, TRI_THREADS, smem, st>>>(jobs, tasks, ntasks, task_counter, p, q,
+                                                                            copies);
     return cudaGetLastError();
 }
 

@@ -865,7 +865,11 @@ def run_serving(args):
            "jobs": len(jobs), "triangles_and_pairs": units,
            "alone_equals_mix": {"jobs_checked": len(kept), "identical": alone_equal}},
           p50_ms=float(np.percentile(lat, 50)), p99_ms=float(np.percentile(lat, 99)),
-          mean_batch_ms=float(np.mean(run)), makespan_s=makespan, units_per_s=units / makespan)
+          mean_batch_ms=float(np.mean(run)), makespan_s=makespan, units_per_s=units / makespan,
+          # a job's latency cannot be below the run time of the batch it ran in:
+          # the share of jobs whose own batch ran longer than 100 ms bounds p99
+          batch_ms_p99=float(np.percentile(run, 99)), jobs_in_batches_over_100ms=int(np.sum(np.array(run) > 100.0)),
+          wait_ms_p99=float(np.percentile(np.array(lat) - np.array(run), 99)))
     eng.close()
     return 0 if alone_equal else 1
 
