@@ -530,33 +530,6 @@ static bool three_side_thresholds(ThreeParams& p) {
     return true;
 }
 
-// s-bin of a side d as distance_to_bin computes it for d >= s_lo
-// (src/3pcf_C_version_triangle_parametrization.cc:84-113), -1 below s_lo.
-// IEEE single operations, as on the device.
-static int tri_s_bin(float d, float lo, float bw) {
-    if (d < lo) return -1;
-    volatile float x = d - lo;
-    volatile float q = x / bw;
-    if (!(q < 1e9f)) return 1000000000;  // (beyond every bin; keeps the conversion defined)
-    return (int)q;
-}
-
-// Thresholds of the division-free s-bin: s_u[b] = smallest float side >= 0
-// whose bin is >= b (the bin is non-decreasing in d).  Off where the first
-// guess could be more than one bin away (very fine or far-offset binnings).
-static void tri_s_thresholds(TriParams& p) {
-    p.s_fast = 0;
-    if (p.S + 2 > TRI_SUMAX) return;
-    if (std::max(fabs((double)p.s_lo), fabs((double)p.s_hi)) / (double)p.s_bw > 16384.0) return;
-    p.s_inv_bw = 1.0f / p.s_bw;
-    p.s_u[0] = -INFINITY;
-    for (int b = 1; b <= p.S; b++)
-        p.s_u[b] = smallest_d2_with_code(b, [&](float x) { return tri_s_bin(x, p.s_lo, p.s_bw); });
-    p.s_u[p.S + 1] = INFINITY;
-    for (int b = p.S + 2; b < TRI_SUMAX; b++) p.s_u[b] = NAN;
-    p.s_fast = 1;
-}
-
 Binning make_binning(const tpcf_spec& sp) {
     Binning b;
     b.kind = sp.kind;
@@ -590,7 +563,6 @@ Binning make_binning(const tpcf_spec& sp) {
         p.s_lo = sp.axis[0].lo;
         p.s_hi = sp.axis[0].hi;
         p.s_bw = ref_bw(p.s_lo, p.s_hi, p.S);
-        tri_s_thresholds(p);
         p.q_lo = sp.axis[1].lo;
         p.q_hi = sp.axis[1].hi;
         p.q_bw = ref_bw(p.q_lo, p.q_hi, p.Q);
@@ -641,7 +613,6 @@ Binning make_binning(const tpcf_spec& sp) {
         p.s_lo = sp.axis[0].lo;
         p.s_hi = sp.axis[0].hi;
         p.s_bw = ref_bw(p.s_lo, p.s_hi, p.S);
-        tri_s_thresholds(p);
         p.q_lo = sp.axis[1].lo;
         p.q_hi = sp.axis[1].hi;
         p.q_bw = ref_bw(p.q_lo, p.q_hi, p.Q);

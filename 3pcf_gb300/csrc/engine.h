@@ -65,8 +65,6 @@ struct DevJob {
     int32_t pad;
 };
 
-constexpr int TRI_SUMAX = 130;  // s-bin thresholds of up to 128 s bins
-
 // Launch-wide binning constants for the triangle kernels.
 struct TriParams {
     int S, Q, T, len;            // len = S*Q*T
@@ -88,13 +86,6 @@ struct TriParams {
     float lmax;                  // sides >= lmax cannot belong to a counted triangle
     float mid_hi;                // s_hi * q_hi (rounded up): permutation 0 needs two sides below it,
                                  // permutation 1 needs all three below it
-    // s-bin of a side without a division (when s_fast != 0): the first guess
-    // trunc((d - s_lo) * s_inv_bw) is within one bin of the reference's
-    // trunc((d - s_lo)/s_bw) and is corrected against s_u[b], the smallest
-    // float side with bin >= b (s_u[0] = -inf, s_u[S + 1] = +inf)
-    int s_fast;
-    float s_inv_bw;
-    float s_u[TRI_SUMAX];
 };
 
 constexpr int TS_UMAX = 68;  // squared-length thresholds of up to 64 bins

@@ -298,8 +298,10 @@ __device__ __forceinline__ int tri_side_code(float d, const TriParams& p) {
 }
 
 // Side word of the fast kernel: code * 128 + class weight (see engine.h).
-// U: the s-bin thresholds p.s_u staged in shared memory (used when p.s_fast).
-__device__ __forceinline__ int tri_side_word(float d, const TriParams& p, const float* U) {
+// (A division-free s-bin -- a guess corrected against exact thresholds
+// staged in shared memory -- measured slower: 14.19 vs 13.95 ms on the
+// default workload.)
+__device__ __forceinline__ int tri_side_word(float d, const TriParams& p) {
     int code, w;
     if (d == 0.f) {
         code = CODE_ZERO;
@@ -311,15 +313,7 @@ __device__ __forceinline__ int tri_side_word(float d, const TriParams& p, const 
         code = CODE_ABOVE;
         w = CW_ABOVE;
     } else {
-        int b;
-        if (p.s_fast) {
-            // the reference's trunc((d - s_lo)/s_bw) without a division: a
-            // guess within one bin, corrected against the exact thresholds
-            b = min(max(__float2int_rz(__fmul_rn(__fsub_rn(d, p.s_lo), p.s_inv_bw)), 0), p.S);
-            b += (d >= U[b + 1] ? 1 : 0) - (d < U[b] ? 1 : 0);
-        } else {
-            b = __float2int_rz(__fdiv_rn(__fsub_rn(d, p.s_lo), p.s_bw));
-        }
+        int b = __float2int_rz(__fdiv_rn(__fsub_rn(d, p.s_lo), p.s_bw));
         code = b * (p.Q * p.T);
         w = b < p.S ? CW_IN : CW_ABOVE;  // b == S: rounding at the top edge, index past the array
     }
@@ -656,7 +650,7 @@ template <int PRED, bool THETA_FULL, bool JBJ>
 __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams& p, float4* P, int2* JK,
                                    int2* IJ, int2* IK, uint32_t* Q, unsigned long long* JM, float* BX,
                                    unsigned int* Hw, RecheckQueue& q, unsigned long long& evaluated,
-                                   unsigned long long& binned, int* next_i, const float* SU) {
+                                   unsigned long long& binned, int* next_i) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const TaskGeom g = task_geom(J, task);
     const uint32_t slot = task.x & TASK_SLOT_MASK;
@@ -726,13 +720,13 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
         int c0 = 0, c1 = 0;
         if (lane < g.nC) {
             float d = ref_dist<false>(pj, P[2 * TILE + lane]);
-            int w = tri_side_word(d, p, SU);
+            int w = tri_side_word(d, p);
             JK[j * TILE + lane] = make_int2(__float_as_int(d), w);
             c0 = side_class(w, d, p);
         }
         if (lane + 32 < g.nC) {
             float d = ref_dist<false>(pj, P[2 * TILE + lane + 32]);
-            int w = tri_side_word(d, p, SU);
+            int w = tri_side_word(d, p);
             JK[j * TILE + lane + 32] = make_int2(__float_as_int(d), w);
             c1 = side_class(w, d, p);
         }
@@ -766,13 +760,13 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
         int c0 = 0, c1 = 0;
         if (lane < g.nC) {
             float d = ref_dist<false>(pi, P[2 * TILE + lane]);
-            int w = tri_side_word(d, p, SU);
+            int w = tri_side_word(d, p);
             row_ik[lane] = make_int2(__float_as_int(d), w);
             c0 = side_class(w, d, p);
         }
         if (lane + 32 < g.nC) {
             float d = ref_dist<false>(pi, P[2 * TILE + lane + 32]);
-            int w = tri_side_word(d, p, SU);
+            int w = tri_side_word(d, p);
             row_ik[lane + 32] = make_int2(__float_as_int(d), w);
             c1 = side_class(w, d, p);
         }
@@ -791,7 +785,7 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
             w2 = 0;
             if (j >= g.nB) return false;
             float d = ref_dist<false>(pi, P[TILE + j]);
-            int w = tri_side_word(d, p, SU);
+            int w = tri_side_word(d, p);
             row_ij[j] = make_int2(__float_as_int(d), w);
             const int c = side_class(w, d, p);
             bool ok = c != 0 && any_k && (!diag_ij || j > i);
@@ -881,14 +875,13 @@ template <bool THETA_FULL, bool JBJ>
 __device__ __forceinline__ void triangle_dispatch(const DevJob& J, uint4 task, const TriParams& p, float4* P,
                                                   int2* JK, int2* IJ, int2* IK, uint32_t* Q,
                                                   unsigned long long* JM, float* BX, unsigned int* Hw, RecheckQueue& q,
-                                                  unsigned long long& ev, unsigned long long& bn, int* next_i,
-                                                  const float* SU) {
+                                                  unsigned long long& ev, unsigned long long& bn, int* next_i) {
     switch ((task.x >> TASK_PRED_SHIFT) & TASK_PRED_MASK) {
-        case PRED_NONE: triangle_task_fast<PRED_NONE, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i, SU); break;
-        case PRED_DDR: triangle_task_fast<PRED_DDR, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i, SU); break;
-        case PRED_RDD: triangle_task_fast<PRED_RDD, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i, SU); break;
-        case PRED_SAME: triangle_task_fast<PRED_SAME, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i, SU); break;
-        default: triangle_task_fast<PRED_ONE, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i, SU); break;
+        case PRED_NONE: triangle_task_fast<PRED_NONE, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i); break;
+        case PRED_DDR: triangle_task_fast<PRED_DDR, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i); break;
+        case PRED_RDD: triangle_task_fast<PRED_RDD, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i); break;
+        case PRED_SAME: triangle_task_fast<PRED_SAME, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i); break;
+        default: triangle_task_fast<PRED_ONE, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i); break;
     }
 }
 
@@ -910,8 +903,6 @@ triangle_fast_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ 
     __shared__ uint4 s_task;
     __shared__ int s_next_i;
     __shared__ float s_box[6 * 6];  // tile bounding boxes: 6 half-tiles x {lo, hi}
-    __shared__ float s_su[TRI_SUMAX];
-    for (int b = threadIdx.x; b < TRI_SUMAX; b += blockDim.x) s_su[b] = p.s_u[b];
     for (int b = threadIdx.x; b < copies * p.len; b += blockDim.x) H[b] = 0;
     unsigned int* Hw = H + ((threadIdx.x >> 5) % copies) * p.len;
     int cur = -1;
@@ -933,8 +924,7 @@ triangle_fast_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ 
         cur = slot;
         if (slot < 0) break;
         since++;
-        triangle_dispatch<THETA_FULL, JBJ>(jobs[slot], task, p, P, JK, IJ, IK, Q, JM, s_box, Hw, q, ev, bn, &s_next_i,
-                                           s_su);
+        triangle_dispatch<THETA_FULL, JBJ>(jobs[slot], task, p, P, JK, IJ, IK, Q, JM, s_box, Hw, q, ev, bn, &s_next_i);
     }
     if ((threadIdx.x & 31) == 0) {
         if (ev) atomicAdd(q.evaluated, ev);

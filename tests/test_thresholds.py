@@ -114,54 +114,3 @@ def test_truncated_guess_misses_the_step_at_hi():
     assert g - 1 + int(f32(1024.0) >= u[g]) + int(f32(1024.0) >= u[g + 1]) == 32
     assert lookup(f32(1024.0), u, lo, f32(1.0) / bw, 0, n + 1, -2.0 ** -20) == 33
 
-
-def tri_s_bin(d, lo, bw):
-    """distance_to_bin of the triangle program for a side d >= lo
-    (src/3pcf_C_version_triangle_parametrization.cc:84-113), -1 below lo."""
-    d = f32(d)
-    if d < lo:
-        return -1
-    q = f32(f32(d - lo) / bw)
-    return int(q) if q < 1e9 else 10 ** 9
-
-
-def tri_s_lookup(d, u, lo, inv_bw, S):
-    """The triangle kernel's division-free s-bin for lo <= d < hi: a truncated
-    guess from d * inv_bw, clamped to [0, S], corrected by one step either way
-    against the thresholds u[b] (smallest side with bin >= b)."""
-    g = int(f32(f32(d - lo) * inv_bw))
-    g = min(max(g, 0), S)
-    return g + int(d >= u[g + 1]) - int(d < u[g])
-
-
-import pytest  # noqa: E402
-
-
-@pytest.mark.parametrize("axis", [(8, 2.0, 10.0), (50, 2.0, 12.0), (6, 0.0, 15.0), (60, 0.0, 120.0), (10, 1.0, 11.0),
-                                  (128, 0.5, 3.0)])
-def test_triangle_s_bin_thresholds(axis):
-    """Every side length around every bin edge (a few ulps either way) and a
-    random sample: the guess-and-correct s-bin equals the reference's."""
-    S, lo, hi = axis[0], f32(axis[1]), f32(axis[2])
-    bw = f32(f32(hi - lo) / f32(S))
-    inv_bw = f32(1.0) / bw
-    u = [f32(-np.inf)] + [smallest_d2(lambda x: tri_s_bin(x, lo, bw), b) for b in range(1, S + 1)] + [f32(np.inf)]
-    u = np.array(u, dtype=np.float32)
-    cases = []
-    for b in range(S + 1):
-        e = f32(lo + f32(b) * bw)
-        x = e
-        for _ in range(6):
-            x = np.nextafter(x, f32(-np.inf))
-        for _ in range(13):
-            cases.append(x)
-            x = np.nextafter(x, f32(np.inf))
-    cases += list(np.random.default_rng(S).uniform(float(lo), float(hi), 4000).astype(np.float32))
-    n = 0
-    for d in cases:
-        d = f32(d)
-        if d < lo or d >= hi or d <= 0:
-            continue
-        assert tri_s_lookup(d, u, lo, inv_bw, S) == tri_s_bin(d, lo, bw), (axis, float(d))
-        n += 1
-    assert n > 1000
