@@ -398,6 +398,17 @@ def impl_ours(args):
     e2e_s = max_over_ranks(dist, statistics.mean(e2e_ms) / 1e3)
     e2e_value = sum_over_ranks(dist, units) / e2e_s
 
+    # the same step's jobs counted one at a time (device time of the counting
+    # kernel per histogram; the batched step runs them in one launch)
+    per_job = {}
+    for name, sp, jb in zip(("DDD", "DDR", "DRR", "RRR"), sp32, jobs):
+        t = []
+        for _ in range(3):
+            eng.count(sp, jb)
+            t.append(eng.stats()["main_kernel_ms"])
+        per_job[name] = {"ms": statistics.median(t), "binned": eng.stats()["binned_units"],
+                         "loop_triangles": eng.stats()["loop_units"]}
+
     # plain FP64 kernel on the same jobs (one step; the >=3x comparison)
     fp64 = None
     if not args.no_fp64:
@@ -465,6 +476,7 @@ def impl_ours(args):
                 "d2h_bytes_per_step": d2h,
                 "breakdown_ms": {k: statistics.median(p[i] for p in e2e_parts) for i, k in
                                  enumerate(("catalogs", "views_and_planning", "kernels", "count_call"))}},
+        "per_job": per_job,
         "plain_fp64": fp64,
         "zeta": zeta,
         "roofline": {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "Tinst/s",
@@ -524,6 +536,56 @@ def run_pairs(args):
                                    "8 lane-instructions per evaluated pair (pairs of tiles within reach)"),
           plain_fp64={"ms_per_step": fp64_ms, "identical": all(np.array_equal(a, b) for a, b in zip(h32, h64))})
     eng.close()
+    return 0
+
+
+JBJ_AXES = [(8, 2.0, 10.0), (8, 0.2, 1.0), (10, 0.0, 1.0)]
+
+
+def run_jbj(args):
+    """JBJ shape parametrization (s, s/m, (l - m)/s) DDD+DDR+DRR+RRR on the
+    default catalogs (10k clustered + 10k uniform): s 8 bins on [2,10), s/m 8
+    on [0.2,1), (l - m)/s 10 on [0,1), the reference's two extra bin-0 counts
+    per visited triangle (compat).  The FP32 fast kernel (exact: the
+    reference's float operations, no guard band) against the per-triangle
+    kernel that visits every triangle of its tasks."""
+    import tpcf
+    d, r = workload(0)
+    eng = tpcf.Engine(0)
+    hd, hr = eng.catalog(d), eng.catalog(r)
+    loops = [tpcf.LOOP_SAME, tpcf.LOOP_ONE, tpcf.LOOP_ONE, tpcf.LOOP_SAME]
+    jobs = [eng.job([hd, hd, hd]), eng.job([hd, hd, hr]), eng.job([hd, hr, hr]), eng.job([hr, hr, hr])]
+    sp = [tpcf.make_spec(tpcf.TRIANGLE_JBJ, lp, JBJ_AXES) for lp in loops]
+    flush = L2Flush(0)
+    for _ in range(args.warmup):
+        eng.count_batch(sp, jobs)
+    ms, ref = [], None
+    for _ in range(args.steps):
+        flush()
+        h = eng.count_batch(sp, jobs)
+        st = eng.stats()
+        ms.append(st["kernel_ms"])
+        if ref is None:
+            ref = h
+        elif any(not np.array_equal(a, b) for a, b in zip(h, ref)):
+            raise RuntimeError("histograms differ between steps")
+    units = st["loop_units"]
+    mean = statistics.mean(ms) / 1e3
+    exact = None
+    if not args.no_fp64:
+        h64 = eng.count_batch([tpcf.make_spec(tpcf.TRIANGLE_JBJ, lp, JBJ_AXES, precision=tpcf.PLAIN_FP64)
+                               for lp in loops], jobs)
+        st64 = eng.stats()
+        exact = {"ms_per_step": st64["kernel_ms"], "identical": all(np.array_equal(a, b) for a, b in zip(h64, ref)),
+                 "fast_over_exhaustive": st64["kernel_ms"] / (mean * 1e3)}
+    _line("triangles/s (bit-exact histos)", units / mean, "triangles/s", args,
+          {"workload": "JBJ (s, s/m, (l-m)/s) DDD+DDR+DRR+RRR, 10k clustered + 10k uniform, s8[2,10) q8[0.2,1) "
+                       "t10[0,1), compat bin-0 counts", "triangles_per_step": units,
+           "evaluated_triangles_per_step": st["evaluated_units"], "binned_triangles_per_step": st["binned_units"]},
+          ms_per_step=mean * 1e3, p50_ms=statistics.median(ms), exhaustive_kernel=exact)
+    eng.close()
+    if exact is not None and not exact["identical"]:
+        return 1
     return 0
 
 
@@ -883,7 +945,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--config", default="tp10k", choices=["tp10k", "three1k", "voxel100k", "lattice500k", "serving",
-                                                              "pairs50k"])
+                                                              "pairs50k", "jbj10k"])
     ap.add_argument("--jobs", type=int, default=2000, help="serving: number of jobs")
     ap.add_argument("--rate", type=float, default=25.0, help="serving: Poisson arrival rate (jobs/s)")
     ap.add_argument("--fp64-slab", action="store_true", help="lattice500k: FP64 comparison on the slab x < 100 only")
@@ -896,7 +958,7 @@ def main():
         return impl_reference(args)
     if args.config != "tp10k":
         return {"three1k": run_three_side, "voxel100k": run_voxel, "lattice500k": run_lattice,
-                "serving": run_serving, "pairs50k": run_pairs}[args.config](args)
+                "serving": run_serving, "pairs50k": run_pairs, "jbj10k": run_jbj}[args.config](args)
     return impl_ours(args)
 
 
