@@ -579,6 +579,11 @@ Binning make_binning(const tpcf_spec& sp) {
         // theta coordinate: acos(c)/(pi' t_bw) - t_lo/t_bw with pi' = 3.14159
         const double pi_ref = 3.14159, pi = 3.14159265358979323846;
         double K = 1.0 / (pi_ref * (double)p.t_bw);
+        // acos(x) ~ sqrt(1 - x) * P(x) on [0, 1], P of degree 5: a minimax (Remez)
+        // fit in absolute error, which equioscillates at 7 points with
+        // |sqrt(1 - x) P(x) - acos(x)| <= 6.37e-7 rad (largest at x = 0; pinned
+        // by tests/test_thresholds.py on a grid of 2e6 points).  The guard band
+        // below budgets 6.4e-7 rad for it.
         static const double coef[6] = {1.5707956894727488, -0.2145428141209928, 0.08817102789580339,
                                        -0.0459271445289548, 0.020619951348088413, -0.004911124693855812};
         for (int i = 0; i < 6; i++) p.t_coef[i] = (float)(coef[i] * K);
@@ -713,6 +718,9 @@ struct Lane {
     cudaGraphExec_t graph = nullptr;
     std::vector<uint64_t> graph_sig;
     bool graphs_ok = true;
+    // SMs a launch of this lane may fill with its persistent CTAs (0: all);
+    // the serving lane that runs heavy jobs leaves some to the light lanes
+    int sm_cap = 0;
     tpcf_stats stats{};
     void drop_graph() {
         if (graph) cudaGraphExecDestroy(graph);
@@ -796,6 +804,8 @@ struct tpcf_ctx {
     bool stop = false;
     int64_t admit_bytes = (int64_t)8 << 30;
     double heavy_cost = 1e12;  // job_cost above which a job runs alone on the first serving lane
+    double light_batch_cost = 2.5e11;  // summed job_cost at which a batch of light jobs closes
+    int reserve_sms = 0;       // SMs a heavy serving batch leaves free for light jobs
     int64_t inflight_bytes = 0;  // device bytes of batches running on serving lanes
     // autotuner: launch shape per batch signature
     std::mutex tune_mu;
@@ -1313,8 +1323,9 @@ std::vector<Shape> shape_candidates(tpcf_ctx* ctx, const tpcf_spec& sp, const Bi
     return out;
 }
 
-int grid_for(tpcf_ctx* ctx, const Shape& sh, uint64_t ntasks) {
-    uint64_t g = (uint64_t)ctx->num_sms * sh.per_sm;
+int grid_for(tpcf_ctx* ctx, const Shape& sh, uint64_t ntasks, int sm_cap) {
+    const int sms = sm_cap > 0 ? std::min(sm_cap, ctx->num_sms) : ctx->num_sms;
+    uint64_t g = (uint64_t)sms * sh.per_sm;
     if (g > ntasks) g = std::max<uint64_t>(ntasks, 1);
     return (int)g;
 }
@@ -1515,7 +1526,7 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
     // the batch repeats).  Returns the device time in ms.
     auto count_with = [&](const Shape& sh, bool allow_graph) -> float {
         const int copies = sh.copies;
-        const int grid = grid_for(ctx, sh, nt);
+        const int grid = grid_for(ctx, sh, nt, L.sm_cap);
         for (int attempt = 0; attempt < 3; attempt++) {
             RecheckQueue q{};
             if (sp.kind == TPCF_TRIANGLE && !fp64) {
@@ -1817,8 +1828,11 @@ void worker_loop(tpcf_ctx* ctx, int lane) {
                     ctx->qcv.wait(lk);
                     continue;
                 }
-                // a heavy job runs alone; light jobs of the same binning share a launch
+                // a heavy job runs alone; light jobs of the same binning share a
+                // launch, up to a summed work estimate, so that a light batch
+                // stays short and the jobs behind it start soon
                 const bool first_heavy = heavy(*first);
+                double batch_cost = 0;
                 for (auto it = ctx->queue.begin(); it != ctx->queue.end();) {
                     auto& p = *it;
                     if (!same_binning(p->spec, first->spec) || p->spec.prune != first->spec.prune ||
@@ -1826,13 +1840,18 @@ void worker_loop(tpcf_ctx* ctx, int lane) {
                         ++it;
                         continue;
                     }
+                    const double c = job_cost(ctx, p->spec, p->job);
+                    if (!batch.empty() && batch_cost + c > ctx->light_batch_cost) break;
                     int64_t jb = job_bytes(ctx, p->spec, p->job);
                     if (!batch.empty() && used + jb > room) break;
                     used += jb;
+                    batch_cost += c;
                     batch.push_back(p);
                     it = ctx->queue.erase(it);
                     if (batch.size() >= 4096) break;
                 }
+                // a heavy batch leaves SMs to the light lanes (its CTAs are persistent)
+                L.sm_cap = first_heavy && ctx->reserve_sms > 0 ? ctx->num_sms - ctx->reserve_sms : 0;
                 ctx->inflight_bytes += used;
                 break;
             }
@@ -1909,8 +1928,15 @@ tpcf_status tpcf_create(tpcf_ctx** out, int32_t device) {
         if (adm) ctx->admit_bytes = atoll(adm);
         const char* hc = getenv("TPCF_HEAVY_COST");
         if (hc) ctx->heavy_cost = atof(hc);
+        const char* lbc = getenv("TPCF_LIGHT_BATCH_COST");
+        if (lbc) ctx->light_batch_cost = atof(lbc);
+        // SMs a heavy serving batch leaves to the light lanes: none by default
+        // (a quarter measured a higher p99 on the serving workload: the
+        // heavy jobs themselves, slower, are the tail)
+        const char* rs = getenv("TPCF_SERVING_RESERVE_SMS");
+        if (rs) ctx->reserve_sms = std::max(0, std::min(ctx->num_sms - 1, atoi(rs)));
         const char* nw = getenv("TPCF_SERVING_LANES");
-        int workers = nw ? std::max(1, std::min(8, atoi(nw))) : 2;
+        int workers = nw ? std::max(1, std::min(8, atoi(nw))) : 3;
         for (int i = 0; i <= workers; i++) {
             auto L = std::make_unique<Lane>();
             CK(cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking));

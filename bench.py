@@ -877,9 +877,11 @@ def run_serving(args):
         pool[fam].append((eng.catalog(dd), eng.catalog(rr), n))
     tp = lambda loop: tpcf.make_spec(tpcf.TRIANGLE, loop, SPEC_AXES, nan_policy=nan)
     pr = lambda loop: tpcf.make_spec(tpcf.PAIR, loop, [(700, 0.0, 70.0)])
-    jobs = []
+    jobs, sizes_of, kinds, cube_jobs = [], [], [], set()
     for k in range(args.jobs):
         fam = "cube" if rng.random() < 0.5 else "cone"
+        if fam == "cube":
+            cube_jobs.add(k)
         a = pool[fam][int(rng.integers(len(pool[fam])))]
         b = pool[fam][int(rng.integers(len(pool[fam])))]
         hd, hr = a[0], b[1]
@@ -888,10 +890,14 @@ def run_serving(args):
             hs, loop = [([hd, hd, hd], tpcf.LOOP_SAME), ([hd, hd, hr], tpcf.LOOP_ONE),
                         ([hd, hr, hr], tpcf.LOOP_ONE), ([hr, hr, hr], tpcf.LOOP_SAME)][kind]
             jobs.append((tp(loop), eng.job(hs)))
+            sizes_of.append((a[2], b[2]))
+            kinds.append(["DDD", "DDR", "DRR", "RRR"][kind])
         else:
             kind = int(rng.integers(3))
             hs, loop = [([hd, hd], tpcf.LOOP_SAME), ([hd, hr], tpcf.LOOP_ONE), ([hr, hr], tpcf.LOOP_SAME)][kind]
             jobs.append((pr(loop), eng.job(hs)))
+            sizes_of.append((a[2], b[2]))
+            kinds.append(["DD", "DR", "RR"][kind])
     units = sum(eng.loop_units(s, j) for s, j in jobs)
     arrivals = np.cumsum(rng.exponential(1.0 / args.rate, size=len(jobs)))
     for s, j in jobs[:20]:  # warm the kernels and the acos table
@@ -909,6 +915,7 @@ def run_serving(args):
     th = threading.Thread(target=submitter)
     th.start()
     lat, run, kept = [], [], {}
+    job_points = [[int(v) for v in sizes_of[i]] for i in range(len(jobs))]  # (data, random) catalog sizes
     for i, (s, j) in enumerate(jobs):
         while tickets[i] is None:
             time.sleep(0.0005)
@@ -931,7 +938,10 @@ def run_serving(args):
           # a job's latency cannot be below the run time of the batch it ran in:
           # the share of jobs whose own batch ran longer than 100 ms bounds p99
           batch_ms_p99=float(np.percentile(run, 99)), jobs_in_batches_over_100ms=int(np.sum(np.array(run) > 100.0)),
-          wait_ms_p99=float(np.percentile(np.array(lat) - np.array(run), 99)))
+          wait_ms_p99=float(np.percentile(np.array(lat) - np.array(run), 99)),
+          slowest_jobs=[{"latency_ms": lat[i], "batch_ms": run[i], "kind": kinds[i], "catalog_points": job_points[i],
+                         "family": "cube" if i in cube_jobs else "cone"}
+                        for i in np.argsort(lat)[::-1][:int(0.01 * len(lat)) + 1]])
     eng.close()
     return 0 if alone_equal else 1
 
