@@ -721,6 +721,8 @@ struct Lane {
     // SMs a launch of this lane may fill with its persistent CTAs (0: all);
     // the serving lane that runs heavy jobs leaves some to the light lanes
     int sm_cap = 0;
+    // count in slices of the task list (heavy serving batches)
+    bool slice_batches = false;
     tpcf_stats stats{};
     void drop_graph() {
         if (graph) cudaGraphExecDestroy(graph);
@@ -806,6 +808,8 @@ struct tpcf_ctx {
     double heavy_cost = 1e12;  // job_cost above which a job runs alone on the first serving lane
     double light_batch_cost = 2.5e11;  // summed job_cost at which a batch of light jobs closes
     int reserve_sms = 0;       // SMs a heavy serving batch leaves free for light jobs
+    bool slice_heavy = true;   // heavy serving batches count in slices (light lanes run between them)
+    int slice_tasks = 0;       // tasks per slice (0: at least 8 per CTA and at most 64 slices)
     int64_t inflight_bytes = 0;  // device bytes of batches running on serving lanes
     // autotuner: launch shape per batch signature
     std::mutex tune_mu;
@@ -1509,7 +1513,7 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
     if (sp.kind == TPCF_TRIANGLE) ensure_acos(ctx);
     const AcosTable acos_t = sp.kind == TPCF_TRIANGLE ? acos_table(ctx) : AcosTable{};
     const unsigned int nt = (unsigned int)ntasks;
-    const uint64_t launches = (sp.kind == TPCF_TRIANGLE && !fp64) ? 2 : 1;
+    uint64_t launches = (sp.kind == TPCF_TRIANGLE && !fp64) ? 2 : 1;  // counting (+ recheck)
     const char* genv = getenv("TPCF_GRAPHS");
     const bool graphs = L.graphs_ok && !(genv && genv[0] == '0');
     L.h_hist.reserve(hist_total);
@@ -1527,6 +1531,11 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
     auto count_with = [&](const Shape& sh, bool allow_graph) -> float {
         const int copies = sh.copies;
         const int grid = grid_for(ctx, sh, nt, L.sm_cap);
+        // slices of at least 8 tasks per CTA, at most 64 of them
+        unsigned int slice =
+            L.slice_batches ? std::max<unsigned int>((unsigned int)grid * 8u, (nt + 63u) / 64u) : std::max(nt, 1u);
+        if (L.slice_batches && ctx->slice_tasks > 0) slice = (unsigned int)ctx->slice_tasks;
+        launches = (nt > slice ? (nt + slice - 1) / slice : 1) + ((sp.kind == TPCF_TRIANGLE && !fp64) ? 1 : 0);
         for (int attempt = 0; attempt < 3; attempt++) {
             RecheckQueue q{};
             if (sp.kind == TPCF_TRIANGLE && !fp64) {
@@ -1550,32 +1559,34 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
                 EQ(cudaMemsetAsync(L.d_hist.p, 0, hist_total * sizeof(unsigned long long), st));
                 EQ(cudaMemsetAsync(L.d_counters.p, 0, 8 * sizeof(unsigned int), st));
                 EQ(cudaEventRecordWithFlags(L.ev0, st, ev_flags));
-                if (sp.kind == TPCF_TRIANGLE && fp64) {
-                    EQ(launch_triangle_fp64(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.tri, acos_t, grid, copies,
-                                            sp.precision == TPCF_GEOMETRY_FP64 ? 1 : 0, st));
-                    EQ(cudaEventRecordWithFlags(L.ev_mid, st, ev_flags));
-                } else if (sp.kind == TPCF_TRIANGLE) {
-                    EQ(launch_triangle_fast(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.tri, q, grid, copies, 0,
-                                            st));
-                    EQ(cudaEventRecordWithFlags(L.ev_mid, st, ev_flags));
-                    EQ(launch_triangle_recheck(L.d_jobs.p, q, bin.tri, acos_t, ctx->num_sms * 8, st));
-                } else if (fast_jbj) {
-                    // JBJ in FP32: the fast kernel, exact without a recheck
-                    EQ(launch_triangle_fast(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.tri, q, grid, copies, 1,
-                                            st));
-                    EQ(cudaEventRecordWithFlags(L.ev_mid, st, ev_flags));
-                } else if (sp.kind == TPCF_TRIANGLE_JBJ) {
-                    EQ(launch_triangle_fp64(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.tri, acos_t, grid, copies,
-                                            2, st));
-                    EQ(cudaEventRecordWithFlags(L.ev_mid, st, ev_flags));
-                } else if (sp.kind == TPCF_THREE_SIDE) {
-                    EQ(launch_three_side(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.three, fp64, grid, copies,
-                                         sh.groups, st));
-                    EQ(cudaEventRecordWithFlags(L.ev_mid, st, ev_flags));
-                } else {
-                    EQ(launch_pairs(L.d_jobs.p, L.d_tasks.p, nt, L.d_counters.p, bin.pair, fp64, grid, copies, st));
-                    EQ(cudaEventRecordWithFlags(L.ev_mid, st, ev_flags));
+                // the counting kernel over tasks [t0, t0 + n)
+                auto launch_main = [&](const uint4* tk, unsigned int n) -> cudaError_t {
+                    if (sp.kind == TPCF_TRIANGLE && fp64)
+                        return launch_triangle_fp64(L.d_jobs.p, tk, n, L.d_counters.p, bin.tri, acos_t, grid, copies,
+                                                    sp.precision == TPCF_GEOMETRY_FP64 ? 1 : 0, st);
+                    if (sp.kind == TPCF_TRIANGLE)
+                        return launch_triangle_fast(L.d_jobs.p, tk, n, L.d_counters.p, bin.tri, q, grid, copies, 0, st);
+                    if (fast_jbj)  // JBJ in FP32: the fast kernel, exact without a recheck
+                        return launch_triangle_fast(L.d_jobs.p, tk, n, L.d_counters.p, bin.tri, q, grid, copies, 1, st);
+                    if (sp.kind == TPCF_TRIANGLE_JBJ)
+                        return launch_triangle_fp64(L.d_jobs.p, tk, n, L.d_counters.p, bin.tri, acos_t, grid, copies, 2,
+                                                    st);
+                    if (sp.kind == TPCF_THREE_SIDE)
+                        return launch_three_side(L.d_jobs.p, tk, n, L.d_counters.p, bin.three, fp64, grid, copies,
+                                                 sh.groups, st);
+                    return launch_pairs(L.d_jobs.p, tk, n, L.d_counters.p, bin.pair, fp64, grid, copies, st);
+                };
+                // one launch over all tasks, or (a heavy serving batch) slices of
+                // them, between which the device can start the kernels that
+                // higher-priority streams (the light serving lanes) have queued
+                EQ(launch_main(L.d_tasks.p, std::min(nt, slice)));
+                for (unsigned int t0 = slice; t0 < nt; t0 += slice) {
+                    EQ(cudaMemsetAsync(L.d_counters.p, 0, sizeof(unsigned int), st));  // the slice's task counter
+                    EQ(launch_main(L.d_tasks.p + t0, std::min(slice, nt - t0)));
                 }
+                EQ(cudaEventRecordWithFlags(L.ev_mid, st, ev_flags));
+                if (sp.kind == TPCF_TRIANGLE && !fp64)
+                    EQ(launch_triangle_recheck(L.d_jobs.p, q, bin.tri, acos_t, ctx->num_sms * 8, st));
                 EQ(cudaEventRecordWithFlags(L.ev1, st, ev_flags));
                 EQ(cudaMemcpyAsync(L.h_counters.p, L.d_counters.p, 8 * sizeof(unsigned int), cudaMemcpyDeviceToHost,
                                    st));
@@ -1593,7 +1604,8 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
                                           (uint64_t)(uintptr_t)L.h_hist.p, (uint64_t)(uintptr_t)L.h_counters.p,
                                           (uint64_t)(uintptr_t)acos_t.keys, (uint64_t)(uintptr_t)acos_t.vals,
                                           (uint64_t)(uintptr_t)acos_t.bucket, (uint64_t)acos_t.n, queue_cap,
-                                          (uint64_t)grid, (uint64_t)copies, (uint64_t)sh.groups, hist_total, ntasks};
+                                          (uint64_t)grid, (uint64_t)copies, (uint64_t)sh.groups, hist_total, ntasks,
+                                          (uint64_t)slice};
                 gsig.insert(gsig.end(), extra, extra + sizeof(extra) / sizeof(extra[0]));
                 if (!L.graph || gsig != L.graph_sig) {
                     L.drop_graph();
@@ -1852,6 +1864,7 @@ void worker_loop(tpcf_ctx* ctx, int lane) {
                 }
                 // a heavy batch leaves SMs to the light lanes (its CTAs are persistent)
                 L.sm_cap = first_heavy && ctx->reserve_sms > 0 ? ctx->num_sms - ctx->reserve_sms : 0;
+                L.slice_batches = first_heavy && ctx->slice_heavy;
                 ctx->inflight_bytes += used;
                 break;
             }
@@ -1928,6 +1941,10 @@ tpcf_status tpcf_create(tpcf_ctx** out, int32_t device) {
         if (adm) ctx->admit_bytes = atoll(adm);
         const char* hc = getenv("TPCF_HEAVY_COST");
         if (hc) ctx->heavy_cost = atof(hc);
+        const char* shv = getenv("TPCF_SLICE_HEAVY");
+        if (shv) ctx->slice_heavy = shv[0] != '0';
+        const char* stk = getenv("TPCF_SLICE_TASKS");
+        if (stk) ctx->slice_tasks = std::max(0, atoi(stk));
         const char* lbc = getenv("TPCF_LIGHT_BATCH_COST");
         if (lbc) ctx->light_batch_cost = atof(lbc);
         // SMs a heavy serving batch leaves to the light lanes: none by default
@@ -1939,7 +1956,12 @@ tpcf_status tpcf_create(tpcf_ctx** out, int32_t device) {
         int workers = nw ? std::max(1, std::min(8, atoi(nw))) : 3;
         for (int i = 0; i <= workers; i++) {
             auto L = std::make_unique<Lane>();
-            CK(cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking));
+            // the light serving lanes (2 and up) get the highest stream
+            // priority: their kernels start at the next slice boundary of a
+            // heavy batch
+            int prio_least = 0, prio_greatest = 0;
+            CK(cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest));
+            CK(cudaStreamCreateWithPriority(&L->stream, cudaStreamNonBlocking, i >= 2 ? prio_greatest : prio_least));
             CK(cudaEventCreate(&L->ev0));
             CK(cudaEventCreate(&L->ev1));
             CK(cudaEventCreate(&L->ev_mid));

@@ -65,6 +65,24 @@ def test_results_identical_alone_and_in_the_mix():
         assert sum(int(a.sum()) for a in alone) > 0
 
 
+@pytest.mark.parametrize("slice_heavy", ["1", "0"])
+def test_heavy_jobs_in_slices_identical(monkeypatch, slice_heavy):
+    """Every job counted as heavy (TPCF_HEAVY_COST=1): heavy serving batches
+    run alone on the first lane, in slices of their task list, while light
+    lanes (none here) could run between the slices; each result equals its
+    count alone."""
+    monkeypatch.setenv("TPCF_HEAVY_COST", "1")
+    monkeypatch.setenv("TPCF_SLICE_HEAVY", slice_heavy)
+    monkeypatch.setenv("TPCF_SLICE_TASKS", "7")  # many slices even for these small jobs
+    with tpcf.Engine(0) as eng:
+        handles = [eng.catalog(c) for c in _catalogs()]
+        jobs = _jobs(eng, handles)
+        alone = [eng.count(s, j) for s, j in jobs]
+        tickets = [eng.submit(s, j) for s, j in jobs]
+        for (spec, _), t, want in zip(jobs, tickets, alone):
+            assert np.array_equal(eng.wait(t, spec), want)
+
+
 def test_cancel_and_timeout():
     with tpcf.Engine(0) as eng:
         h = eng.catalog(synth.blobs(6000, n_blobs=6, sigma=5.0, box=60.0, seed=3))
