@@ -187,11 +187,16 @@ struct PinnedBuf {
         p = nullptr;
         n = 0;
     }
+    // grows to a power of two: cudaFreeHost waits for all work on the device,
+    // so a serving lane that reallocated for every new batch size would wait
+    // for the other lanes' kernels
     void reserve(size_t m) {
         if (m <= n) return;
         release();
-        CK(cudaMallocHost((void**)&p, std::max<size_t>(m, 1) * sizeof(T)));
-        n = m;
+        size_t c = 4096;
+        while (c < m) c <<= 1;
+        CK(cudaMallocHost((void**)&p, c * sizeof(T)));
+        n = c;
     }
 };
 
@@ -804,6 +809,10 @@ struct tpcf_ctx {
     uint64_t next_ticket = 1;
     std::vector<std::thread> workers;
     bool stop = false;
+    // serving trace (TPCF_SERVING_TRACE=file): one line per batch, written by
+    // tpcf_destroy: lane, jobs, first ticket, oldest submit, start, planned, done (ms)
+    std::string trace_path;
+    std::vector<std::string> trace;
     int64_t admit_bytes = (int64_t)8 << 30;
     double heavy_cost = 1e12;  // job_cost above which a job runs alone on the first serving lane
     double light_batch_cost = 2.5e11;  // summed job_cost at which a batch of light jobs closes
@@ -1881,6 +1890,15 @@ void worker_loop(tpcf_ctx* ctx, int lane) {
         }
         tpcf_status st = guarded(ctx, [&] { run_group(ctx, L, group); });
         double t_done = now_ms();
+        if (!ctx->trace_path.empty()) {
+            double oldest = t_start;
+            for (auto& p : batch) oldest = std::min(oldest, p->t_submit);
+            char line[256];
+            snprintf(line, sizeof(line), "%d %zu %llu %.3f %.3f %.3f %.3f\n", lane, batch.size(),
+                     (unsigned long long)batch[0]->ticket, oldest, t_start, t_start + L.stats.plan_ms, t_done);
+            std::lock_guard<std::mutex> lk(ctx->qmu);
+            ctx->trace.push_back(line);
+        }
         {
             std::lock_guard<std::mutex> lk(ctx->qmu);
             ctx->inflight_bytes -= used;
@@ -1941,6 +1959,7 @@ tpcf_status tpcf_create(tpcf_ctx** out, int32_t device) {
         if (adm) ctx->admit_bytes = atoll(adm);
         const char* hc = getenv("TPCF_HEAVY_COST");
         if (hc) ctx->heavy_cost = atof(hc);
+        if (const char* tr = getenv("TPCF_SERVING_TRACE")) ctx->trace_path = tr;
         const char* shv = getenv("TPCF_SLICE_HEAVY");
         if (shv) ctx->slice_heavy = shv[0] != '0';
         const char* stk = getenv("TPCF_SLICE_TASKS");
@@ -1965,6 +1984,19 @@ tpcf_status tpcf_create(tpcf_ctx** out, int32_t device) {
             CK(cudaEventCreate(&L->ev0));
             CK(cudaEventCreate(&L->ev1));
             CK(cudaEventCreate(&L->ev_mid));
+            if (i >= 1) {
+                // serving lanes: buffers sized up front.  A device or
+                // page-locked allocation issued while another lane's kernel
+                // runs keeps this lane's next kernel from running beside it
+                // (implicit synchronisation), so light batches must not allocate.
+                L->h_hist.reserve((size_t)1 << 20);
+                L->h_counters.reserve(8);
+                L->d_hist.reserve((size_t)1 << 22);
+                L->d_counters.reserve(8);
+                L->d_jobs.reserve((size_t)1 << 16);
+                L->d_tasks.reserve((size_t)1 << 21);
+                L->d_queue.reserve((size_t)1 << 22);
+            }
             ctx->lanes.push_back(std::move(L));
         }
     });
@@ -1988,6 +2020,12 @@ tpcf_status tpcf_destroy(tpcf_ctx* ctx) {
     ctx->qcv.notify_all();
     for (auto& t : ctx->workers)
         if (t.joinable()) t.join();
+    if (!ctx->trace_path.empty()) {
+        if (FILE* f = fopen(ctx->trace_path.c_str(), "w")) {
+            for (auto& l : ctx->trace) fputs(l.c_str(), f);
+            fclose(f);
+        }
+    }
     {
         std::lock_guard<std::recursive_mutex> lk(ctx->mu);
         std::lock_guard<std::recursive_mutex> vlk(ctx->view_mu);

@@ -364,7 +364,12 @@ __device__ __forceinline__ bool mask_bit(unsigned mask, unsigned idx) { return (
 
 // Two floats in one 64-bit register for the packed FP32 instructions of
 // sm_100+ (add/sub/mul/fma .rn .f32x2: two IEEE single operations per
-// instruction, each element rounded exactly as the scalar operation).
+// instruction, each element rounded exactly as the scalar operation).  Unlike
+// the scalar __fmul_rn/__fadd_rn intrinsics, a packed product that feeds a
+// packed sum is contracted into one fma.f32x2 by ptxas (measured: the packed
+// squared side sums differ from the scalar ones in a fifth of the cases), so
+// only results whose exact rounding does not matter, or that no contraction
+// can reach, are computed packed.
 typedef unsigned long long f32x2;
 __device__ __forceinline__ f32x2 pk2(float a, float b) {
     f32x2 r;
@@ -457,7 +462,13 @@ __device__ __forceinline__ void triangle_full2(const float (&a)[2], const int (&
         off_m[t] = max(wlo, min(whi, wc[t])) >> 7;
     }
     const f32x2 S = pk2(s[0], s[1]), M = pk2(m[0], m[1]), L = pk2(l[0], l[1]);
-    const f32x2 S2 = mul2(S, S), M2 = mul2(M, M), L2 = mul2(L, L);
+    // the squares enter the cosine numerators as the reference rounds them:
+    // scalar products (ptxas contracts a packed mul.rn.f32x2 feeding an
+    // add.rn.f32x2 into fma.f32x2, measured on sm_103a, which would change
+    // the numerators' rounding)
+    const f32x2 S2 = pk2(__fmul_rn(s[0], s[0]), __fmul_rn(s[1], s[1]));
+    const f32x2 M2 = pk2(__fmul_rn(m[0], m[0]), __fmul_rn(m[1], m[1]));
+    const f32x2 L2 = pk2(__fmul_rn(l[0], l[0]), __fmul_rn(l[1], l[1]));
     const f32x2 qs = splat2(p.q_scale), qo = splat2(p.q_off);
     const f32x2 rsq = mul2(pk2(rcp_approx(s[0]), rcp_approx(s[1])), qs);
     const f32x2 rmq = mul2(pk2(rcp_approx(m[0]), rcp_approx(m[1])), qs);
@@ -573,8 +584,8 @@ __device__ __forceinline__ void load_points(float4* P, const DevJob& J, const Ta
 
 __device__ __forceinline__ int pkey(float4 p) { return __float_as_int(p.w); }
 
-// Candidate triangle of the current i: j (6 bits), k (6 bits), weight (2 bits).
-__device__ __forceinline__ uint32_t pack_cand(int j, int k, unsigned w) { return (uint32_t)j | ((uint32_t)k << 6) | (w << 12); }
+// Queued candidate triangle of the current i: j (bits 0-5), k (bits 6-11) and
+// its weight (bits 12-13).
 
 // Runs the full binning path on n (<= 64) queued candidates, two per lane
 // (packed into the f32x2 instructions of one binning path).
@@ -825,7 +836,10 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
         // (A lane-parallel compaction of the j's with few candidates, through
         // a prefix sum of per-lane counts, measured slower on clustered data:
         // its scattered j/k break the conflict-free table reads of binning.)
-        const unsigned lt = (1u << lane) - 1u;
+        const unsigned lbit = 1u << lane, lt = lbit - 1u;
+        // queue entries of this lane's k = lane and k = lane + 32 (weight 1;
+        // plus j and the weight bit of two-array jobs)
+        const uint32_t klo = ((uint32_t)lane << 6) | (1u << 12), khi = ((uint32_t)(lane + 32) << 6) | (1u << 12);
         int qn = 0;  // queued candidates (warp-uniform)
 #pragma unroll
         for (int h = 0; h < 2; h++) {
@@ -834,26 +848,22 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
             while (live) {
                 const int src = __ffs(live) - 1;
                 live &= live - 1u;
-                const int j = src + 32 * h;
+                const uint32_t j = (uint32_t)(src + 32 * h);
                 const unsigned lo = __shfl_sync(0xffffffffu, (unsigned)cmv, src);
                 const unsigned hi = __shfl_sync(0xffffffffu, (unsigned)(cmv >> 32), src);
-                unsigned w2lo = 0, w2hi = 0;
+                uint32_t vlo = klo + j, vhi = khi + j;
                 if (PRED == PRED_DDR || PRED == PRED_RDD) {
-                    w2lo = __shfl_sync(0xffffffffu, (unsigned)w2v, src);
-                    w2hi = __shfl_sync(0xffffffffu, (unsigned)(w2v >> 32), src);
+                    const unsigned w2lo = __shfl_sync(0xffffffffu, (unsigned)w2v, src);
+                    const unsigned w2hi = __shfl_sync(0xffffffffu, (unsigned)(w2v >> 32), src);
+                    vlo += (w2lo & lbit) ? (1u << 12) : 0u;
+                    vhi += (w2hi & lbit) ? (1u << 12) : 0u;
                 }
                 const int nlo = __popc(lo);
-                if ((lo >> lane) & 1u) {
-                    const unsigned w = (PRED == PRED_DDR || PRED == PRED_RDD) ? 1u + ((w2lo >> lane) & 1u) : 1u;
-                    cand[qn + __popc(lo & lt)] = pack_cand(j, lane, w);
-                }
-                if ((hi >> lane) & 1u) {
-                    const unsigned w = (PRED == PRED_DDR || PRED == PRED_RDD) ? 1u + ((w2hi >> lane) & 1u) : 1u;
-                    cand[qn + nlo + __popc(hi & lt)] = pack_cand(j, lane + 32, w);
-                }
+                if (lo & lbit) cand[qn + __popc(lo & lt)] = vlo;
+                if (hi & lbit) cand[qn + nlo + __popc(hi & lt)] = vhi;
                 qn += nlo + __popc(hi);
-                __syncwarp();
                 if (qn >= 64) {
+                    __syncwarp();
                     qn -= 64;
                     run_candidates<THETA_FULL, JBJ>(cand + qn, 64, row_ij, row_ik, JK, p, Hw, q, slot, ia, g.b0, g.c0);
                     bn += 64;
@@ -861,6 +871,7 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
                 }
             }
         }
+        __syncwarp();
         if (qn > 0) {
             run_candidates<THETA_FULL, JBJ>(cand, qn, row_ij, row_ik, JK, p, Hw, q, slot, ia, g.b0, g.c0);
             bn += qn;
