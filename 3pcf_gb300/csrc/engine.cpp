@@ -755,6 +755,7 @@ struct Lane {
 struct Pending {
     uint64_t ticket;
     double t_submit = 0, t_start = 0, t_done = 0;  // steady-clock ms
+    double cost = 0;                                // job_cost at submission
     tpcf_spec spec;
     tpcf_job job;
     std::vector<uint64_t> result;
@@ -814,8 +815,9 @@ struct tpcf_ctx {
     std::string trace_path;
     std::vector<std::string> trace;
     int64_t admit_bytes = (int64_t)8 << 30;
-    double heavy_cost = 1e12;  // job_cost above which a job runs alone on the first serving lane
-    double light_batch_cost = 2.5e11;  // summed job_cost at which a batch of light jobs closes
+    double heavy_cost = 4e11;  // job_cost above which a job runs alone on the first serving lane (~50 ms)
+    double light_batch_cost = 1e11;  // summed job_cost at which a batch of light jobs closes
+    std::map<std::tuple<uint64_t, int64_t, int64_t, uint64_t, int64_t, int64_t, double>, double> density;
     int reserve_sms = 0;       // SMs a heavy serving batch leaves free for light jobs
     bool slice_heavy = true;   // heavy serving batches count in slices (light lanes run between them)
     int slice_tasks = 0;       // tasks per slice (0: at least 8 per CTA and at most 64 slices)
@@ -1793,15 +1795,53 @@ double now_ms() {
 // the device.
 // Work estimate of a job for scheduling: the product of its catalog range
 // sizes (the loop size up to a constant).
+// Mean number of points of catalog range b within 'reach' of a point of range
+// a, from 64 points spread over range a (cached per ranges and reach).
+// Called with ctx->mu held.
+double neighbour_density(tpcf_ctx* ctx, uint64_t ha, int64_t a0, int64_t a1, uint64_t hb, int64_t b0, int64_t b1,
+                         double reach) {
+    auto key = std::make_tuple(ha, a0, a1, hb, b0, b1, reach);
+    auto hit = ctx->density.find(key);
+    if (hit != ctx->density.end()) return hit->second;
+    const Catalog& A = *ctx->catalogs.at(ha);
+    const Catalog& B = *ctx->catalogs.at(hb);
+    const int64_t na = a1 - a0;
+    const double r2 = reach * reach;
+    const int samples = (int)std::min<int64_t>(64, na);
+    uint64_t near = 0;
+    for (int t = 0; t < samples; t++) {
+        const int64_t i = a0 + (int64_t)t * na / samples;
+        for (int64_t j = b0; j < b1; j++) {
+            const double dx = (double)A.x[i] - B.x[j], dy = (double)A.y[i] - B.y[j], dz = (double)A.z[i] - B.z[j];
+            near += dx * dx + dy * dy + dz * dz < r2;
+        }
+    }
+    const double rho = samples ? (double)near / samples : 0.0;
+    ctx->density[key] = rho;
+    return rho;
+}
+
+// Work estimate of a job for serving (which lane, how many per batch): the
+// number of index pairs (pairs) or of i-j, i-k pairs of sides (triangles)
+// within the largest side that can be counted, from the neighbour densities;
+// the product of the range sizes where every triple counts.  Called with
+// ctx->mu held, at submission.
 double job_cost(tpcf_ctx* ctx, const tpcf_spec& sp, const tpcf_job& job) {
-    double c = 1;
     int nc = sp.kind == TPCF_PAIR ? 2 : 3;
+    int64_t b[3] = {0, 0, 0}, e[3] = {0, 0, 0};
+    double prod = 1;
     for (int r = 0; r < nc; r++) {
         auto it = ctx->catalogs.find(job.catalog[r]);
-        if (it == ctx->catalogs.end()) continue;
-        int64_t e = job.end[r] < 0 ? it->second->n : job.end[r];
-        c *= (double)std::max<int64_t>(e - job.begin[r], 0);
+        if (it == ctx->catalogs.end()) return 0;
+        b[r] = job.begin[r];
+        e[r] = job.end[r] < 0 ? it->second->n : job.end[r];
+        prod *= (double)std::max<int64_t>(e[r] - b[r], 0);
     }
+    const double reach = make_binning(sp).lmax;
+    if (!(reach < 1e30) || (sp.kind == TPCF_THREE_SIDE && sp.overflow != TPCF_OVERFLOW_CLEAN)) return prod;
+    const double na = (double)(e[0] - b[0]);
+    double c = na * neighbour_density(ctx, job.catalog[0], b[0], e[0], job.catalog[1], b[1], e[1], reach);
+    if (nc == 3) c *= neighbour_density(ctx, job.catalog[0], b[0], e[0], job.catalog[2], b[2], e[2], reach);
     return c;
 }
 
@@ -1811,7 +1851,7 @@ void worker_loop(tpcf_ctx* ctx, int lane) {
     // the first serving lane takes any job; the others only light ones, so
     // that light jobs keep flowing while heavy ones run
     const bool light_only = lane >= 2;
-    auto heavy = [&](const Pending& p) { return job_cost(ctx, p.spec, p.job) > ctx->heavy_cost; };
+    auto heavy = [&](const Pending& p) { return p.cost > ctx->heavy_cost; };
     for (;;) {
         std::vector<std::shared_ptr<Pending>> batch;
         int64_t used = 0;
@@ -1861,7 +1901,7 @@ void worker_loop(tpcf_ctx* ctx, int lane) {
                         ++it;
                         continue;
                     }
-                    const double c = job_cost(ctx, p->spec, p->job);
+                    const double c = p->cost;
                     if (!batch.empty() && batch_cost + c > ctx->light_batch_cost) break;
                     int64_t jb = job_bytes(ctx, p->spec, p->job);
                     if (!batch.empty() && used + jb > room) break;
@@ -2230,15 +2270,22 @@ tpcf_status tpcf_count(tpcf_ctx* ctx, const tpcf_spec* spec, const tpcf_job* job
 
 tpcf_status tpcf_submit(tpcf_ctx* ctx, const tpcf_spec* spec, const tpcf_job* job, uint64_t* ticket) {
     if (!ctx || !spec || !job || !ticket) return fail(ctx, TPCF_ERR_INVALID, "null argument");
+    double cost = 0;
     tpcf_status s = guarded(ctx, [&] {
         std::lock_guard<std::recursive_mutex> lk(ctx->mu);
         validate(spec, job);
         int nc = spec->kind == TPCF_PAIR ? 2 : 3;
-        for (int r = 0; r < nc; r++)
-            if (!ctx->catalogs.count(job->catalog[r])) throw InvalidArg{"unknown catalog handle"};
+        for (int r = 0; r < nc; r++) {
+            auto it = ctx->catalogs.find(job->catalog[r]);
+            if (it == ctx->catalogs.end()) throw InvalidArg{"unknown catalog handle"};
+            const int64_t e = job->end[r] < 0 ? it->second->n : job->end[r];
+            if (job->begin[r] < 0 || job->begin[r] > e || e > it->second->n) throw InvalidArg{"catalog range out of bounds"};
+        }
+        cost = job_cost(ctx, *spec, *job);
     });
     if (s != TPCF_OK) return s;
     auto p = std::make_shared<Pending>();
+    p->cost = cost;
     p->spec = *spec;
     p->job = *job;
     p->t_submit = now_ms();
