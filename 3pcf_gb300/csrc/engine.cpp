@@ -700,6 +700,28 @@ uint64_t loop_units(int kind, int loop, const int64_t n[3]) {
 // ---------------------------------------------------------------------------
 // context
 
+// tile triples (pairs) with their unit estimates, in enumeration order
+typedef std::vector<std::pair<uint64_t, uint4>> TaskList;
+
+// one window's task groups of the fast triangle kernel: sizes, boxes (lo, hi)
+// of their A tiles and summed unit estimates; keys: radix-sort scratch
+struct GroupedPart {
+    std::vector<uint32_t> sizes;
+    std::vector<float> boxes;
+    std::vector<uint64_t> units;
+    std::vector<uint64_t> keys[2];
+};
+
+// host buffers of the planner, kept from batch to batch so that they are not
+// allocated (and paged in) again for every batch
+struct PlanScratch {
+    std::vector<TaskList> part;
+    std::vector<GroupedPart> gpart;
+    std::vector<uint4> tasks;
+    std::vector<uint32_t> groups;
+    std::vector<float> gbox;
+};
+
 // One lane = one stream with its own scratch buffers.  The synchronous API uses
 // lane 0; every serving worker owns one further lane, so batches of different
 // workers run concurrently on the device.
@@ -709,6 +731,8 @@ struct Lane {
     uint64_t h2d = 0, d2h = 0;  // bytes copied since the last stats read
     DevBuf<DevJob> d_jobs;
     DevBuf<uint4> d_tasks;
+    DevBuf<uint32_t> d_groups;  // fast triangle kernel: first task of each group (+ end)
+    DevBuf<float> d_gbox;       // ... and the box of each group's A tiles
     DevBuf<unsigned int> d_counters;  // [0] task counter, [1] recheck count, [2..5] evaluated/binned
     DevBuf<uint4> d_queue;
     DevBuf<unsigned long long> d_hist;
@@ -717,6 +741,7 @@ struct Lane {
     // last planned batch (see run_group)
     std::vector<uint64_t> plan_sig;
     size_t plan_ntasks = 0;
+    size_t plan_ngroups = 0;  // task groups of the fast triangle kernel
     uint64_t plan_evaluated = 0;
     // the launch sequence of the last batch, captured as a CUDA graph and
     // replayed while the batch and every buffer it touches stay the same
@@ -728,6 +753,7 @@ struct Lane {
     int sm_cap = 0;
     // count in slices of the task list (heavy serving batches)
     bool slice_batches = false;
+    PlanScratch scratch;
     tpcf_stats stats{};
     void drop_graph() {
         if (graph) cudaGraphExecDestroy(graph);
@@ -740,9 +766,12 @@ struct Lane {
         h_counters.release();
         d_jobs.release();
         d_tasks.release();
+        d_groups.release();
+        d_gbox.release();
         d_counters.release();
         d_queue.release();
         d_hist.release();
+        scratch = PlanScratch();
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (ev_mid) cudaEventDestroy(ev_mid);
@@ -821,6 +850,7 @@ struct tpcf_ctx {
     int reserve_sms = 0;       // SMs a heavy serving batch leaves free for light jobs
     bool slice_heavy = true;   // heavy serving batches count in slices (light lanes run between them)
     int slice_tasks = 0;       // tasks per slice (0: at least 8 per CTA and at most 64 slices)
+    int group_tasks = 4;       // fast triangle kernel: most tasks sharing one j-k table
     int64_t inflight_bytes = 0;  // device bytes of batches running on serving lanes
     // autotuner: launch shape per batch signature
     std::mutex tune_mu;
@@ -1012,7 +1042,6 @@ bool tri_triple_possible(const Binning& bin, double l0, double l1, double l2, do
     return p0 || p1;
 }
 
-typedef std::vector<std::pair<uint64_t, uint4>> TaskList;
 
 // Lower/upper side bounds and neighbour lists (tile pairs whose lower bound is
 // below lmax) of one pair of views, shared by every job of a launch that
@@ -1345,6 +1374,125 @@ int grid_for(tpcf_ctx* ctx, const Shape& sh, uint64_t ntasks, int sm_cap) {
     return (int)g;
 }
 
+// Task groups of the fast triangle kernel: tasks of one job with the same
+// tiles B and C run one after another in one CTA, which builds their j-k
+// table once.  Each window of planning parts (one job, a run of consecutive A
+// tiles) groups its own tasks, in parallel with the others: a sort on (b, c)
+// that keeps the order of A tiles, runs of equal (b, c) cut into groups of at
+// most max_group tasks (a group is the unit a CTA takes, so large ones would
+// leave a long tail at the end of the launch).  boxes: lo/hi of the union of each
+// group's A tiles, for the j-k rows that no point of the group can reach;
+// units: the group's summed task estimates.
+
+void group_parts(const TaskList* parts, size_t nparts, const PlannedJob& J, size_t max_group, uint4* dst,
+                 GroupedPart& out) {
+    const uint64_t nc = (uint64_t)J.role(2)->ntiles;
+    size_t n = 0;
+    for (size_t i = 0; i < nparts; i++) n += parts[i].size();
+    // (b, c) key above the task's index in the window, sorted by an LSD
+    // radix sort on the key (stable: ties stay in the order of A tiles)
+    std::vector<uint64_t>&ka = out.keys[0], &kb = out.keys[1];
+    ka.resize(n);
+    kb.resize(n);
+    uint64_t kmax = 0;
+    for (size_t i = 0, t = 0; i < nparts; i++)
+        for (const auto& pr : parts[i]) {
+            const uint64_t k = (uint64_t)pr.second.z * nc + pr.second.w;
+            kmax = std::max(kmax, k);
+            ka[t] = k << 32 | t;
+            t++;
+        }
+    for (int shift = 32; shift < 64 && (kmax >> (shift - 32)) != 0; shift += 8) {
+        uint32_t cnt[257] = {0};
+        for (size_t t = 0; t < n; t++) cnt[((ka[t] >> shift) & 255) + 1]++;
+        for (int d = 0; d < 256; d++) cnt[d + 1] += cnt[d];
+        for (size_t t = 0; t < n; t++) kb[cnt[(ka[t] >> shift) & 255]++] = ka[t];
+        ka.swap(kb);
+    }
+    // the window's tasks by index
+    std::vector<const std::pair<uint64_t, uint4>*> src(n);
+    for (size_t i = 0, t = 0; i < nparts; i++)
+        for (const auto& pr : parts[i]) src[t++] = &pr;
+    const View& A = *J.role(0);
+    out.sizes.resize(n);
+    out.boxes.resize(6 * n);
+    out.units.resize(n);
+    size_t ng = 0;
+    for (size_t t = 0; t < n;) {
+        const uint64_t k = ka[t] >> 32;
+        size_t e = t + 1;
+        while (e < n && e - t < max_group && (ka[e] >> 32) == k) e++;
+        float* bx = &out.boxes[6 * ng];
+        bx[0] = bx[1] = bx[2] = INFINITY;
+        bx[3] = bx[4] = bx[5] = -INFINITY;
+        uint64_t u = 0;
+        for (size_t q = t; q < e; q++) {
+            const auto& pr = *src[(uint32_t)ka[q]];
+            dst[q] = pr.second;
+            u += pr.first;
+            const Box& b = A.boxes[pr.second.y];
+            for (int d = 0; d < 3; d++) {
+                bx[d] = std::min(bx[d], b.lo[d]);
+                bx[3 + d] = std::max(bx[3 + d], b.hi[d]);
+            }
+        }
+        out.sizes[ng] = (uint32_t)(e - t);
+        out.units[ng++] = u;
+        t = e;
+    }
+    out.sizes.resize(ng);
+    out.boxes.resize(6 * ng);
+    out.units.resize(ng);
+}
+
+// Group starts (ngroups + 1 entries) and boxes of the grouped windows, whose
+// tasks are in place in `tasks` (window w from toff[w]).  With few tasks per
+// CTA the groups go largest first (summed estimates), so that the dynamic
+// fetch balances the tail; else in window order (job order).
+void assemble_groups(const std::vector<GroupedPart>& gp, size_t nw, const std::vector<size_t>& toff,
+                     bool largest_first, std::vector<uint4>& tasks, std::vector<uint32_t>& starts,
+                     std::vector<float>& boxes) {
+    std::vector<size_t> goff(nw + 1, 0);
+    for (size_t i = 0; i < nw; i++) goff[i + 1] = goff[i] + gp[i].sizes.size();
+    const size_t total = toff[nw], ng = goff[nw];
+    starts.resize(ng + 1);
+    boxes.resize(6 * ng);
+    starts[ng] = (uint32_t)total;
+    if (largest_first) {
+        std::vector<std::array<uint32_t, 2>> ref;  // window, group in window
+        std::vector<uint32_t> first;                // its first task
+        std::vector<uint64_t> units;
+        for (size_t i = 0; i < nw; i++)
+            for (uint32_t g = 0, t = (uint32_t)toff[i]; g < gp[i].sizes.size(); t += gp[i].sizes[g], g++) {
+                ref.push_back({(uint32_t)i, g});
+                first.push_back(t);
+                units.push_back(gp[i].units[g]);
+            }
+        std::vector<uint32_t> order(ng);
+        for (size_t g = 0; g < ng; g++) order[g] = (uint32_t)g;
+        std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return units[a] > units[b]; });
+        const std::vector<uint4> in(tasks.begin(), tasks.begin() + total);
+        size_t w = 0;
+        for (size_t o = 0; o < ng; o++) {
+            const auto& r = ref[order[o]];
+            const GroupedPart& P = gp[r[0]];
+            starts[o] = (uint32_t)w;
+            for (uint32_t t = 0; t < P.sizes[r[1]]; t++) tasks[w++] = in[first[order[o]] + t];
+            std::copy(&P.boxes[6 * r[1]], &P.boxes[6 * r[1]] + 6, &boxes[6 * o]);
+        }
+        return;
+    }
+    parallel_items(nw, [&](size_t i) {
+        const GroupedPart& P = gp[i];
+        std::copy(P.boxes.begin(), P.boxes.end(), boxes.begin() + 6 * goff[i]);
+        uint32_t s = (uint32_t)toff[i];
+        for (size_t g = 0; g < P.sizes.size(); g++) {
+            starts[goff[i] + g] = s;
+            s += P.sizes[g];
+        }
+    });
+}
+
 // Runs one group of jobs that share kind, binning and precision in a single
 // persistent launch.  outs[i] receives hist_len counts.
 void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
@@ -1421,10 +1569,23 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
     }
     cudaStream_t st = L.stream;
     L.d_counters.reserve(8);
-    size_t ntasks = 0;
+    size_t ntasks = 0, ngroups = 0;
     const bool plan_hit = sig == L.plan_sig;
+    // TPCF_PLAN_TRACE=1: the planning phases' wall times on stderr
+    static const bool plan_trace = [] {
+        const char* e = getenv("TPCF_PLAN_TRACE");
+        return e && e[0] == '1';
+    }();
+    std::vector<std::pair<const char*, double>> phases;
+    auto phase = [&](const char* name) {
+        if (plan_trace)
+            phases.push_back({name, std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() -
+                                                                              t_wall0).count()});
+    };
+    phase("views");
     if (plan_hit) {
         ntasks = L.plan_ntasks;
+        ngroups = L.plan_ngroups;
         evaluated = L.plan_evaluated;
     } else {
         // plan in parallel: bound tables and neighbour lists by rows, then
@@ -1462,6 +1623,9 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
                 table_list[it[0]]->rows(it[1], it[2]);
             });
         }
+        phase("tables");
+        const bool fast_tri = (sp.kind == TPCF_TRIANGLE || sp.kind == TPCF_TRIANGLE_JBJ) &&
+                              sp.precision == TPCF_GUARDED_FP32;
         std::vector<std::array<int, 3>> items;  // job, A-tile begin, end
         for (size_t g = 0; g < group.size(); g++) {
             const int na = pj[g].role(0)->ntiles, step = pairs ? 16 : 2;
@@ -1469,43 +1633,84 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
         }
         // one task list per item, so that the concatenation keeps job order
         // (a CTA flushes its shared histogram whenever the job changes)
-        std::vector<TaskList> part(items.size());
+        PlanScratch& S = L.scratch;
+        std::vector<TaskList>& part = S.part;
+        if (part.size() < items.size()) part.resize(items.size());
         std::vector<uint64_t> part_eval(items.size(), 0);
         parallel_items(items.size(), [&](size_t i) {
             const auto& it = items[i];
+            part[i].clear();
             if (pairs)
                 plan_pairs(*group[it[0]].spec, pj[it[0]], (uint32_t)it[0], bin.lmax, it[1], it[2], part[i],
                            part_eval[i]);
             else
                 tp[it[0]].enumerate(it[1], it[2], part[i], part_eval[i]);
         });
-        size_t total = 0;
-        for (size_t i = 0; i < part.size(); i++) {
-            evaluated += part_eval[i];
-            total += part[i].size();
+        phase("enumerate");
+        // fast triangle kernel: groups form in windows of consecutive items of
+        // one job spanning twice the group size in A tiles
+        std::vector<std::array<size_t, 2>> windows;  // first item, item count
+        if (fast_tri) {
+            const size_t per = (size_t)std::max(1, ctx->group_tasks);
+            for (size_t i = 0; i < items.size();) {
+                size_t e = i + 1;
+                while (e < items.size() && e - i < per && items[e][0] == items[i][0]) e++;
+                windows.push_back({i, e - i});
+                i = e;
+            }
         }
-        std::vector<uint4> h_tasks(total);
-        // (three-side histograms above 8192 bins keep job order: their CTAs
-        // flush, and the task pipelines of one CTA meet, at every job change)
-        if (total <= (size_t)ctx->num_sms * 3 * 64 && !(sp.kind == TPCF_THREE_SIDE && bin.len > 8192)) {
+        std::vector<size_t> off(items.size() + 1, 0);  // each item's first task
+        for (size_t i = 0; i < items.size(); i++) {
+            evaluated += part_eval[i];
+            off[i + 1] = off[i] + part[i].size();
+        }
+        const size_t total = off[items.size()];
+        std::vector<uint4>& h_tasks = S.tasks;
+        std::vector<uint32_t>& h_groups = S.groups;
+        std::vector<float>& h_gbox = S.gbox;
+        h_tasks.resize(total);
+        h_groups.clear();
+        h_gbox.clear();
+        if (fast_tri) {
+            if (S.gpart.size() < windows.size()) S.gpart.resize(windows.size());
+            std::vector<size_t> toff(windows.size() + 1);
+            for (size_t w = 0; w < windows.size(); w++) toff[w] = off[windows[w][0]];
+            toff[windows.size()] = total;
+            parallel_items(windows.size(), [&](size_t w) {
+                group_parts(&part[windows[w][0]], windows[w][1], pj[items[windows[w][0]][0]],
+                            (size_t)ctx->group_tasks, h_tasks.data() + toff[w], S.gpart[w]);
+            });
+            assemble_groups(S.gpart, windows.size(), toff, total <= (size_t)ctx->num_sms * 3 * 64, h_tasks, h_groups,
+                            h_gbox);
+        } else if (total <= (size_t)ctx->num_sms * 3 * 64 && !(sp.kind == TPCF_THREE_SIDE && bin.len > 8192)) {
+            // (three-side histograms above 8192 bins keep job order: their CTAs
+            // flush, and the task pipelines of one CTA meet, at every job change)
             // few tasks per CTA: largest first, so that the dynamic fetch
             // balances the tail (a stable counting pass over 64 size classes)
             auto cls = [](uint64_t u) { return 63 - (u ? 63 - __builtin_clzll(u) : 0); };
             std::vector<size_t> start(65, 0);
-            for (auto& pt : part)
-                for (auto& e : pt) start[cls(e.first) + 1]++;
+            for (size_t i = 0; i < items.size(); i++)
+                for (auto& e : part[i]) start[cls(e.first) + 1]++;
             for (int c = 0; c < 64; c++) start[c + 1] += start[c];
-            for (auto& pt : part)
-                for (auto& e : pt) h_tasks[start[cls(e.first)]++] = e.second;
+            for (size_t i = 0; i < items.size(); i++)
+                for (auto& e : part[i]) h_tasks[start[cls(e.first)]++] = e.second;
         } else {
             // many tasks per CTA: the tail is a small share; job order
-            std::vector<size_t> off(part.size() + 1, 0);
-            for (size_t i = 0; i < part.size(); i++) off[i + 1] = off[i] + part[i].size();
-            parallel_items(part.size(), [&](size_t i) {
+            parallel_items(items.size(), [&](size_t i) {
                 for (size_t e = 0; e < part[i].size(); e++) h_tasks[off[i] + e] = part[i][e].second;
             });
         }
+        phase("order");
         ntasks = h_tasks.size();
+        ngroups = h_groups.empty() ? 0 : h_groups.size() - 1;
+        if (ngroups) {
+            L.d_groups.reserve(h_groups.size());
+            L.d_gbox.reserve(h_gbox.size());
+            CK(cudaMemcpyAsync(L.d_groups.p, h_groups.data(), h_groups.size() * sizeof(uint32_t),
+                               cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(L.d_gbox.p, h_gbox.data(), h_gbox.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+            L.h2d += h_groups.size() * sizeof(uint32_t) + h_gbox.size() * sizeof(float);
+        }
         L.d_jobs.reserve(dj.size());
         L.d_tasks.reserve(std::max<size_t>(h_tasks.size(), 1));
         CK(cudaMemcpyAsync(L.d_jobs.p, dj.data(), dj.size() * sizeof(DevJob), cudaMemcpyHostToDevice, st));
@@ -1515,10 +1720,21 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
         CK(cudaStreamSynchronize(st));
         L.plan_sig = sig;
         L.plan_ntasks = ntasks;
+        L.plan_ngroups = ngroups;
         L.plan_evaluated = evaluated;
+        phase("upload");
     }
     L.stats.plan_ms =
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_wall0).count();
+    if (plan_trace) {
+        std::string line = "tpcf plan: tasks " + std::to_string(ntasks) + " groups " + std::to_string(ngroups);
+        double prev = 0;
+        for (auto& ph : phases) {
+            line += std::string(" ") + ph.first + " " + std::to_string(ph.second - prev);
+            prev = ph.second;
+        }
+        fprintf(stderr, "%s\n", line.c_str());
+    }
     const bool fp64 = sp.precision != TPCF_GUARDED_FP32;
     const bool fast_jbj = sp.kind == TPCF_TRIANGLE_JBJ && !fp64;  // the fast kernel's JBJ binning
     if (sp.kind == TPCF_TRIANGLE) ensure_acos(ctx);
@@ -1541,12 +1757,14 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
     // the batch repeats).  Returns the device time in ms.
     auto count_with = [&](const Shape& sh, bool allow_graph) -> float {
         const int copies = sh.copies;
-        const int grid = grid_for(ctx, sh, nt, L.sm_cap);
-        // slices of at least 8 tasks per CTA, at most 64 of them
-        unsigned int slice =
-            L.slice_batches ? std::max<unsigned int>((unsigned int)grid * 8u, (nt + 63u) / 64u) : std::max(nt, 1u);
+        // units the persistent CTAs pull: task groups (fast triangle kernel) or tasks
+        const unsigned int nwork = ngroups ? (unsigned int)ngroups : nt;
+        const int grid = grid_for(ctx, sh, nwork, L.sm_cap);
+        // slices of at least 8 units per CTA, at most 64 of them
+        unsigned int slice = L.slice_batches ? std::max<unsigned int>((unsigned int)grid * 8u, (nwork + 63u) / 64u)
+                                             : std::max(nwork, 1u);
         if (L.slice_batches && ctx->slice_tasks > 0) slice = (unsigned int)ctx->slice_tasks;
-        launches = (nt > slice ? (nt + slice - 1) / slice : 1) + ((sp.kind == TPCF_TRIANGLE && !fp64) ? 1 : 0);
+        launches = (nwork > slice ? (nwork + slice - 1) / slice : 1) + ((sp.kind == TPCF_TRIANGLE && !fp64) ? 1 : 0);
         for (int attempt = 0; attempt < 3; attempt++) {
             RecheckQueue q{};
             if (sp.kind == TPCF_TRIANGLE && !fp64) {
@@ -1570,15 +1788,16 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
                 EQ(cudaMemsetAsync(L.d_hist.p, 0, hist_total * sizeof(unsigned long long), st));
                 EQ(cudaMemsetAsync(L.d_counters.p, 0, 8 * sizeof(unsigned int), st));
                 EQ(cudaEventRecordWithFlags(L.ev0, st, ev_flags));
-                // the counting kernel over tasks [t0, t0 + n)
-                auto launch_main = [&](const uint4* tk, unsigned int n) -> cudaError_t {
+                // the counting kernel over tasks [t0, t0 + n) (groups [t0, t0 + n)
+                // for the fast triangle kernel)
+                auto launch_main = [&](unsigned int t0, unsigned int n) -> cudaError_t {
+                    const uint4* tk = L.d_tasks.p + t0;
                     if (sp.kind == TPCF_TRIANGLE && fp64)
                         return launch_triangle_fp64(L.d_jobs.p, tk, n, L.d_counters.p, bin.tri, acos_t, grid, copies,
                                                     sp.precision == TPCF_GEOMETRY_FP64 ? 1 : 0, st);
-                    if (sp.kind == TPCF_TRIANGLE)
-                        return launch_triangle_fast(L.d_jobs.p, tk, n, L.d_counters.p, bin.tri, q, grid, copies, 0, st);
-                    if (fast_jbj)  // JBJ in FP32: the fast kernel, exact without a recheck
-                        return launch_triangle_fast(L.d_jobs.p, tk, n, L.d_counters.p, bin.tri, q, grid, copies, 1, st);
+                    if (sp.kind == TPCF_TRIANGLE || fast_jbj)  // JBJ in FP32: exact without a recheck
+                        return launch_triangle_fast(L.d_jobs.p, L.d_tasks.p, L.d_groups.p + t0, L.d_gbox.p + 6 * (size_t)t0,
+                                                    n, L.d_counters.p, bin.tri, q, grid, copies, fast_jbj ? 1 : 0, st);
                     if (sp.kind == TPCF_TRIANGLE_JBJ)
                         return launch_triangle_fp64(L.d_jobs.p, tk, n, L.d_counters.p, bin.tri, acos_t, grid, copies, 2,
                                                     st);
@@ -1590,10 +1809,10 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
                 // one launch over all tasks, or (a heavy serving batch) slices of
                 // them, between which the device can start the kernels that
                 // higher-priority streams (the light serving lanes) have queued
-                EQ(launch_main(L.d_tasks.p, std::min(nt, slice)));
-                for (unsigned int t0 = slice; t0 < nt; t0 += slice) {
+                EQ(launch_main(0, std::min(nwork, slice)));
+                for (unsigned int t0 = slice; t0 < nwork; t0 += slice) {
                     EQ(cudaMemsetAsync(L.d_counters.p, 0, sizeof(unsigned int), st));  // the slice's task counter
-                    EQ(launch_main(L.d_tasks.p + t0, std::min(slice, nt - t0)));
+                    EQ(launch_main(t0, std::min(slice, nwork - t0)));
                 }
                 EQ(cudaEventRecordWithFlags(L.ev_mid, st, ev_flags));
                 if (sp.kind == TPCF_TRIANGLE && !fp64)
@@ -1616,7 +1835,8 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
                                           (uint64_t)(uintptr_t)acos_t.keys, (uint64_t)(uintptr_t)acos_t.vals,
                                           (uint64_t)(uintptr_t)acos_t.bucket, (uint64_t)acos_t.n, queue_cap,
                                           (uint64_t)grid, (uint64_t)copies, (uint64_t)sh.groups, hist_total, ntasks,
-                                          (uint64_t)slice};
+                                          (uint64_t)slice, (uint64_t)(uintptr_t)L.d_groups.p,
+                                          (uint64_t)(uintptr_t)L.d_gbox.p, (uint64_t)ngroups};
                 gsig.insert(gsig.end(), extra, extra + sizeof(extra) / sizeof(extra[0]));
                 if (!L.graph || gsig != L.graph_sig) {
                     L.drop_graph();
@@ -2000,6 +2220,7 @@ tpcf_status tpcf_create(tpcf_ctx** out, int32_t device) {
         const char* hc = getenv("TPCF_HEAVY_COST");
         if (hc) ctx->heavy_cost = atof(hc);
         if (const char* tr = getenv("TPCF_SERVING_TRACE")) ctx->trace_path = tr;
+        if (const char* gt = getenv("TPCF_GROUP_TASKS")) ctx->group_tasks = std::max(1, atoi(gt));
         const char* shv = getenv("TPCF_SLICE_HEAVY");
         if (shv) ctx->slice_heavy = shv[0] != '0';
         const char* stk = getenv("TPCF_SLICE_TASKS");

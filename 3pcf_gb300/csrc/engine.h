@@ -141,9 +141,11 @@ struct LaunchStats {
 
 // ---- kernel launchers (kernels.cu) ----
 cudaError_t prepare_kernels(int device);  // once per device before any launch
-cudaError_t launch_triangle_fast(const DevJob* jobs, const uint4* tasks, unsigned int ntasks,
-                                 unsigned int* task_counter, const TriParams& p, RecheckQueue q,
-                                 int grid, int hist_copies, int jbj, cudaStream_t st);  // jbj: JBJ binning
+// groups[g] .. groups[g + 1]: the tasks of group g (same job, tiles B and C);
+// gbox[6 g ..]: lo/hi of the union of their A tiles; jbj: JBJ binning
+cudaError_t launch_triangle_fast(const DevJob* jobs, const uint4* tasks, const uint32_t* groups, const float* gbox,
+                                 unsigned int ngroups, unsigned int* group_counter, const TriParams& p,
+                                 RecheckQueue q, int grid, int hist_copies, int jbj, cudaStream_t st);
 cudaError_t launch_triangle_recheck(const DevJob* jobs, RecheckQueue q, const TriParams& p, AcosTable t,
                                     int grid, cudaStream_t st);
 cudaError_t launch_triangle_fp64(const DevJob* jobs, const uint4* tasks, unsigned int ntasks,

@@ -661,18 +661,26 @@ template <int PRED, bool THETA_FULL, bool JBJ>
 __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams& p, float4* P, int2* JK,
                                    int2* IJ, int2* IK, uint32_t* Q, unsigned long long* JM, float* BX,
                                    unsigned int* Hw, RecheckQueue& q, unsigned long long& evaluated,
-                                   unsigned long long& binned, int* next_i) {
+                                   unsigned long long& binned, int* next_i, bool reuse_bc, const float* abox) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const TaskGeom g = task_geom(J, task);
     const uint32_t slot = task.x & TASK_SLOT_MASK;
     const bool diag_ij = task.x & TASK_DIAG_IJ, diag_jk = task.x & TASK_DIAG_JK;
-    load_points(P, J, g);
+    // the tasks of a group share tiles B and C: the first loads all three
+    // tiles and builds the j-k table, the others load tile A only
+    if (reuse_bc) {
+        __syncthreads();  // the previous task's i loop is done with tile A
+        for (int t = threadIdx.x; t < TILE; t += blockDim.x)
+            P[t] = t < g.nA ? J.pts[0][g.a0 + t] : make_float4(0.f, 0.f, 0.f, 0.f);
+    } else {
+        load_points(P, J, g);
+    }
     if (threadIdx.x == 0) *next_i = 0;
     __syncthreads();
-    // bounding boxes of the three tiles (two 32-point halves each), for tasks
-    // whose tiles are not wholly within reach of each other
+    // bounding boxes of tiles B and C (two 32-point halves each), for the
+    // points of A out of reach of a whole tile
     const bool chk_b = task.x & TASK_CHECK_B, chk_c = task.x & TASK_CHECK_C;
-    if ((chk_b || chk_c) && warp < 6) {
+    if (!reuse_bc && warp >= 2 && warp < 6) {
         const int role = warp >> 1, idx = (warp & 1) * 32 + lane;
         const int n = role == 0 ? g.nA : (role == 1 ? g.nB : g.nC);
         const float4 pt = P[role * TILE + idx];
@@ -694,7 +702,7 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
             }
         }
     }
-    __syncthreads();
+    if (!reuse_bc) __syncthreads();
     // a side that provably reaches lmax is rejected whatever its exact value:
     // points farther than that from a whole tile take no part in the task
     // (the 1e-5 margin covers the rounding of the bound and of the distance)
@@ -721,10 +729,18 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
         return s2 >= reach2;
     };
     // rows j of the j-k side table and their class masks, one warp per row
+    // (once per group of tasks); abox: the box of every A tile of the group
     const int key_k0 = pkey(P[2 * TILE + lane]), key_k1 = pkey(P[2 * TILE + lane + 32]);
-    for (int j = warp; j < g.nB; j += TRI_WARPS) {
+    for (int j = reuse_bc ? g.nB : warp; j < g.nB; j += TRI_WARPS) {
         const float4 pj = P[TILE + j];
-        if (chk_b && far_from(pj, 0)) {  // no i reaches j: empty masks, the row is never read
+        float a2 = 0.f;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const float v = a == 0 ? pj.x : (a == 1 ? pj.y : pj.z);
+            const float gap = fmaxf(0.f, fmaxf(abox[a] - v, v - abox[3 + a]));
+            a2 = fmaf(gap, gap, a2);
+        }
+        if (a2 >= reach2) {  // no i of the group reaches j: empty masks, the row is never read
             if (lane < JM_WORDS) JM[lane * TILE + j] = 0ull;
             continue;
         }
@@ -878,31 +894,40 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
         }
         __syncwarp();
     }
-    evaluated += ev;
-    binned += bn;
+    // (per-warp totals into the CTA's counters: no 64-bit accumulators live
+    // in registers across the kernel)
+    if (lane == 0) {
+        atomicAdd(&evaluated, (unsigned long long)ev);
+        atomicAdd(&binned, (unsigned long long)bn);
+    }
 }
 
 template <bool THETA_FULL, bool JBJ>
 __device__ __forceinline__ void triangle_dispatch(const DevJob& J, uint4 task, const TriParams& p, float4* P,
                                                   int2* JK, int2* IJ, int2* IK, uint32_t* Q,
                                                   unsigned long long* JM, float* BX, unsigned int* Hw, RecheckQueue& q,
-                                                  unsigned long long& ev, unsigned long long& bn, int* next_i) {
+                                                  unsigned long long& ev, unsigned long long& bn, int* next_i,
+                                                  bool reuse_bc, const float* abox) {
     switch ((task.x >> TASK_PRED_SHIFT) & TASK_PRED_MASK) {
-        case PRED_NONE: triangle_task_fast<PRED_NONE, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i); break;
-        case PRED_DDR: triangle_task_fast<PRED_DDR, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i); break;
-        case PRED_RDD: triangle_task_fast<PRED_RDD, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i); break;
-        case PRED_SAME: triangle_task_fast<PRED_SAME, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i); break;
-        default: triangle_task_fast<PRED_ONE, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i); break;
+        case PRED_NONE: triangle_task_fast<PRED_NONE, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i, reuse_bc, abox); break;
+        case PRED_DDR: triangle_task_fast<PRED_DDR, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i, reuse_bc, abox); break;
+        case PRED_RDD: triangle_task_fast<PRED_RDD, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i, reuse_bc, abox); break;
+        case PRED_SAME: triangle_task_fast<PRED_SAME, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i, reuse_bc, abox); break;
+        default: triangle_task_fast<PRED_ONE, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i, reuse_bc, abox); break;
     }
 }
 
 #ifndef TRI_MIN_BLOCKS
 #define TRI_MIN_BLOCKS 4
 #endif
+// Persistent over groups of tasks: group g is tasks [groups[g], groups[g+1]),
+// which share the job, tile B and tile C; gbox[6 g ..] is the box (lo, hi) of
+// all their A tiles.
 template <bool THETA_FULL, bool JBJ>
 __global__ void __launch_bounds__(TRI_THREADS, TRI_MIN_BLOCKS)
-triangle_fast_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ tasks, unsigned int ntasks,
-                     unsigned int* task_counter, TriParams p, RecheckQueue q, int copies) {
+triangle_fast_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ tasks, const uint32_t* __restrict__ groups,
+                     const float* __restrict__ gbox, unsigned int ngroups, unsigned int* group_counter, TriParams p,
+                     RecheckQueue q, int copies) {
     extern __shared__ __align__(16) unsigned char smem[];
     float4* P = reinterpret_cast<float4*>(smem);
     int2* JK = reinterpret_cast<int2*>(smem + 3 * TILE * sizeof(float4));
@@ -911,33 +936,40 @@ triangle_fast_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ 
     uint32_t* Q = reinterpret_cast<uint32_t*>(IK + TRI_WARPS * TILE);
     unsigned long long* JM = reinterpret_cast<unsigned long long*>(Q + TRI_WARPS * TRI_QCAP);
     unsigned int* H = reinterpret_cast<unsigned int*>(JM + JM_WORDS * TILE);
-    __shared__ uint4 s_task;
+    __shared__ unsigned int s_group;
     __shared__ int s_next_i;
     __shared__ float s_box[6 * 6];  // tile bounding boxes: 6 half-tiles x {lo, hi}
+    __shared__ float s_abox[6];
     for (int b = threadIdx.x; b < copies * p.len; b += blockDim.x) H[b] = 0;
     unsigned int* Hw = H + ((threadIdx.x >> 5) % copies) * p.len;
     int cur = -1;
     unsigned int since = 0;
-    unsigned long long ev = 0, bn = 0;
+    __shared__ unsigned long long ev, bn;  // triangles walked and binned by this CTA
+    if (threadIdx.x == 0) ev = bn = 0;
     for (;;) {
         __syncthreads();
-        if (threadIdx.x == 0) {
-            unsigned int t = atomicAdd(task_counter, 1u);
-            s_task = t < ntasks ? tasks[t] : make_uint4(TASK_NONE, 0, 0, 0);
-        }
+        if (threadIdx.x == 0) s_group = atomicAdd(group_counter, 1u);
         __syncthreads();
-        const uint4 task = s_task;
-        const int slot = task.x == TASK_NONE ? -1 : (int)(task.x & TASK_SLOT_MASK);
-        if ((slot != cur || since >= FLUSH_EVERY) && cur >= 0) {
-            flush_hist(H, copies, p.len, jobs[cur].hist);
-            since = 0;
+        const unsigned int gi = s_group;
+        if (gi >= ngroups) break;
+        if (threadIdx.x < 6) s_abox[threadIdx.x] = gbox[6 * (size_t)gi + threadIdx.x];
+        const uint32_t t0 = groups[gi], t1 = groups[gi + 1];
+        for (uint32_t t = t0; t < t1; t++) {
+            const uint4 task = tasks[t];
+            const int slot = (int)(task.x & TASK_SLOT_MASK);
+            if ((slot != cur || since >= FLUSH_EVERY) && cur >= 0) {
+                flush_hist(H, copies, p.len, jobs[cur].hist);
+                since = 0;
+            }
+            cur = slot;
+            since++;
+            triangle_dispatch<THETA_FULL, JBJ>(jobs[slot], task, p, P, JK, IJ, IK, Q, JM, s_box, Hw, q, ev, bn,
+                                               &s_next_i, t > t0, s_abox);
         }
-        cur = slot;
-        if (slot < 0) break;
-        since++;
-        triangle_dispatch<THETA_FULL, JBJ>(jobs[slot], task, p, P, JK, IJ, IK, Q, JM, s_box, Hw, q, ev, bn, &s_next_i);
     }
-    if ((threadIdx.x & 31) == 0) {
+    if (cur >= 0) flush_hist(H, copies, p.len, jobs[cur].hist);
+    __syncthreads();
+    if (threadIdx.x == 0) {
         if (ev) atomicAdd(q.evaluated, ev);
         if (bn) atomicAdd(q.evaluated + 1, bn);
     }
@@ -1840,19 +1872,19 @@ cudaError_t prepare_kernels(int device) {
     return cudaSuccess;
 }
 
-cudaError_t launch_triangle_fast(const DevJob* jobs, const uint4* tasks, unsigned int ntasks,
-                                 unsigned int* task_counter, const TriParams& p, RecheckQueue q, int grid,
-                                 int copies, int jbj, cudaStream_t st) {
+cudaError_t launch_triangle_fast(const DevJob* jobs, const uint4* tasks, const uint32_t* groups, const float* gbox,
+                                 unsigned int ngroups, unsigned int* group_counter, const TriParams& p, RecheckQueue q,
+                                 int grid, int copies, int jbj, cudaStream_t st) {
     size_t smem = triangle_smem_bytes(p.len, copies);
     if (jbj)
-        triangle_fast_kernel<false, true><<<grid, TRI_THREADS, smem, st>>>(jobs, tasks, ntasks, task_counter, p, q,
-                                                                           copies);
+        triangle_fast_kernel<false, true><<<grid, TRI_THREADS, smem, st>>>(jobs, tasks, groups, gbox, ngroups,
+                                                                           group_counter, p, q, copies);
     else if (p.theta_full)
-        triangle_fast_kernel<true, false><<<grid, TRI_THREADS, smem, st>>>(jobs, tasks, ntasks, task_counter, p, q,
-                                                                           copies);
+        triangle_fast_kernel<true, false><<<grid, TRI_THREADS, smem, st>>>(jobs, tasks, groups, gbox, ngroups,
+                                                                           group_counter, p, q, copies);
     else
-        triangle_fast_kernel<false, false><<<grid, TRI_THREADS, smem, st>>>(jobs, tasks, ntasks, task_counter, p, q,
-                                                                            copies);
+        triangle_fast_kernel<false, false><<<grid, TRI_THREADS, smem, st>>>(jobs, tasks, groups, gbox, ngroups,
+                                                                            group_counter, p, q, copies);
     return cudaGetLastError();
 }
 

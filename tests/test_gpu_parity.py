@@ -563,3 +563,35 @@ def test_counts_do_not_depend_on_tile_size(monkeypatch, tile_points):
     for hw, hg in zip(want, got):
         assert np.array_equal(hw, hg)
         assert hw.sum() > 0
+
+
+_GROUP_WANT = {}
+
+
+@pytest.mark.parametrize("group_tasks", ["1", "3", "64"])
+def test_counts_do_not_depend_on_task_groups(monkeypatch, group_tasks):
+    """The fast triangle kernel takes groups of tasks that share tiles B and C
+    (one j-k table per group, rows skipped from the union box of the group's
+    A tiles): any group size gives the oracle's histograms, TP and JBJ."""
+    monkeypatch.setenv("TPCF_GROUP_TASKS", group_tasks)
+    d = synth.blobs(900, n_blobs=3, sigma=5.0, box=50.0, seed=81)
+    r = synth.uniform(800, box=60.0, seed=82)
+    tp = ((8, 2.0, 10.0), (8, 1.0, 3.0), (16, 0.0, 1.0))
+    jbj = ((8, 2.0, 10.0), (8, 0.2, 1.0), (10, 0.0, 1.0))
+    combos = [([d, d, d], 0), ([d, d, r], 1), ([d, r, r], 1), ([r, r, r], 0)]
+    if not _GROUP_WANT:
+        for (cats, w) in combos:
+            _GROUP_WANT[("tp", w, len(cats[1]), len(cats[2]))] = \
+                oracle.triangle(cats, w, tp, nan_zero=NATIVE_NAN == tpcf.NAN_ZERO)[0]
+            _GROUP_WANT[("jbj", w, len(cats[1]), len(cats[2]))] = oracle.triangle_jbj(cats, w, jbj)[0]
+    with tpcf.Engine(0) as e:
+        hd, hr = e.catalog(d), e.catalog(r)
+        hmap = {id(d): hd, id(r): hr}
+        jobs = [e.job([hmap[id(c)] for c in cats]) for cats, _ in combos]
+        for name, kind, spec in (("tp", tpcf.TRIANGLE, tp), ("jbj", tpcf.TRIANGLE_JBJ, jbj)):
+            specs = [tpcf.make_spec(kind, _loop_of(w), spec, nan_policy=NATIVE_NAN) for _, w in combos]
+            got = e.count_batch(specs, jobs)
+            for (cats, w), g in zip(combos, got):
+                want = _GROUP_WANT[(name, w, len(cats[1]), len(cats[2]))]
+                assert want.sum() > 0
+                assert np.array_equal(g, want), (name, w)
