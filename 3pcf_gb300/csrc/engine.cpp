@@ -449,6 +449,15 @@ struct Binning {
     double lmin_pair = 0;     // pairs: no counted pair has d < lmin_pair
 };
 
+// Whether a job of this spec runs in the guarded FP32 kernels.  The fast
+// triangle kernel keeps side words of 16 bits (s-bin below 255): binnings with
+// more s bins are counted by the plain FP64 kernel, with the same histograms.
+bool guarded_fp32(const tpcf_spec& sp, const Binning& bin) {
+    if (sp.precision != TPCF_GUARDED_FP32) return false;
+    if (sp.kind == TPCF_TRIANGLE || sp.kind == TPCF_TRIANGLE_JBJ) return bin.tri.S <= MAX_FAST_S;
+    return true;
+}
+
 float ref_bw(float lo, float hi, int n) {
     // (hist_max - hist_min)/nbins in float, as distance_to_bin computes it
     volatile float d = hi - lo;
@@ -1546,7 +1555,7 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
         units += pj[g].loop_units;
         pj[g].swap = 0;
         if (rdd && (jsp.kind == TPCF_TRIANGLE || jsp.kind == TPCF_TRIANGLE_JBJ) &&
-            jsp.precision == TPCF_GUARDED_FP32 && jsp.loop == TPCF_LOOP_ONE) {
+            guarded_fp32(jsp, bin) && jsp.loop == TPCF_LOOP_ONE) {
             if (pj[g].v[0] == pj[g].v[1] && pj[g].v[1] != pj[g].v[2]) pj[g].swap = 1;
             else if (pj[g].v[1] == pj[g].v[2] && pj[g].v[0] != pj[g].v[1]) pj[g].swap = 2;
         }
@@ -1624,8 +1633,7 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
             });
         }
         phase("tables");
-        const bool fast_tri = (sp.kind == TPCF_TRIANGLE || sp.kind == TPCF_TRIANGLE_JBJ) &&
-                              sp.precision == TPCF_GUARDED_FP32;
+        const bool fast_tri = (sp.kind == TPCF_TRIANGLE || sp.kind == TPCF_TRIANGLE_JBJ) && guarded_fp32(sp, bin);
         std::vector<std::array<int, 3>> items;  // job, A-tile begin, end
         for (size_t g = 0; g < group.size(); g++) {
             const int na = pj[g].role(0)->ntiles, step = pairs ? 16 : 2;
@@ -1735,7 +1743,7 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
         }
         fprintf(stderr, "%s\n", line.c_str());
     }
-    const bool fp64 = sp.precision != TPCF_GUARDED_FP32;
+    const bool fp64 = !guarded_fp32(sp, bin);
     const bool fast_jbj = sp.kind == TPCF_TRIANGLE_JBJ && !fp64;  // the fast kernel's JBJ binning
     if (sp.kind == TPCF_TRIANGLE) ensure_acos(ctx);
     const AcosTable acos_t = sp.kind == TPCF_TRIANGLE ? acos_table(ctx) : AcosTable{};
@@ -2220,7 +2228,7 @@ tpcf_status tpcf_create(tpcf_ctx** out, int32_t device) {
         const char* hc = getenv("TPCF_HEAVY_COST");
         if (hc) ctx->heavy_cost = atof(hc);
         if (const char* tr = getenv("TPCF_SERVING_TRACE")) ctx->trace_path = tr;
-        if (const char* gt = getenv("TPCF_GROUP_TASKS")) ctx->group_tasks = std::max(1, atoi(gt));
+        if (const char* gt = getenv("TPCF_GROUP_TASKS")) ctx->group_tasks = std::min(MAX_GROUP_TASKS, std::max(1, atoi(gt)));
         const char* shv = getenv("TPCF_SLICE_HEAVY");
         if (shv) ctx->slice_heavy = shv[0] != '0';
         const char* stk = getenv("TPCF_SLICE_TASKS");

@@ -47,7 +47,18 @@ constexpr int CODE_ZERO = -(1 << 23);   // side length exactly 0
 constexpr int CODE_BELOW = -(1 << 22);  // 0 < side < s_lo
 constexpr int CODE_ABOVE = (1 << 22);   // side >= s_hi
 constexpr int CW_IN = 0, CW_ABOVE = 1, CW_BELOW = 4, CW_REJECT = 32;
-constexpr int MAX_TRI_BINS = (1 << 22) - 1;  // S*Q*T limit of the fast kernel encodings
+constexpr int MAX_TRI_BINS = (1 << 22) - 1;  // S*Q*T limit of the triangle kernel encodings
+// The fast (guarded FP32) kernel's side words fit 16 bits, so that its j-k
+// table holds them in two bytes: word = code16 * 128 + class_weight with
+// code16 the side's s-bin itself (the kernel multiplies by Q*T) and the
+// special codes below, in the same order as above.  It takes binnings of at
+// most MAX_FAST_S s bins (b == S, rounding at the top edge, stays below
+// CODE16_ABOVE).
+constexpr int CODE16_ZERO = -2, CODE16_BELOW = -1, CODE16_ABOVE = 255;
+constexpr int MAX_FAST_S = 254;
+// most tasks in one group of the fast triangle kernel (its shared histogram is
+// flushed between groups, at most every 256 tasks)
+constexpr int MAX_GROUP_TASKS = 64;
 // weight sum (4*nBelow + nAbove, >= 32 if rejected) -> permutation validity
 constexpr unsigned VALID_ANY = 0x37u;   // shortest or middle side in range
 constexpr unsigned VALID_02 = 0x07u;    // shortest side in range (permutations 0 and 2)

@@ -282,9 +282,21 @@ struct JMasks {
     unsigned long long kge;
 };
 constexpr int JM_WORDS = 5;
-constexpr size_t TRI_SMEM_FIXED = 3 * TILE * sizeof(float4) + TILE * TILE * sizeof(int2) +
-                                  2 * TRI_WARPS * TILE * sizeof(int2) + TRI_WARPS * TRI_QCAP * sizeof(uint32_t) +
-                                  JM_WORDS * TILE * sizeof(unsigned long long);
+// A tiles resident at once: the tasks of a group (one job, tiles B and C
+// shared) are counted up to four at a time, their points i handed out to the
+// warps together
+constexpr int TRI_GROUP_A = 4;
+// layout: tiles B, C and up to TRI_GROUP_A A tiles | j-class masks | per-warp
+// i-j and i-k rows | j-k sides | per-warp candidate queues | j-k side words
+// (16 bits) | histogram copies
+constexpr size_t TRI_SMEM_FIXED = (2 + TRI_GROUP_A) * TILE * sizeof(float4) +
+                                  JM_WORDS * TILE * sizeof(unsigned long long) + 2 * TRI_WARPS * TILE * sizeof(int2) +
+                                  TILE * TILE * sizeof(float) + TRI_WARPS * TRI_QCAP * sizeof(uint32_t) +
+                                  TILE * TILE * sizeof(short);
+// (the plain FP64 kernel's layout -- three tiles, a j-k table of int2 and one
+// row per warp -- fits the same allocation)
+static_assert(TRI_SMEM_FIXED >= 3 * TILE * sizeof(float4) + TILE * TILE * sizeof(int2) + TRI_WARPS * TILE * sizeof(int2),
+              "FP64 triangle layout");
 
 // s-bin code of one side, monotone in the side length, multiplied by Q*T
 // (used by the plain FP64 kernel).
@@ -297,25 +309,25 @@ __device__ __forceinline__ int tri_side_code(float d, const TriParams& p) {
     return __float2int_rz(F::div(F::sub(d, p.s_lo), p.s_bw)) * (p.Q * p.T);
 }
 
-// Side word of the fast kernel: code * 128 + class weight (see engine.h).
+// Side word of the fast kernel: code16 * 128 + class weight, 16 bits (see
+// engine.h); code16 is the s-bin itself.
 // (A division-free s-bin -- a guess corrected against exact thresholds
 // staged in shared memory -- measured slower: 14.19 vs 13.95 ms on the
 // default workload.)
 __device__ __forceinline__ int tri_side_word(float d, const TriParams& p) {
     int code, w;
     if (d == 0.f) {
-        code = CODE_ZERO;
+        code = CODE16_ZERO;
         w = CW_REJECT;
     } else if (d < p.s_lo) {
-        code = CODE_BELOW;
+        code = CODE16_BELOW;
         w = CW_BELOW;
     } else if (d >= p.s_hi) {
-        code = CODE_ABOVE;
+        code = CODE16_ABOVE;
         w = CW_ABOVE;
     } else {
-        int b = __float2int_rz(__fdiv_rn(__fsub_rn(d, p.s_lo), p.s_bw));
-        code = b * (p.Q * p.T);
-        w = b < p.S ? CW_IN : CW_ABOVE;  // b == S: rounding at the top edge, index past the array
+        code = __float2int_rz(__fdiv_rn(__fsub_rn(d, p.s_lo), p.s_bw));
+        w = code < p.S ? CW_IN : CW_ABOVE;  // code == S: rounding at the top edge, index past the array
     }
     if (d >= p.lmax) w = CW_REJECT;
     return code * 128 + w;
@@ -458,8 +470,9 @@ __device__ __forceinline__ void triangle_full2(const float (&a)[2], const int (&
         l[t] = fmaxf(hi_ab, c[t]);
         m[t] = fmaxf(lo_ab, fminf(hi_ab, c[t]));
         const int wlo = min(wa[t], wb[t]), whi = max(wa[t], wb[t]);
-        off_s[t] = min(wlo, wc[t]) >> 7;
-        off_m[t] = max(wlo, min(whi, wc[t])) >> 7;
+        // s-bins of the shortest and the middle side, times Q
+        off_s[t] = (min(wlo, wc[t]) >> 7) * p.Q;
+        off_m[t] = (max(wlo, min(whi, wc[t])) >> 7) * p.Q;
     }
     const f32x2 S = pk2(s[0], s[1]), M = pk2(m[0], m[1]), L = pk2(l[0], l[1]);
     // the squares enter the cosine numerators as the reference rounds them:
@@ -512,9 +525,9 @@ __device__ __forceinline__ void triangle_full2(const float (&a)[2], const int (&
             ok1 = ok1 && (unsigned)t1b[t] < (unsigned)p.T;
             ok2 = ok2 && (unsigned)t2b[t] < (unsigned)p.T;
         }
-        if (ok0) atomicAdd(Hw + off_s[t] + q0b[t] * p.T + t0b[t], w[t]);
-        if (ok1) atomicAdd(Hw + off_m[t] + q1b[t] * p.T + t1b[t], w[t]);
-        if (ok2) atomicAdd(Hw + off_s[t] + q2b[t] * p.T + t2b[t], w[t]);
+        if (ok0) atomicAdd(Hw + (off_s[t] + q0b[t]) * p.T + t0b[t], w[t]);
+        if (ok1) atomicAdd(Hw + (off_m[t] + q1b[t]) * p.T + t1b[t], w[t]);
+        if (ok2) atomicAdd(Hw + (off_s[t] + q2b[t]) * p.T + t2b[t], w[t]);
         guard[t] = g;
     }
 }
@@ -544,10 +557,10 @@ __device__ __forceinline__ void jbj_full2(const float (&a)[2], const int (&wa)[2
         const bool v = w[t] && mask_bit(VALID_02, idx);
         const float lo_ab = fminf(a[t], b[t]), hi_ab = fmaxf(a[t], b[t]);
         const float s = fminf(lo_ab, c[t]), l = fmaxf(hi_ab, c[t]), m = fmaxf(lo_ab, fminf(hi_ab, c[t]));
-        const int code = min(min(wa[t], wb[t]), wc[t]) >> 7;
+        const int code = min(min(wa[t], wb[t]), wc[t]) >> 7;  // s-bin of the shortest side
         const int i1 = jbj_axis_bin(__fdiv_rn(s, m), p.q_lo, p.q_hi, p.q_bw);
         const int i2 = jbj_axis_bin(__fdiv_rn(__fsub_rn(l, m), s), p.t_lo, p.t_hi, p.t_bw);
-        const int x = code + i1 * p.T + i2;
+        const int x = (code * p.Q + i1) * p.T + i2;
         if (v && i1 >= 0 && i2 >= 0 && x < p.len) atomicAdd(Hw + x, w[t]);
     }
 }
@@ -591,19 +604,20 @@ __device__ __forceinline__ int pkey(float4 p) { return __float_as_int(p.w); }
 // (packed into the f32x2 instructions of one binning path).
 template <bool THETA_FULL, bool JBJ>
 __device__ __forceinline__ void run_candidates(const uint32_t* cand, int n, const int2* row_ij, const int2* row_ik,
-                                               const int2* JK, const TriParams& p, unsigned int* Hw, RecheckQueue& q,
-                                               uint32_t slot, uint32_t ia, int b0, int c0) {
+                                               const float* JKd, const short* JKw, const TriParams& p, unsigned int* Hw,
+                                               RecheckQueue& q, uint32_t slot, uint32_t ia, int b0, int c0) {
     const int lane = threadIdx.x & 31;
     const uint32_t e0 = lane < n ? cand[lane] : 0u;
     const uint32_t e1 = lane + 32 < n ? cand[lane + 32] : 0u;
     const int j0 = e0 & 63, k0 = (e0 >> 6) & 63, j1 = e1 & 63, k1 = (e1 >> 6) & 63;
     const unsigned w0 = e0 >> 12, w1 = e1 >> 12;
-    const int2 ij0 = row_ij[j0], ik0 = row_ik[k0], jk0 = JK[j0 * TILE + k0];
-    const int2 ij1 = row_ij[j1], ik1 = row_ik[k1], jk1 = JK[j1 * TILE + k1];
+    const int2 ij0 = row_ij[j0], ik0 = row_ik[k0];
+    const int2 ij1 = row_ij[j1], ik1 = row_ik[k1];
     const float fa[2] = {__int_as_float(ij0.x), __int_as_float(ij1.x)};
     const float fb[2] = {__int_as_float(ik0.x), __int_as_float(ik1.x)};
-    const float fc[2] = {__int_as_float(jk0.x), __int_as_float(jk1.x)};
-    const int wa[2] = {ij0.y, ij1.y}, wb[2] = {ik0.y, ik1.y}, wc[2] = {jk0.y, jk1.y};
+    const float fc[2] = {JKd[j0 * TILE + k0], JKd[j1 * TILE + k1]};
+    const int wa[2] = {ij0.y, ij1.y}, wb[2] = {ik0.y, ik1.y};
+    const int wc[2] = {JKw[j0 * TILE + k0], JKw[j1 * TILE + k1]};
     const unsigned ww[2] = {w0, w1};
     if (JBJ) {
         jbj_full2(fa, wa, fb, wb, fc, wc, ww, p, Hw);
@@ -658,241 +672,271 @@ __device__ __forceinline__ unsigned long long candidate_mask_jbj(int cij, unsign
 }
 
 template <int PRED, bool THETA_FULL, bool JBJ>
-__device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams& p, float4* P, int2* JK,
-                                   int2* IJ, int2* IK, uint32_t* Q, unsigned long long* JM, float* BX,
-                                   unsigned int* Hw, RecheckQueue& q, unsigned long long& evaluated,
-                                   unsigned long long& binned, int* next_i, bool reuse_bc, const float* abox) {
+__device__ void triangle_group_fast(const DevJob& J, const uint4* __restrict__ gt, int nt, const TriParams& p,
+                                    float4* P, float* JKd, short* JKw, int2* IJ, int2* IK, uint32_t* Q,
+                                    unsigned long long* JM, float* BX, int4* s_meta, unsigned int* Hw,
+                                    RecheckQueue& q, unsigned long long& evaluated, unsigned long long& binned,
+                                    int* next_i, const float* abox) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const TaskGeom g = task_geom(J, task);
-    const uint32_t slot = task.x & TASK_SLOT_MASK;
-    const bool diag_ij = task.x & TASK_DIAG_IJ, diag_jk = task.x & TASK_DIAG_JK;
-    // the tasks of a group share tiles B and C: the first loads all three
-    // tiles and builds the j-k table, the others load tile A only
-    if (reuse_bc) {
-        __syncthreads();  // the previous task's i loop is done with tile A
-        for (int t = threadIdx.x; t < TILE; t += blockDim.x)
-            P[t] = t < g.nA ? J.pts[0][g.a0 + t] : make_float4(0.f, 0.f, 0.f, 0.f);
-    } else {
-        load_points(P, J, g);
-    }
-    if (threadIdx.x == 0) *next_i = 0;
-    __syncthreads();
-    // bounding boxes of tiles B and C (two 32-point halves each), for the
-    // points of A out of reach of a whole tile
-    const bool chk_b = task.x & TASK_CHECK_B, chk_c = task.x & TASK_CHECK_C;
-    if (!reuse_bc && warp >= 2 && warp < 6) {
-        const int role = warp >> 1, idx = (warp & 1) * 32 + lane;
-        const int n = role == 0 ? g.nA : (role == 1 ? g.nB : g.nC);
-        const float4 pt = P[role * TILE + idx];
-        const bool valid = idx < n;
-        float lo[3] = {valid ? pt.x : INFINITY, valid ? pt.y : INFINITY, valid ? pt.z : INFINITY};
-        float hi[3] = {valid ? pt.x : -INFINITY, valid ? pt.y : -INFINITY, valid ? pt.z : -INFINITY};
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
-#pragma unroll
-            for (int a = 0; a < 3; a++) {
-                lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
-                hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
-            }
-        if (lane == 0) {
-#pragma unroll
-            for (int a = 0; a < 3; a++) {
-                BX[warp * 6 + a] = lo[a];
-                BX[warp * 6 + 3 + a] = hi[a];
-            }
-        }
-    }
-    if (!reuse_bc) __syncthreads();
+    float4 *PB = P, *PC = P + TILE, *PA = P + 2 * TILE;
+    // every task of the group has the same job and tiles B and C
+    const uint4 t0 = gt[0];
+    const uint32_t slot = t0.x & TASK_SLOT_MASK;
+    const bool diag_jk = t0.x & TASK_DIAG_JK;
+    const int tb0 = J.tile_start[1][t0.z], numB = J.tile_start[1][t0.z + 1] - tb0;  // first point, points of B
+    const int tc0 = J.tile_start[2][t0.w], numC = J.tile_start[2][t0.w + 1] - tc0;  // ... of C
     // a side that provably reaches lmax is rejected whatever its exact value:
     // points farther than that from a whole tile take no part in the task
     // (the 1e-5 margin covers the rounding of the bound and of the distance)
     const float reach = p.lmax * (1.0f + 1e-5f);
     const float reach2 = reach * reach;
     auto far_from = [&](float4 pt, int role) -> bool {
-        const float* b0 = BX + role * 12;
+        const float* bx = BX + role * 12;
         float s2 = 0.f;
         {
-            const float lo = fminf(b0[0], b0[6]), hi = fmaxf(b0[3], b0[9]);
+            const float lo = fminf(bx[0], bx[6]), hi = fmaxf(bx[3], bx[9]);
             const float gap = fmaxf(0.f, fmaxf(lo - pt.x, pt.x - hi));
             s2 = fmaf(gap, gap, s2);
         }
         {
-            const float lo = fminf(b0[1], b0[7]), hi = fmaxf(b0[4], b0[10]);
+            const float lo = fminf(bx[1], bx[7]), hi = fmaxf(bx[4], bx[10]);
             const float gap = fmaxf(0.f, fmaxf(lo - pt.y, pt.y - hi));
             s2 = fmaf(gap, gap, s2);
         }
         {
-            const float lo = fminf(b0[2], b0[8]), hi = fmaxf(b0[5], b0[11]);
+            const float lo = fminf(bx[2], bx[8]), hi = fmaxf(bx[5], bx[11]);
             const float gap = fmaxf(0.f, fmaxf(lo - pt.z, pt.z - hi));
             s2 = fmaf(gap, gap, s2);
         }
         return s2 >= reach2;
     };
-    // rows j of the j-k side table and their class masks, one warp per row
-    // (once per group of tasks); abox: the box of every A tile of the group
-    const int key_k0 = pkey(P[2 * TILE + lane]), key_k1 = pkey(P[2 * TILE + lane + 32]);
-    for (int j = reuse_bc ? g.nB : warp; j < g.nB; j += TRI_WARPS) {
-        const float4 pj = P[TILE + j];
-        float a2 = 0.f;
-#pragma unroll
-        for (int a = 0; a < 3; a++) {
-            const float v = a == 0 ? pj.x : (a == 1 ? pj.y : pj.z);
-            const float gap = fmaxf(0.f, fmaxf(abox[a] - v, v - abox[3 + a]));
-            a2 = fmaf(gap, gap, a2);
-        }
-        if (a2 >= reach2) {  // no i of the group reaches j: empty masks, the row is never read
-            if (lane < JM_WORDS) JM[lane * TILE + j] = 0ull;
-            continue;
-        }
-        int c0 = 0, c1 = 0;
-        if (lane < g.nC) {
-            float d = ref_dist<false>(pj, P[2 * TILE + lane]);
-            int w = tri_side_word(d, p);
-            JK[j * TILE + lane] = make_int2(__float_as_int(d), w);
-            c0 = side_class(w, d, p);
-        }
-        if (lane + 32 < g.nC) {
-            float d = ref_dist<false>(pj, P[2 * TILE + lane + 32]);
-            int w = tri_side_word(d, p);
-            JK[j * TILE + lane + 32] = make_int2(__float_as_int(d), w);
-            c1 = side_class(w, d, p);
-        }
-        JMasks m;
-#pragma unroll
-        for (int c = 0; c < 4; c++) m.c[c] = ballot64(c0 == c + 1, c1 == c + 1);
-        const int kj = pkey(pj);
-        m.kge = ballot64(lane < g.nC && key_k0 >= kj, lane + 32 < g.nC && key_k1 >= kj);
-        if (lane == 0) {
-#pragma unroll
-            for (int c = 0; c < 4; c++) JM[c * TILE + j] = m.c[c];
-            JM[4 * TILE + j] = m.kge;
-        }
-    }
-    __syncthreads();
     int2* row_ij = IJ + warp * TILE;
     int2* row_ik = IK + warp * TILE;
     uint32_t* cand = Q + warp * TRI_QCAP;
+    int key_k0 = 0, key_k1 = 0;
     unsigned ev = 0, bn = 0;
-    for (;;) {
-        // points of role A are handed out to warps dynamically (balances the
-        // very uneven work per point)
-        int i = 0;
-        if (lane == 0) i = atomicAdd(next_i, 1);
-        i = __shfl_sync(0xffffffffu, i, 0);
-        if (i >= g.nA) break;
-        const float4 pi = P[i];
-        if ((chk_b && far_from(pi, 1)) || (chk_c && far_from(pi, 2))) continue;
-        const int ki = pkey(pi);
-        // i-k sides: words for the binning path, class masks for the filter
-        int c0 = 0, c1 = 0;
-        if (lane < g.nC) {
-            float d = ref_dist<false>(pi, P[2 * TILE + lane]);
-            int w = tri_side_word(d, p);
-            row_ik[lane] = make_int2(__float_as_int(d), w);
-            c0 = side_class(w, d, p);
-        }
-        if (lane + 32 < g.nC) {
-            float d = ref_dist<false>(pi, P[2 * TILE + lane + 32]);
-            int w = tri_side_word(d, p);
-            row_ik[lane + 32] = make_int2(__float_as_int(d), w);
-            c1 = side_class(w, d, p);
-        }
-        const unsigned long long nB = ballot64(c0 == 1, c1 == 1), nI = ballot64(c0 == 2, c1 == 2);
-        const unsigned long long nM = ballot64(c0 == 3, c1 == 3), nH = ballot64(c0 == 4, c1 == 4);
-        const unsigned long long any_k = nB | nI | nM | nH;
-        if (!any_k) continue;  // no k within reach of i (warp-uniform)
-        unsigned long long kge_i = 0;  // PRED_DDR: key_k >= key_i; PRED_RDD: key_k <= key_i
-        if (PRED == PRED_DDR) kge_i = ballot64(lane < g.nC && key_k0 >= ki, lane + 32 < g.nC && key_k1 >= ki);
-        if (PRED == PRED_RDD) kge_i = ballot64(lane < g.nC && key_k0 <= ki, lane + 32 < g.nC && key_k1 <= ki);
-        // i-j sides: words for the binning path; each lane then forms the
-        // candidate-k mask of its own two j's (the scan over j is lane-parallel)
-        // mask of candidate k's (and of weight-2 k's) of the pair (i, j)
-        auto scan_j = [&](int j, unsigned long long& cm, unsigned long long& w2) -> bool {
-            cm = 0;
-            w2 = 0;
-            if (j >= g.nB) return false;
-            float d = ref_dist<false>(pi, P[TILE + j]);
-            int w = tri_side_word(d, p);
-            row_ij[j] = make_int2(__float_as_int(d), w);
-            const int c = side_class(w, d, p);
-            bool ok = c != 0 && any_k && (!diag_ij || j > i);
-            if (PRED == PRED_SAME) ok = ok && ki <= pkey(P[TILE + j]);
-            if (!ok) return false;
-            cm = JBJ ? candidate_mask_jbj(c, nI, nM, nH, JM[TILE + j], JM[2 * TILE + j], JM[3 * TILE + j])
-                     : candidate_mask(c, nB, nI, nM, nH, JM[j], JM[TILE + j], JM[2 * TILE + j], JM[3 * TILE + j]);
-            if (diag_jk) cm &= j >= 63 ? 0ull : (~0ull << (j + 1));
-            if (PRED == PRED_RDD) {
-                // weight [key_j <= key_i] + [key_k <= key_i]
-                if (pkey(P[TILE + j]) <= ki) {
-                    w2 = cm & kge_i;
-                } else {
-                    cm &= kge_i;
-                }
-            } else if (PRED != PRED_NONE) {
-                const unsigned long long kge_j = JM[4 * TILE + j];
-                if (PRED == PRED_DDR) {
-                    w2 = cm & kge_i & kge_j;  // weight 2: k >= i and k >= j
-                    cm &= kge_i | kge_j;      // weight 0 otherwise
-                } else {
-                    cm &= kge_j;              // key_j <= key_k
-                }
+    for (int ch = 0; ch < nt; ch += TRI_GROUP_A) {
+        const int nr = min(TRI_GROUP_A, nt - ch);
+        if (ch > 0) __syncthreads();  // the previous chunk's i loops are done with its A tiles
+        // tiles B and C (first chunk) and the chunk's A tiles; A tile r of
+        // the chunk at PA + r * TILE
+        for (int tt = (ch == 0 ? 0 : 2 * TILE) + threadIdx.x; tt < (2 + nr) * TILE; tt += blockDim.x) {
+            const int idx = tt % TILE;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (tt < TILE) {
+                if (idx < numB) v = J.pts[1][tb0 + idx];
+            } else if (tt < 2 * TILE) {
+                if (idx < numC) v = J.pts[2][tc0 + idx];
+            } else {
+                const uint32_t at = gt[ch + tt / TILE - 2].y;
+                const int a0 = J.tile_start[0][at];
+                if (idx < J.tile_start[0][at + 1] - a0) v = J.pts[0][a0 + idx];
             }
-            return true;
-        };
-        unsigned long long cm0, w20, cm1, w21;
-        const bool ok0 = scan_j(lane, cm0, w20);
-        const bool ok1 = scan_j(lane + 32, cm1, w21);
-        // walked (i, j, k): every k with a usable i-k side, for every usable j
-        ev += (unsigned)__popcll(any_k) *
-              (unsigned)(__popc(__ballot_sync(0xffffffffu, ok0)) + __popc(__ballot_sync(0xffffffffu, ok1)));
-        __syncwarp();
-        const uint32_t ia = (uint32_t)(g.a0 + i);
-        // Candidates of this i: every j with a non-empty mask in turn, expanded
-        // by the whole warp (lanes over k), queued and binned 64 at a time.
-        // (A lane-parallel compaction of the j's with few candidates, through
-        // a prefix sum of per-lane counts, measured slower on clustered data:
-        // its scattered j/k break the conflict-free table reads of binning.)
-        const unsigned lbit = 1u << lane, lt = lbit - 1u;
-        // queue entries of this lane's k = lane and k = lane + 32 (weight 1;
-        // plus j and the weight bit of two-array jobs)
-        const uint32_t klo = ((uint32_t)lane << 6) | (1u << 12), khi = ((uint32_t)(lane + 32) << 6) | (1u << 12);
-        int qn = 0;  // queued candidates (warp-uniform)
+            P[tt] = v;
+        }
+        if (threadIdx.x < nr) {
+            const uint4 t = gt[ch + threadIdx.x];
+            const int a0 = J.tile_start[0][t.y];
+            s_meta[threadIdx.x] = make_int4(a0, J.tile_start[0][t.y + 1] - a0, (int)t.x, 0);
+        }
+        if (threadIdx.x == 0) *next_i = 0;
+        __syncthreads();
+        if (ch == 0) {
+            // bounding boxes of tiles B and C (two 32-point halves each), for
+            // the points of A out of reach of a whole tile
+            if (warp >= 2 && warp < 6) {
+                const int role = warp >> 1, idx = (warp & 1) * 32 + lane;
+                const int n = role == 1 ? numB : numC;
+                const float4 pt = P[(role - 1) * TILE + idx];
+                const bool valid = idx < n;
+                float lo[3] = {valid ? pt.x : INFINITY, valid ? pt.y : INFINITY, valid ? pt.z : INFINITY};
+                float hi[3] = {valid ? pt.x : -INFINITY, valid ? pt.y : -INFINITY, valid ? pt.z : -INFINITY};
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
-            unsigned live = __ballot_sync(0xffffffffu, (h ? cm1 : cm0) != 0ull);
-            const unsigned long long cmv = h ? cm1 : cm0, w2v = h ? w21 : w20;
-            while (live) {
-                const int src = __ffs(live) - 1;
-                live &= live - 1u;
-                const uint32_t j = (uint32_t)(src + 32 * h);
-                const unsigned lo = __shfl_sync(0xffffffffu, (unsigned)cmv, src);
-                const unsigned hi = __shfl_sync(0xffffffffu, (unsigned)(cmv >> 32), src);
-                uint32_t vlo = klo + j, vhi = khi + j;
-                if (PRED == PRED_DDR || PRED == PRED_RDD) {
-                    const unsigned w2lo = __shfl_sync(0xffffffffu, (unsigned)w2v, src);
-                    const unsigned w2hi = __shfl_sync(0xffffffffu, (unsigned)(w2v >> 32), src);
-                    vlo += (w2lo & lbit) ? (1u << 12) : 0u;
-                    vhi += (w2hi & lbit) ? (1u << 12) : 0u;
-                }
-                const int nlo = __popc(lo);
-                if (lo & lbit) cand[qn + __popc(lo & lt)] = vlo;
-                if (hi & lbit) cand[qn + nlo + __popc(hi & lt)] = vhi;
-                qn += nlo + __popc(hi);
-                if (qn >= 64) {
-                    __syncwarp();
-                    qn -= 64;
-                    run_candidates<THETA_FULL, JBJ>(cand + qn, 64, row_ij, row_ik, JK, p, Hw, q, slot, ia, g.b0, g.c0);
-                    bn += 64;
-                    __syncwarp();
+                for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+                    for (int a = 0; a < 3; a++) {
+                        lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+                        hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+                    }
+                if (lane == 0) {
+#pragma unroll
+                    for (int a = 0; a < 3; a++) {
+                        BX[warp * 6 + a] = lo[a];
+                        BX[warp * 6 + 3 + a] = hi[a];
+                    }
                 }
             }
+            key_k0 = pkey(PC[lane]);
+            key_k1 = pkey(PC[lane + 32]);
+            // rows j of the j-k side table and their class masks, one warp per row;
+            // abox: the box of every A tile of the group
+            for (int j = warp; j < numB; j += TRI_WARPS) {
+                const float4 pj = PB[j];
+                float a2 = 0.f;
+#pragma unroll
+                for (int a = 0; a < 3; a++) {
+                    const float v = a == 0 ? pj.x : (a == 1 ? pj.y : pj.z);
+                    const float gap = fmaxf(0.f, fmaxf(abox[a] - v, v - abox[3 + a]));
+                    a2 = fmaf(gap, gap, a2);
+                }
+                if (a2 >= reach2) {  // no i of the group reaches j: empty masks, the row is never read
+                    if (lane < JM_WORDS) JM[lane * TILE + j] = 0ull;
+                    continue;
+                }
+                int c0 = 0, c1 = 0;
+                if (lane < numC) {
+                    float d = ref_dist<false>(pj, PC[lane]);
+                    int w = tri_side_word(d, p);
+                    JKd[j * TILE + lane] = d;
+                    JKw[j * TILE + lane] = (short)w;
+                    c0 = side_class(w, d, p);
+                }
+                if (lane + 32 < numC) {
+                    float d = ref_dist<false>(pj, PC[lane + 32]);
+                    int w = tri_side_word(d, p);
+                    JKd[j * TILE + lane + 32] = d;
+                    JKw[j * TILE + lane + 32] = (short)w;
+                    c1 = side_class(w, d, p);
+                }
+                JMasks m;
+#pragma unroll
+                for (int c = 0; c < 4; c++) m.c[c] = ballot64(c0 == c + 1, c1 == c + 1);
+                const int kj = pkey(pj);
+                m.kge = ballot64(lane < numC && key_k0 >= kj, lane + 32 < numC && key_k1 >= kj);
+                if (lane == 0) {
+#pragma unroll
+                    for (int c = 0; c < 4; c++) JM[c * TILE + j] = m.c[c];
+                    JM[4 * TILE + j] = m.kge;
+                }
+            }
+            __syncthreads();
         }
-        __syncwarp();
-        if (qn > 0) {
-            run_candidates<THETA_FULL, JBJ>(cand, qn, row_ij, row_ik, JK, p, Hw, q, slot, ia, g.b0, g.c0);
-            bn += qn;
+        for (;;) {
+            // points of the chunk's A tiles are handed out to warps
+            // dynamically (balances the very uneven work per point)
+            int ii = 0;
+            if (lane == 0) ii = atomicAdd(next_i, 1);
+            ii = __shfl_sync(0xffffffffu, ii, 0);
+            if (ii >= nr * TILE) break;
+            const int4 meta = s_meta[ii / TILE];  // first point, points, task flags
+            const int i = ii % TILE;
+            if (i >= meta.y) continue;
+            const bool diag_ij = meta.z & TASK_DIAG_IJ;
+            const bool chk_b = meta.z & TASK_CHECK_B, chk_c = meta.z & TASK_CHECK_C;
+            const float4 pi = PA[ii];
+            if ((chk_b && far_from(pi, 1)) || (chk_c && far_from(pi, 2))) continue;
+            const int ki = pkey(pi);
+            // i-k sides: words for the binning path, class masks for the filter
+            int c0 = 0, c1 = 0;
+            if (lane < numC) {
+                float d = ref_dist<false>(pi, PC[lane]);
+                int w = tri_side_word(d, p);
+                row_ik[lane] = make_int2(__float_as_int(d), w);
+                c0 = side_class(w, d, p);
+            }
+            if (lane + 32 < numC) {
+                float d = ref_dist<false>(pi, PC[lane + 32]);
+                int w = tri_side_word(d, p);
+                row_ik[lane + 32] = make_int2(__float_as_int(d), w);
+                c1 = side_class(w, d, p);
+            }
+            const unsigned long long nB = ballot64(c0 == 1, c1 == 1), nI = ballot64(c0 == 2, c1 == 2);
+            const unsigned long long nM = ballot64(c0 == 3, c1 == 3), nH = ballot64(c0 == 4, c1 == 4);
+            const unsigned long long any_k = nB | nI | nM | nH;
+            if (!any_k) continue;  // no k within reach of i (warp-uniform)
+            unsigned long long kge_i = 0;  // PRED_DDR: key_k >= key_i; PRED_RDD: key_k <= key_i
+            if (PRED == PRED_DDR) kge_i = ballot64(lane < numC && key_k0 >= ki, lane + 32 < numC && key_k1 >= ki);
+            if (PRED == PRED_RDD) kge_i = ballot64(lane < numC && key_k0 <= ki, lane + 32 < numC && key_k1 <= ki);
+            // i-j sides: words for the binning path; each lane then forms the
+            // candidate-k mask of its own two j's (the scan over j is lane-parallel)
+            // mask of candidate k's (and of weight-2 k's) of the pair (i, j)
+            auto scan_j = [&](int j, unsigned long long& cm, unsigned long long& w2) -> bool {
+                cm = 0;
+                w2 = 0;
+                if (j >= numB) return false;
+                float d = ref_dist<false>(pi, PB[j]);
+                int w = tri_side_word(d, p);
+                row_ij[j] = make_int2(__float_as_int(d), w);
+                const int c = side_class(w, d, p);
+                bool ok = c != 0 && any_k && (!diag_ij || j > i);
+                if (PRED == PRED_SAME) ok = ok && ki <= pkey(PB[j]);
+                if (!ok) return false;
+                cm = JBJ ? candidate_mask_jbj(c, nI, nM, nH, JM[TILE + j], JM[2 * TILE + j], JM[3 * TILE + j])
+                         : candidate_mask(c, nB, nI, nM, nH, JM[j], JM[TILE + j], JM[2 * TILE + j], JM[3 * TILE + j]);
+                if (diag_jk) cm &= j >= 63 ? 0ull : (~0ull << (j + 1));
+                if (PRED == PRED_RDD) {
+                    // weight [key_j <= key_i] + [key_k <= key_i]
+                    if (pkey(PB[j]) <= ki) {
+                        w2 = cm & kge_i;
+                    } else {
+                        cm &= kge_i;
+                    }
+                } else if (PRED != PRED_NONE) {
+                    const unsigned long long kge_j = JM[4 * TILE + j];
+                    if (PRED == PRED_DDR) {
+                        w2 = cm & kge_i & kge_j;  // weight 2: k >= i and k >= j
+                        cm &= kge_i | kge_j;      // weight 0 otherwise
+                    } else {
+                        cm &= kge_j;              // key_j <= key_k
+                    }
+                }
+                return true;
+            };
+            unsigned long long cm0, w20, cm1, w21;
+            const bool ok0 = scan_j(lane, cm0, w20);
+            const bool ok1 = scan_j(lane + 32, cm1, w21);
+            // walked (i, j, k): every k with a usable i-k side, for every usable j
+            ev += (unsigned)__popcll(any_k) *
+                  (unsigned)(__popc(__ballot_sync(0xffffffffu, ok0)) + __popc(__ballot_sync(0xffffffffu, ok1)));
+            __syncwarp();
+            const uint32_t ia = (uint32_t)(meta.x + i);
+            // Candidates of this i: every j with a non-empty mask in turn, expanded
+            // by the whole warp (lanes over k), queued and binned 64 at a time.
+            // (A lane-parallel compaction of the j's with few candidates, through
+            // a prefix sum of per-lane counts, measured slower on clustered data:
+            // its scattered j/k break the conflict-free table reads of binning.)
+            const unsigned lbit = 1u << lane, lt = lbit - 1u;
+            // queue entries of this lane's k = lane and k = lane + 32 (weight 1;
+            // plus j and the weight bit of two-array jobs)
+            const uint32_t klo = ((uint32_t)lane << 6) | (1u << 12), khi = ((uint32_t)(lane + 32) << 6) | (1u << 12);
+            int qn = 0;  // queued candidates (warp-uniform)
+    #pragma unroll
+            for (int h = 0; h < 2; h++) {
+                unsigned live = __ballot_sync(0xffffffffu, (h ? cm1 : cm0) != 0ull);
+                const unsigned long long cmv = h ? cm1 : cm0, w2v = h ? w21 : w20;
+                while (live) {
+                    const int src = __ffs(live) - 1;
+                    live &= live - 1u;
+                    const uint32_t j = (uint32_t)(src + 32 * h);
+                    const unsigned lo = __shfl_sync(0xffffffffu, (unsigned)cmv, src);
+                    const unsigned hi = __shfl_sync(0xffffffffu, (unsigned)(cmv >> 32), src);
+                    uint32_t vlo = klo + j, vhi = khi + j;
+                    if (PRED == PRED_DDR || PRED == PRED_RDD) {
+                        const unsigned w2lo = __shfl_sync(0xffffffffu, (unsigned)w2v, src);
+                        const unsigned w2hi = __shfl_sync(0xffffffffu, (unsigned)(w2v >> 32), src);
+                        vlo += (w2lo & lbit) ? (1u << 12) : 0u;
+                        vhi += (w2hi & lbit) ? (1u << 12) : 0u;
+                    }
+                    const int nlo = __popc(lo);
+                    if (lo & lbit) cand[qn + __popc(lo & lt)] = vlo;
+                    if (hi & lbit) cand[qn + nlo + __popc(hi & lt)] = vhi;
+                    qn += nlo + __popc(hi);
+                    if (qn >= 64) {
+                        __syncwarp();
+                        qn -= 64;
+                        run_candidates<THETA_FULL, JBJ>(cand + qn, 64, row_ij, row_ik, JKd, JKw, p, Hw, q, slot, ia, tb0, tc0);
+                        bn += 64;
+                        __syncwarp();
+                    }
+                }
+            }
+            __syncwarp();
+            if (qn > 0) {
+                run_candidates<THETA_FULL, JBJ>(cand, qn, row_ij, row_ik, JKd, JKw, p, Hw, q, slot, ia, tb0, tc0);
+                bn += qn;
+            }
+            __syncwarp();
         }
-        __syncwarp();
     }
     // (per-warp totals into the CTA's counters: no 64-bit accumulators live
     // in registers across the kernel)
@@ -903,18 +947,20 @@ __device__ void triangle_task_fast(const DevJob& J, uint4 task, const TriParams&
 }
 
 template <bool THETA_FULL, bool JBJ>
-__device__ __forceinline__ void triangle_dispatch(const DevJob& J, uint4 task, const TriParams& p, float4* P,
-                                                  int2* JK, int2* IJ, int2* IK, uint32_t* Q,
-                                                  unsigned long long* JM, float* BX, unsigned int* Hw, RecheckQueue& q,
-                                                  unsigned long long& ev, unsigned long long& bn, int* next_i,
-                                                  bool reuse_bc, const float* abox) {
-    switch ((task.x >> TASK_PRED_SHIFT) & TASK_PRED_MASK) {
-        case PRED_NONE: triangle_task_fast<PRED_NONE, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i, reuse_bc, abox); break;
-        case PRED_DDR: triangle_task_fast<PRED_DDR, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i, reuse_bc, abox); break;
-        case PRED_RDD: triangle_task_fast<PRED_RDD, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i, reuse_bc, abox); break;
-        case PRED_SAME: triangle_task_fast<PRED_SAME, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i, reuse_bc, abox); break;
-        default: triangle_task_fast<PRED_ONE, THETA_FULL, JBJ>(J, task, p, P, JK, IJ, IK, Q, JM, BX, Hw, q, ev, bn, next_i, reuse_bc, abox); break;
+__device__ __forceinline__ void triangle_dispatch(const DevJob& J, const uint4* gt, int nt, const TriParams& p,
+                                                  float4* P, float* JKd, short* JKw, int2* IJ, int2* IK, uint32_t* Q,
+                                                  unsigned long long* JM, float* BX, int4* s_meta, unsigned int* Hw,
+                                                  RecheckQueue& q, unsigned long long& ev, unsigned long long& bn,
+                                                  int* next_i, const float* abox) {
+#define TRI_GROUP_ARGS J, gt, nt, p, P, JKd, JKw, IJ, IK, Q, JM, BX, s_meta, Hw, q, ev, bn, next_i, abox
+    switch ((gt[0].x >> TASK_PRED_SHIFT) & TASK_PRED_MASK) {
+        case PRED_NONE: triangle_group_fast<PRED_NONE, THETA_FULL, JBJ>(TRI_GROUP_ARGS); break;
+        case PRED_DDR: triangle_group_fast<PRED_DDR, THETA_FULL, JBJ>(TRI_GROUP_ARGS); break;
+        case PRED_RDD: triangle_group_fast<PRED_RDD, THETA_FULL, JBJ>(TRI_GROUP_ARGS); break;
+        case PRED_SAME: triangle_group_fast<PRED_SAME, THETA_FULL, JBJ>(TRI_GROUP_ARGS); break;
+        default: triangle_group_fast<PRED_ONE, THETA_FULL, JBJ>(TRI_GROUP_ARGS); break;
     }
+#undef TRI_GROUP_ARGS
 }
 
 #ifndef TRI_MIN_BLOCKS
@@ -930,16 +976,18 @@ triangle_fast_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ 
                      RecheckQueue q, int copies) {
     extern __shared__ __align__(16) unsigned char smem[];
     float4* P = reinterpret_cast<float4*>(smem);
-    int2* JK = reinterpret_cast<int2*>(smem + 3 * TILE * sizeof(float4));
-    int2* IJ = JK + TILE * TILE;
+    unsigned long long* JM = reinterpret_cast<unsigned long long*>(P + (2 + TRI_GROUP_A) * TILE);
+    int2* IJ = reinterpret_cast<int2*>(JM + JM_WORDS * TILE);
     int2* IK = IJ + TRI_WARPS * TILE;
-    uint32_t* Q = reinterpret_cast<uint32_t*>(IK + TRI_WARPS * TILE);
-    unsigned long long* JM = reinterpret_cast<unsigned long long*>(Q + TRI_WARPS * TRI_QCAP);
-    unsigned int* H = reinterpret_cast<unsigned int*>(JM + JM_WORDS * TILE);
+    float* JKd = reinterpret_cast<float*>(IK + TRI_WARPS * TILE);
+    uint32_t* Q = reinterpret_cast<uint32_t*>(JKd + TILE * TILE);
+    short* JKw = reinterpret_cast<short*>(Q + TRI_WARPS * TRI_QCAP);
+    unsigned int* H = reinterpret_cast<unsigned int*>(JKw + TILE * TILE);
     __shared__ unsigned int s_group;
     __shared__ int s_next_i;
     __shared__ float s_box[6 * 6];  // tile bounding boxes: 6 half-tiles x {lo, hi}
     __shared__ float s_abox[6];
+    __shared__ int4 s_meta[TRI_GROUP_A];  // A tiles of the chunk: first point, points, task flags
     for (int b = threadIdx.x; b < copies * p.len; b += blockDim.x) H[b] = 0;
     unsigned int* Hw = H + ((threadIdx.x >> 5) % copies) * p.len;
     int cur = -1;
@@ -954,18 +1002,16 @@ triangle_fast_kernel(const DevJob* __restrict__ jobs, const uint4* __restrict__ 
         if (gi >= ngroups) break;
         if (threadIdx.x < 6) s_abox[threadIdx.x] = gbox[6 * (size_t)gi + threadIdx.x];
         const uint32_t t0 = groups[gi], t1 = groups[gi + 1];
-        for (uint32_t t = t0; t < t1; t++) {
-            const uint4 task = tasks[t];
-            const int slot = (int)(task.x & TASK_SLOT_MASK);
-            if ((slot != cur || since >= FLUSH_EVERY) && cur >= 0) {
-                flush_hist(H, copies, p.len, jobs[cur].hist);
-                since = 0;
-            }
-            cur = slot;
-            since++;
-            triangle_dispatch<THETA_FULL, JBJ>(jobs[slot], task, p, P, JK, IJ, IK, Q, JM, s_box, Hw, q, ev, bn,
-                                               &s_next_i, t > t0, s_abox);
+        const int slot = (int)(tasks[t0].x & TASK_SLOT_MASK);
+        // (groups hold at most MAX_GROUP_TASKS <= FLUSH_EVERY tasks)
+        if ((slot != cur || since + (t1 - t0) > FLUSH_EVERY) && cur >= 0) {
+            flush_hist(H, copies, p.len, jobs[cur].hist);
+            since = 0;
         }
+        cur = slot;
+        since += t1 - t0;
+        triangle_dispatch<THETA_FULL, JBJ>(jobs[slot], tasks + t0, (int)(t1 - t0), p, P, JKd, JKw, IJ, IK, Q, JM,
+                                           s_box, s_meta, Hw, q, ev, bn, &s_next_i, s_abox);
     }
     if (cur >= 0) flush_hist(H, copies, p.len, jobs[cur].hist);
     __syncthreads();
