@@ -285,7 +285,10 @@ constexpr int JM_WORDS = 5;
 // A tiles resident at once: the tasks of a group (one job, tiles B and C
 // shared) are counted up to four at a time, their points i handed out to the
 // warps together
-constexpr int TRI_GROUP_A = 4;
+#ifndef TRI_GROUP_A_TILES
+#define TRI_GROUP_A_TILES 4
+#endif
+constexpr int TRI_GROUP_A = TRI_GROUP_A_TILES;
 // layout: tiles B, C and up to TRI_GROUP_A A tiles | j-class masks | per-warp
 // i-j and i-k rows | j-k sides | per-warp candidate queues | j-k side words
 // (16 bits) | histogram copies

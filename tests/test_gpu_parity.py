@@ -595,3 +595,25 @@ def test_counts_do_not_depend_on_task_groups(monkeypatch, group_tasks):
                 want = _GROUP_WANT[(name, w, len(cats[1]), len(cats[2]))]
                 assert want.sum() > 0
                 assert np.array_equal(g, want), (name, w)
+
+
+@pytest.mark.parametrize("kind", ["tp", "jbj"])
+def test_many_s_bins_counted_exactly(kind):
+    """The fast kernel's side words hold s-bins below 255; a guarded-FP32 count
+    with more s bins runs in the plain FP64 kernel and gives the oracle's
+    histogram all the same."""
+    d = synth.blobs(500, n_blobs=3, sigma=4.0, box=40.0, seed=91)
+    r = synth.uniform(400, box=40.0, seed=92)
+    if kind == "tp":
+        spec = ((300, 2.0, 10.0), (4, 1.0, 3.0), (4, 0.0, 1.0))
+        want = oracle.triangle([d, d, r], 1, spec, nan_zero=NATIVE_NAN == tpcf.NAN_ZERO)[0]
+        s = tpcf.make_spec(tpcf.TRIANGLE, tpcf.LOOP_ONE, spec, nan_policy=NATIVE_NAN)
+    else:
+        spec = ((300, 2.0, 10.0), (4, 0.2, 1.0), (4, 0.0, 1.0))
+        want = oracle.triangle_jbj([d, d, r], 1, spec)[0]
+        s = tpcf.make_spec(tpcf.TRIANGLE_JBJ, tpcf.LOOP_ONE, spec, nan_policy=NATIVE_NAN)
+    with tpcf.Engine(0) as e:
+        hd, hr = e.catalog(d), e.catalog(r)
+        got = e.count(s, e.job([hd, hd, hr]))
+    assert want.sum() > 0
+    assert np.array_equal(got, want)
