@@ -38,9 +38,11 @@
 #include <array>
 #include <atomic>
 #include <chrono>
+#include <cmath>
 #include <condition_variable>
 #include <deque>
 #include <functional>
+#include <future>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -217,12 +219,10 @@ struct View {
     DevBuf<int32_t> tile_start;  // ntiles + 1
     std::vector<int32_t> h_tile_start;
     std::vector<Box> boxes;
+    size_t upload_bytes = 0;  // host-to-device bytes of its construction
     size_t bytes() const { return pts.bytes() + tile_start.bytes(); }
 };
 
-// Balanced k-d split: order[lo, hi) is split along the widest axis so that the
-// left part holds a multiple of TILE points, recursively, until parts hold at
-// most TILE points.  Leaves appear in order, giving spatially compact tiles.
 // One split of order[lo, hi): along the widest axis, so that the left part
 // holds a multiple of `tile` points.  Returns the split point, or -1 for a
 // part of at most `tile` points (a leaf).
@@ -242,12 +242,18 @@ int64_t kd_split(const float* xyz, std::vector<int32_t>& order, int64_t lo, int6
     int64_t ntile = (n + tile - 1) / tile;
     int64_t left = ((ntile + 1) / 2) * tile;
     if (left >= n) left = n - tile;
-    int64_t mid = lo + left;
-    std::nth_element(order.begin() + lo, order.begin() + mid, order.begin() + hi, [&](int32_t p, int32_t q) {
-        float vp = xyz[3 * (int64_t)p + ax], vq = xyz[3 * (int64_t)q + ax];
-        return vp < vq || (vp == vq && p < q);
-    });
-    return mid;
+    // the split coordinate beside each index, contiguous, so that the
+    // selection compares without gathering from xyz (a NaN coordinate sorts
+    // as +inf: the order stays a strict weak one)
+    static thread_local std::vector<std::pair<float, int32_t>> keys;
+    keys.resize((size_t)n);
+    for (int64_t i = 0; i < n; i++) {
+        const float v = xyz[3 * (int64_t)order[lo + i] + ax];
+        keys[i] = {std::isnan(v) ? INFINITY : v, order[lo + i]};
+    }
+    std::nth_element(keys.begin(), keys.begin() + left, keys.begin() + n);  // (coordinate, index) order
+    for (int64_t i = 0; i < n; i++) order[lo + i] = keys[i].second;
+    return lo + left;
 }
 
 void parallel_items(size_t n, const std::function<void(size_t)>& fn);
@@ -668,6 +674,13 @@ Binning make_binning(const tpcf_spec& sp) {
         b.tri.lmax = b.lmax < 3e38 ? nextafterf((float)b.lmax, INFINITY) : INFINITY;
         double mid = (double)b.tri.s_hi * (double)b.tri.q_hi * (1 + 1e-5) + 1e-6;
         b.tri.mid_hi = sp.prune && b.tri.q_hi > 0 ? nextafterf((float)mid, INFINITY) : INFINITY;
+        // a permutation whose side ratio is at least q_rej (computed as a float
+        // product with the shorter side) lies past q_hi by more than 1e-4 of
+        // the q range, which no rounding of the reference's q = l/s and
+        // (q - q_lo)/q_bw brings back into the last bin
+        const double qr = (double)b.tri.q_hi + 1e-4 * ((double)b.tri.q_hi - (double)b.tri.q_lo) +
+                          1e-5 * fabs((double)b.tri.q_hi);
+        b.tri.q_rej = sp.prune ? nextafterf((float)qr, INFINITY) : INFINITY;
     }
     return b;
 }
@@ -833,6 +846,9 @@ struct tpcf_ctx {
     std::map<uint64_t, std::shared_ptr<Catalog>> catalogs;
     // (catalog, begin, end, tile points, global loop indices) -> view
     std::map<std::tuple<uint64_t, int64_t, int64_t, int, bool>, std::shared_ptr<View>> views;
+    // full views of new catalogs being built in the background
+    std::map<std::tuple<uint64_t, int64_t, int64_t, int, bool>, std::shared_future<std::shared_ptr<View>>>
+        pending_views;
     int tile_points = TILE;  // points per spatial tile (<= TILE)
     uint64_t next_view_id = 0;
     // acos table
@@ -874,21 +890,22 @@ tpcf_status fail(tpcf_ctx* ctx, tpcf_status s, const std::string& msg) {
     return s;
 }
 
-std::shared_ptr<View> get_view(tpcf_ctx* ctx, Lane& L, uint64_t handle, int64_t begin, int64_t end,
-                               bool global = false) {
-    std::lock_guard<std::recursive_mutex> vlk(ctx->view_mu);
-    auto it = ctx->catalogs.find(handle);
-    if (it == ctx->catalogs.end()) throw InvalidArg{"unknown catalog handle"};
-    const Catalog& c = *it->second;
-    if (end < 0) end = c.n;
-    if (begin < 0 || begin > end || end > c.n) throw InvalidArg{"catalog range out of bounds"};
-    const int tile = ctx->tile_points;
-    if (begin == 0) global = false;  // the same loop indices
-    auto key = std::make_tuple(handle, begin, end, tile, global);
-    auto vi = ctx->views.find(key);
-    if (vi != ctx->views.end()) return vi->second;
+// TPCF_PLAN_TRACE=1: wall times of view building and batch planning on stderr
+bool plan_trace() {
+    static const bool on = [] {
+        const char* e = getenv("TPCF_PLAN_TRACE");
+        return e && e[0] == '1';
+    }();
+    return on;
+}
+
+// Builds the spatial view of points [begin, end) of a catalog: k-d order,
+// tiles, their boxes, and the device copy (on stream st, synchronized).
+std::shared_ptr<View> build_view(const Catalog& c, int64_t begin, int64_t end, int tile, bool global, uint64_t id,
+                                 cudaStream_t st) {
+    const auto tv0 = std::chrono::steady_clock::now();
     auto v = std::make_shared<View>();
-    v->id = ++ctx->next_view_id;
+    v->id = id;
     int64_t n = end - begin;
     v->n = n;
     std::vector<float> xyz(3 * (size_t)n);
@@ -899,7 +916,9 @@ std::shared_ptr<View> get_view(tpcf_ctx* ctx, Lane& L, uint64_t handle, int64_t 
     }
     std::vector<int32_t> order(n);
     std::iota(order.begin(), order.end(), 0);
+    const auto tv1 = std::chrono::steady_clock::now();
     kd_order(xyz.data(), order, n, tile);
+    const auto tv2 = std::chrono::steady_clock::now();
     v->ntiles = (int)((n + tile - 1) / tile);
     std::vector<float4> pts(std::max<int64_t>(n, 1));
     for (int64_t i = 0; i < n; i++) {
@@ -931,13 +950,62 @@ std::shared_ptr<View> get_view(tpcf_ctx* ctx, Lane& L, uint64_t handle, int64_t 
         }
         v->boxes[t] = b;
     }
+    const auto tv3 = std::chrono::steady_clock::now();
     v->pts.reserve(pts.size());
-    CK(cudaMemcpyAsync(v->pts.p, pts.data(), pts.size() * sizeof(float4), cudaMemcpyHostToDevice, L.stream));
-    L.h2d += pts.size() * sizeof(float4) + (v->ntiles + 1) * sizeof(int32_t);
+    CK(cudaMemcpyAsync(v->pts.p, pts.data(), pts.size() * sizeof(float4), cudaMemcpyHostToDevice, st));
     v->tile_start.reserve(v->ntiles + 1);
     CK(cudaMemcpyAsync(v->tile_start.p, v->h_tile_start.data(), (v->ntiles + 1) * sizeof(int32_t),
-                       cudaMemcpyHostToDevice, L.stream));
-    CK(cudaStreamSynchronize(L.stream));
+                       cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
+    v->upload_bytes = pts.size() * sizeof(float4) + (v->ntiles + 1) * sizeof(int32_t);
+    if (plan_trace()) {
+        auto ms = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
+            return std::chrono::duration<double, std::milli>(b - a).count();
+        };
+        const auto tv4 = std::chrono::steady_clock::now();
+        fprintf(stderr, "tpcf view: points %lld copy %.4f order %.4f pack %.4f upload %.4f\n", (long long)n,
+                ms(tv0, tv1), ms(tv1, tv2), ms(tv2, tv3), ms(tv3, tv4));
+    }
+    return v;
+}
+
+// The view of catalog `handle` over [begin, end) for the context's tile size:
+// cached, being built in the background (a new catalog's full view), or built
+// now on the lane's stream.
+std::shared_ptr<View> get_view(tpcf_ctx* ctx, Lane& L, uint64_t handle, int64_t begin, int64_t end,
+                               bool global = false) {
+    std::unique_lock<std::recursive_mutex> vlk(ctx->view_mu);
+    auto it = ctx->catalogs.find(handle);
+    if (it == ctx->catalogs.end()) throw InvalidArg{"unknown catalog handle"};
+    const std::shared_ptr<Catalog> cat = it->second;
+    if (end < 0) end = cat->n;
+    if (begin < 0 || begin > end || end > cat->n) throw InvalidArg{"catalog range out of bounds"};
+    const int tile = ctx->tile_points;
+    if (begin == 0) global = false;  // the same loop indices
+    auto key = std::make_tuple(handle, begin, end, tile, global);
+    auto vi = ctx->views.find(key);
+    if (vi != ctx->views.end()) return vi->second;
+    auto pi = ctx->pending_views.find(key);
+    if (pi != ctx->pending_views.end()) {
+        std::shared_future<std::shared_ptr<View>> fut = pi->second;
+        vlk.unlock();
+        std::shared_ptr<View> v;
+        try {
+            v = fut.get();
+        } catch (...) {
+            vlk.lock();
+            ctx->pending_views.erase(key);
+            throw;
+        }
+        vlk.lock();
+        ctx->pending_views.erase(key);
+        if (!ctx->catalogs.count(handle)) throw InvalidArg{"unknown catalog handle"};
+        auto ins = ctx->views.emplace(key, v);
+        if (ins.second) L.h2d += v->upload_bytes;
+        return ins.first->second;
+    }
+    auto v = build_view(*cat, begin, end, tile, global, ++ctx->next_view_id, L.stream);
+    L.h2d += v->upload_bytes;
     ctx->views[key] = v;
     return v;
 }
@@ -1580,14 +1648,9 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
     L.d_counters.reserve(8);
     size_t ntasks = 0, ngroups = 0;
     const bool plan_hit = sig == L.plan_sig;
-    // TPCF_PLAN_TRACE=1: the planning phases' wall times on stderr
-    static const bool plan_trace = [] {
-        const char* e = getenv("TPCF_PLAN_TRACE");
-        return e && e[0] == '1';
-    }();
     std::vector<std::pair<const char*, double>> phases;
     auto phase = [&](const char* name) {
-        if (plan_trace)
+        if (plan_trace())
             phases.push_back({name, std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() -
                                                                               t_wall0).count()});
     };
@@ -1734,7 +1797,7 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
     }
     L.stats.plan_ms =
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_wall0).count();
-    if (plan_trace) {
+    if (plan_trace()) {
         std::string line = "tpcf plan: tasks " + std::to_string(ntasks) + " groups " + std::to_string(ngroups);
         double prev = 0;
         for (auto& ph : phases) {
@@ -2299,6 +2362,8 @@ tpcf_status tpcf_destroy(tpcf_ctx* ctx) {
         std::lock_guard<std::recursive_mutex> lk(ctx->mu);
         std::lock_guard<std::recursive_mutex> vlk(ctx->view_mu);
         cudaSetDevice(ctx->device);
+        for (auto& kv : ctx->pending_views) kv.second.wait();
+        ctx->pending_views.clear();
         ctx->views.clear();
         for (auto& L : ctx->lanes) L->release();
         ctx->acos_keys.release();
@@ -2325,13 +2390,26 @@ tpcf_status tpcf_catalog_create(tpcf_ctx* ctx, const float* x, const float* y, c
         uint64_t h = ctx->next_handle++;
         ctx->catalogs[h] = c;
         // the resident form of a catalog is its spatial view (sorted points,
-        // tiles); sub-range views are made on demand from the host copy
-        try {
-            get_view(ctx, *ctx->lanes[0], h, 0, n);
-        } catch (...) {
-            ctx->catalogs.erase(h);
-            throw;
-        }
+        // tiles, device copy), built on a thread of its own so that the
+        // caller's next catalog (or anything else) proceeds meanwhile; the
+        // first use waits for it.  Sub-range views are made on demand from the
+        // host copy.
+        const int dev = ctx->device, tile = ctx->tile_points;
+        const uint64_t id = ++ctx->next_view_id;
+        ctx->pending_views[std::make_tuple(h, (int64_t)0, n, tile, false)] =
+            std::async(std::launch::async, [c, n, tile, dev, id] {
+                CK(cudaSetDevice(dev));
+                cudaStream_t st = nullptr;
+                CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+                try {
+                    auto v = build_view(*c, 0, n, tile, false, id, st);
+                    cudaStreamDestroy(st);
+                    return v;
+                } catch (...) {
+                    cudaStreamDestroy(st);
+                    throw;
+                }
+            }).share();
         *handle = h;
     });
 }
@@ -2345,6 +2423,16 @@ tpcf_status tpcf_catalog_release(tpcf_ctx* ctx, uint64_t handle) {
         if (std::get<0>(it->first) == handle) it = ctx->views.erase(it);
         else ++it;
     }
+    // a view still being built: wait for it (its device buffers are freed
+    // with the last reference), whatever its outcome
+    for (auto it = ctx->pending_views.begin(); it != ctx->pending_views.end();) {
+        if (std::get<0>(it->first) == handle) {
+            it->second.wait();
+            it = ctx->pending_views.erase(it);
+        } else {
+            ++it;
+        }
+    }
     return TPCF_OK;
 }
 
@@ -2353,6 +2441,12 @@ tpcf_status tpcf_resident_bytes(tpcf_ctx* ctx, int64_t* bytes) {
     std::lock_guard<std::recursive_mutex> lk(ctx->view_mu);
     int64_t b = 0;
     for (auto& kv : ctx->views) b += (int64_t)kv.second->bytes();
+    for (auto& kv : ctx->pending_views) {  // (a failed build holds nothing)
+        try {
+            b += (int64_t)kv.second.get()->bytes();
+        } catch (...) {
+        }
+    }
     *bytes = b;
     return TPCF_OK;
 }

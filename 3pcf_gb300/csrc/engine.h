@@ -97,6 +97,7 @@ struct TriParams {
     float lmax;                  // sides >= lmax cannot belong to a counted triangle
     float mid_hi;                // s_hi * q_hi (rounded up): permutation 0 needs two sides below it,
                                  // permutation 1 needs all three below it
+    float q_rej;                 // a side ratio at or above it is out of the q range whatever the rounding
 };
 
 constexpr int TS_UMAX = 68;  // squared-length thresholds of up to 64 bins

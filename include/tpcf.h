@@ -173,7 +173,10 @@ int32_t tpcf_abi_version(void);
 /* ---- catalogs --------------------------------------------------------------- */
 /* Upload n points (SoA float arrays) as a resident catalog.  Replaces the
  * reference's per-program read + malloc of h_x/h_y/h_z
- * (src/3pcf_C_version.cc:311-332, src/3pcf_C_version_triangle_parametrization.cc:366-439). */
+ * (src/3pcf_C_version.cc:311-332, src/3pcf_C_version_triangle_parametrization.cc:366-439).
+ * The arrays are copied before the call returns; the catalog's spatial order
+ * and its device copy are built on a thread of the library meanwhile, and the
+ * first count that uses the catalog waits for them (and reports their errors). */
 tpcf_status tpcf_catalog_create(tpcf_ctx* ctx, const float* x, const float* y, const float* z,
                                 int64_t n, uint64_t* handle);
 tpcf_status tpcf_catalog_release(tpcf_ctx* ctx, uint64_t handle);
