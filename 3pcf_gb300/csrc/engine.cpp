@@ -173,6 +173,11 @@ struct DevBuf {
         n = m;
     }
     size_t bytes() const { return n * sizeof(T); }
+    void swap(DevBuf& o) {
+        std::swap(p, o.p);
+        std::swap(n, o.n);
+        std::swap(cap, o.cap);
+    }
 };
 
 // Page-locked host buffer (device-to-host copies inside captured graphs need one).
@@ -742,6 +747,12 @@ struct PlanScratch {
     std::vector<uint4> tasks;
     std::vector<uint32_t> groups;
     std::vector<float> gbox;
+    std::vector<uint4> tasks2;  // the second part of a pipelined plan
+    std::vector<uint32_t> groups2;
+    std::vector<float> gbox2;
+    std::vector<uint4> tasks3;  // both parts in one (the merged plan)
+    std::vector<uint32_t> groups3;
+    std::vector<float> gbox3;
 };
 
 // One lane = one stream with its own scratch buffers.  The synchronous API uses
@@ -755,6 +766,19 @@ struct Lane {
     DevBuf<uint4> d_tasks;
     DevBuf<uint32_t> d_groups;  // fast triangle kernel: first task of each group (+ end)
     DevBuf<float> d_gbox;       // ... and the box of each group's A tiles
+    // second part of a pipelined plan (the jobs after the first, planned while
+    // the first job counts): its tasks, groups and boxes
+    DevBuf<uint4> d_tasks2;
+    DevBuf<uint32_t> d_groups2;
+    DevBuf<float> d_gbox2;
+    // the whole plan in one part, uploaded while the parts count, for the
+    // repeats of the batch
+    DevBuf<uint4> d_tasks3;
+    DevBuf<uint32_t> d_groups3;
+    DevBuf<float> d_gbox3;
+    cudaStream_t side = nullptr;   // the second part: its upload and its launch
+    cudaStream_t side2 = nullptr;  // the upload of the merged plan
+    cudaEvent_t ev_side = nullptr;
     DevBuf<unsigned int> d_counters;  // [0] task counter, [1] recheck count, [2..5] evaluated/binned
     DevBuf<uint4> d_queue;
     DevBuf<unsigned long long> d_hist;
@@ -764,6 +788,7 @@ struct Lane {
     std::vector<uint64_t> plan_sig;
     size_t plan_ntasks = 0;
     size_t plan_ngroups = 0;  // task groups of the fast triangle kernel
+    size_t plan_ntasks2 = 0, plan_ngroups2 = 0;  // second part of a pipelined plan (0: none)
     uint64_t plan_evaluated = 0;
     // the launch sequence of the last batch, captured as a CUDA graph and
     // replayed while the batch and every buffer it touches stay the same
@@ -790,6 +815,17 @@ struct Lane {
         d_tasks.release();
         d_groups.release();
         d_gbox.release();
+        d_tasks2.release();
+        d_groups2.release();
+        d_gbox2.release();
+        d_tasks3.release();
+        d_groups3.release();
+        d_gbox3.release();
+        if (ev_side) cudaEventDestroy(ev_side);
+        if (side) cudaStreamDestroy(side);
+        if (side2) cudaStreamDestroy(side2);
+        ev_side = nullptr;
+        side = side2 = nullptr;
         d_counters.release();
         d_queue.release();
         d_hist.release();
@@ -1655,18 +1691,31 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
                                                                               t_wall0).count()});
     };
     phase("views");
-    if (plan_hit) {
-        ntasks = L.plan_ntasks;
-        ngroups = L.plan_ngroups;
-        evaluated = L.plan_evaluated;
-    } else {
+    const bool pairs = sp.kind == TPCF_PAIR;
+    const bool fast_tri = (sp.kind == TPCF_TRIANGLE || sp.kind == TPCF_TRIANGLE_JBJ) && guarded_fp32(sp, bin);
+    // A newly planned batch of two to eight fast-kernel jobs (an estimator's
+    // DDD/DDR/DRR/RRR set) is pipelined: the first job is planned, uploaded and
+    // launched, and the others are planned while it counts (a second launch
+    // follows on the same stream).  Larger batches -- voxel and jackknife sets
+    // of many similar jobs, whose first job is a small share -- keep one launch.
+    const char* pl_env = getenv("TPCF_PIPELINE");
+    const bool pipeline = !plan_hit && fast_tri && group.size() >= 2 && group.size() <= 8 && !L.slice_batches &&
+                          !(pl_env && pl_env[0] == '0');
+    size_t ntasks2 = 0, ngroups2 = 0;
+    uint64_t evaluated2 = 0;
+    // planning state shared by the parts of a plan: bound tables by view pair
+    std::vector<TripletPlan> tp(pairs ? 0 : group.size());
+    std::map<std::pair<const View*, const View*>, std::unique_ptr<PairTable>> tables;
+    std::vector<PairTable*> table_list;
+    // Plans jobs [g0, g1) into task list, group starts and group boxes (the
+    // last two for the fast triangle kernel); returns the evaluated units.
+    auto plan_jobs = [&](size_t g0, size_t g1, std::vector<uint4>& h_tasks, std::vector<uint32_t>& h_groups,
+                         std::vector<float>& h_gbox) -> uint64_t {
         // plan in parallel: bound tables and neighbour lists by rows, then
         // tile triples (pairs) by ranges of A tiles
-        const bool pairs = sp.kind == TPCF_PAIR;
-        std::vector<TripletPlan> tp(pairs ? 0 : group.size());
-        std::map<std::pair<const View*, const View*>, std::unique_ptr<PairTable>> tables;
-        std::vector<PairTable*> table_list;
+        uint64_t ev = 0;
         if (!pairs) {
+            const size_t t_first = table_list.size();
             auto table = [&](const View* x, const View* y, bool nb) {
                 auto& t = tables[std::make_pair(x, y)];
                 if (!t) {
@@ -1675,19 +1724,21 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
                     table_list.push_back(t.get());
                 }
                 if (nb && !t->need_nb) {
+                    if (table_list.end() == std::find(table_list.begin() + t_first, table_list.end(), t.get()))
+                        table_list.push_back(t.get());  // filled before without neighbour lists: fill again
                     t->need_nb = true;
                     t->nb.assign(x->ntiles, {});
                 }
                 return t.get();
             };
-            for (size_t g = 0; g < group.size(); g++) {
+            for (size_t g = g0; g < g1; g++) {
                 const View *A = pj[g].role(0), *B = pj[g].role(1), *C = pj[g].role(2);
                 const bool empty = A->ntiles == 0 || B->ntiles == 0 || C->ntiles == 0;
                 tp[g].init(*group[g].spec, pj[g], (uint32_t)g, bin, empty ? nullptr : table(A, B, true),
                            empty ? nullptr : table(A, C, true), empty ? nullptr : table(B, C, false));
             }
             std::vector<std::array<int, 3>> items;  // table, row begin, row end
-            for (size_t t = 0; t < table_list.size(); t++)
+            for (size_t t = t_first; t < table_list.size(); t++)
                 for (int r = 0; r < table_list[t]->x->ntiles; r += 16)
                     items.push_back({(int)t, r, std::min(r + 16, table_list[t]->x->ntiles)});
             parallel_items(items.size(), [&](size_t i) {
@@ -1696,9 +1747,8 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
             });
         }
         phase("tables");
-        const bool fast_tri = (sp.kind == TPCF_TRIANGLE || sp.kind == TPCF_TRIANGLE_JBJ) && guarded_fp32(sp, bin);
         std::vector<std::array<int, 3>> items;  // job, A-tile begin, end
-        for (size_t g = 0; g < group.size(); g++) {
+        for (size_t g = g0; g < g1; g++) {
             const int na = pj[g].role(0)->ntiles, step = pairs ? 16 : 2;
             for (int a0 = 0; a0 < na; a0 += step) items.push_back({(int)g, a0, std::min(a0 + step, na)});
         }
@@ -1732,13 +1782,10 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
         }
         std::vector<size_t> off(items.size() + 1, 0);  // each item's first task
         for (size_t i = 0; i < items.size(); i++) {
-            evaluated += part_eval[i];
+            ev += part_eval[i];
             off[i + 1] = off[i] + part[i].size();
         }
         const size_t total = off[items.size()];
-        std::vector<uint4>& h_tasks = S.tasks;
-        std::vector<uint32_t>& h_groups = S.groups;
-        std::vector<float>& h_gbox = S.gbox;
         h_tasks.resize(total);
         h_groups.clear();
         h_gbox.clear();
@@ -1772,40 +1819,94 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
             });
         }
         phase("order");
-        ntasks = h_tasks.size();
-        ngroups = h_groups.empty() ? 0 : h_groups.size() - 1;
-        if (ngroups) {
-            L.d_groups.reserve(h_groups.size());
-            L.d_gbox.reserve(h_gbox.size());
-            CK(cudaMemcpyAsync(L.d_groups.p, h_groups.data(), h_groups.size() * sizeof(uint32_t),
-                               cudaMemcpyHostToDevice, st));
-            CK(cudaMemcpyAsync(L.d_gbox.p, h_gbox.data(), h_gbox.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+        return ev;
+    };
+    // Uploads a planned part on stream s into the given buffers; returns the
+    // group count.
+    auto upload_part = [&](const std::vector<uint4>& h_tasks, const std::vector<uint32_t>& h_groups,
+                           const std::vector<float>& h_gbox, DevBuf<uint4>& d_tasks, DevBuf<uint32_t>& d_groups,
+                           DevBuf<float>& d_gbox, cudaStream_t s) -> size_t {
+        const size_t ng = h_groups.empty() ? 0 : h_groups.size() - 1;
+        if (ng) {
+            d_groups.reserve(h_groups.size());
+            d_gbox.reserve(h_gbox.size());
+            CK(cudaMemcpyAsync(d_groups.p, h_groups.data(), h_groups.size() * sizeof(uint32_t),
+                               cudaMemcpyHostToDevice, s));
+            CK(cudaMemcpyAsync(d_gbox.p, h_gbox.data(), h_gbox.size() * sizeof(float), cudaMemcpyHostToDevice, s));
             L.h2d += h_groups.size() * sizeof(uint32_t) + h_gbox.size() * sizeof(float);
         }
-        L.d_jobs.reserve(dj.size());
-        L.d_tasks.reserve(std::max<size_t>(h_tasks.size(), 1));
-        CK(cudaMemcpyAsync(L.d_jobs.p, dj.data(), dj.size() * sizeof(DevJob), cudaMemcpyHostToDevice, st));
-        L.h2d += dj.size() * sizeof(DevJob) + h_tasks.size() * sizeof(uint4);
+        d_tasks.reserve(std::max<size_t>(h_tasks.size(), 1));
+        L.h2d += h_tasks.size() * sizeof(uint4);
         if (!h_tasks.empty())
-            CK(cudaMemcpyAsync(L.d_tasks.p, h_tasks.data(), h_tasks.size() * sizeof(uint4), cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(d_tasks.p, h_tasks.data(), h_tasks.size() * sizeof(uint4), cudaMemcpyHostToDevice, s));
+        return ng;
+    };
+    if (plan_hit) {
+        ntasks = L.plan_ntasks;
+        ngroups = L.plan_ngroups;
+        ntasks2 = L.plan_ntasks2;
+        ngroups2 = L.plan_ngroups2;
+        evaluated = L.plan_evaluated;
+    } else {
+        L.plan_sig.clear();  // (set again once the whole plan is on the device)
+        PlanScratch& S = L.scratch;
+        const size_t g_first = pipeline ? 1 : group.size();
+        evaluated = plan_jobs(0, g_first, S.tasks, S.groups, S.gbox);
+        L.d_jobs.reserve(dj.size());
+        CK(cudaMemcpyAsync(L.d_jobs.p, dj.data(), dj.size() * sizeof(DevJob), cudaMemcpyHostToDevice, st));
+        L.h2d += dj.size() * sizeof(DevJob);
+        ngroups = upload_part(S.tasks, S.groups, S.gbox, L.d_tasks, L.d_groups, L.d_gbox, st);
+        ntasks = S.tasks.size();
         CK(cudaStreamSynchronize(st));
-        L.plan_sig = sig;
-        L.plan_ntasks = ntasks;
-        L.plan_ngroups = ngroups;
-        L.plan_evaluated = evaluated;
+        if (!pipeline) {
+            L.plan_sig = sig;
+            L.plan_ntasks = ntasks;
+            L.plan_ngroups = ngroups;
+            L.plan_ntasks2 = L.plan_ngroups2 = 0;
+            L.plan_evaluated = evaluated;
+        }
         phase("upload");
     }
+    // the second part of a pipelined plan, planned and uploaded (on the side
+    // stream) while the first part counts; the counting stream waits for it
+    bool second_pending = pipeline;
+    auto plan_second = [&]() {
+        PlanScratch& S = L.scratch;
+        evaluated2 = plan_jobs(1, group.size(), S.tasks2, S.groups2, S.gbox2);
+        if (!L.side) {
+            CK(cudaStreamCreateWithFlags(&L.side, cudaStreamNonBlocking));
+            CK(cudaEventCreateWithFlags(&L.ev_side, cudaEventDisableTiming));
+        }
+        ngroups2 = upload_part(S.tasks2, S.groups2, S.gbox2, L.d_tasks2, L.d_groups2, L.d_gbox2, L.side);
+        ntasks2 = S.tasks2.size();
+        evaluated += evaluated2;
+        second_pending = false;
+        phase("second part");
+    };
+    // The merged plan (the first part's groups, then the second's, its task
+    // indices shifted), uploaded on a stream of its own while the parts count;
+    // it replaces the two parts once they are done.
+    bool merge_pending = pipeline;
+    auto merge_plan = [&]() {
+        PlanScratch& S = L.scratch;
+        S.tasks3.resize(ntasks + ntasks2);
+        std::copy(S.tasks.begin(), S.tasks.end(), S.tasks3.begin());
+        std::copy(S.tasks2.begin(), S.tasks2.end(), S.tasks3.begin() + ntasks);
+        S.groups3.resize(ngroups + ngroups2 + 1);
+        for (size_t g = 0; g < ngroups; g++) S.groups3[g] = S.groups[g];
+        for (size_t g = 0; g <= ngroups2; g++)
+            S.groups3[ngroups + g] = (uint32_t)ntasks + (ngroups2 ? S.groups2[g] : 0u);
+        S.gbox3.resize(6 * (ngroups + ngroups2));
+        std::copy(S.gbox.begin(), S.gbox.begin() + 6 * ngroups, S.gbox3.begin());
+        std::copy(S.gbox2.begin(), S.gbox2.begin() + 6 * ngroups2, S.gbox3.begin() + 6 * ngroups);
+        if (!L.side2) CK(cudaStreamCreateWithFlags(&L.side2, cudaStreamNonBlocking));
+        const uint64_t h2d0 = L.h2d;
+        upload_part(S.tasks3, S.groups3, S.gbox3, L.d_tasks3, L.d_groups3, L.d_gbox3, L.side2);
+        L.h2d = h2d0;  // (a copy for later calls: not this count's input)
+        merge_pending = false;
+    };
     L.stats.plan_ms =
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_wall0).count();
-    if (plan_trace()) {
-        std::string line = "tpcf plan: tasks " + std::to_string(ntasks) + " groups " + std::to_string(ngroups);
-        double prev = 0;
-        for (auto& ph : phases) {
-            line += std::string(" ") + ph.first + " " + std::to_string(ph.second - prev);
-            prev = ph.second;
-        }
-        fprintf(stderr, "%s\n", line.c_str());
-    }
     const bool fp64 = !guarded_fp32(sp, bin);
     const bool fast_jbj = sp.kind == TPCF_TRIANGLE_JBJ && !fp64;  // the fast kernel's JBJ binning
     if (sp.kind == TPCF_TRIANGLE) ensure_acos(ctx);
@@ -1829,13 +1930,16 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
     auto count_with = [&](const Shape& sh, bool allow_graph) -> float {
         const int copies = sh.copies;
         // units the persistent CTAs pull: task groups (fast triangle kernel) or tasks
-        const unsigned int nwork = ngroups ? (unsigned int)ngroups : nt;
+        const unsigned int nwork = fast_tri ? (unsigned int)ngroups : nt;
         const int grid = grid_for(ctx, sh, nwork, L.sm_cap);
         // slices of at least 8 units per CTA, at most 64 of them
         unsigned int slice = L.slice_batches ? std::max<unsigned int>((unsigned int)grid * 8u, (nwork + 63u) / 64u)
                                              : std::max(nwork, 1u);
         if (L.slice_batches && ctx->slice_tasks > 0) slice = (unsigned int)ctx->slice_tasks;
-        launches = (nwork > slice ? (nwork + slice - 1) / slice : 1) + ((sp.kind == TPCF_TRIANGLE && !fp64) ? 1 : 0);
+        // a pipelined plan: two launches, one per part
+        const bool two_part = fast_tri && (ngroups2 > 0 || second_pending);
+        launches = (two_part ? 2 : (nwork > slice ? (nwork + slice - 1) / slice : 1)) +
+                   ((sp.kind == TPCF_TRIANGLE && !fp64) ? 1 : 0);
         for (int attempt = 0; attempt < 3; attempt++) {
             RecheckQueue q{};
             if (sp.kind == TPCF_TRIANGLE && !fp64) {
@@ -1877,13 +1981,34 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
                                                  sh.groups, st);
                     return launch_pairs(L.d_jobs.p, tk, n, L.d_counters.p, bin.pair, fp64, grid, copies, st);
                 };
-                // one launch over all tasks, or (a heavy serving batch) slices of
-                // them, between which the device can start the kernels that
-                // higher-priority streams (the light serving lanes) have queued
-                EQ(launch_main(0, std::min(nwork, slice)));
-                for (unsigned int t0 = slice; t0 < nwork; t0 += slice) {
-                    EQ(cudaMemsetAsync(L.d_counters.p, 0, sizeof(unsigned int), st));  // the slice's task counter
-                    EQ(launch_main(t0, std::min(slice, nwork - t0)));
+                if (two_part) {
+                    // the first job's groups, then the others' (their own group
+                    // counter, d_counters[6]); on the first count of a pipelined
+                    // plan the second part is planned between the two launches
+                    EQ(launch_main(0, (unsigned int)ngroups));
+                    if (second_pending) plan_second();
+                    if (ngroups2) {
+                        // on the side stream, behind its upload and the zeroing of
+                        // the histograms and counters: its CTAs take the SMs the
+                        // first part's CTAs leave at its end
+                        EQ(cudaStreamWaitEvent(L.side, L.ev0, 0));
+                        EQ(launch_triangle_fast(L.d_jobs.p, L.d_tasks2.p, L.d_groups2.p, L.d_gbox2.p,
+                                                (unsigned int)ngroups2, L.d_counters.p + 6, bin.tri, q,
+                                                grid_for(ctx, sh, ngroups2, L.sm_cap), copies, fast_jbj ? 1 : 0,
+                                                L.side));
+                        EQ(cudaEventRecord(L.ev_side, L.side));
+                        EQ(cudaStreamWaitEvent(st, L.ev_side, 0));
+                    }
+                    if (merge_pending) merge_plan();
+                } else {
+                    // one launch over all tasks, or (a heavy serving batch) slices of
+                    // them, between which the device can start the kernels that
+                    // higher-priority streams (the light serving lanes) have queued
+                    EQ(launch_main(0, std::min(nwork, slice)));
+                    for (unsigned int t0 = slice; t0 < nwork; t0 += slice) {
+                        EQ(cudaMemsetAsync(L.d_counters.p, 0, sizeof(unsigned int), st));  // the slice's task counter
+                        EQ(launch_main(t0, std::min(slice, nwork - t0)));
+                    }
                 }
                 EQ(cudaEventRecordWithFlags(L.ev_mid, st, ev_flags));
                 if (sp.kind == TPCF_TRIANGLE && !fp64)
@@ -1907,7 +2032,9 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
                                           (uint64_t)(uintptr_t)acos_t.bucket, (uint64_t)acos_t.n, queue_cap,
                                           (uint64_t)grid, (uint64_t)copies, (uint64_t)sh.groups, hist_total, ntasks,
                                           (uint64_t)slice, (uint64_t)(uintptr_t)L.d_groups.p,
-                                          (uint64_t)(uintptr_t)L.d_gbox.p, (uint64_t)ngroups};
+                                          (uint64_t)(uintptr_t)L.d_gbox.p, (uint64_t)ngroups,
+                                          (uint64_t)(uintptr_t)L.d_tasks2.p, (uint64_t)(uintptr_t)L.d_groups2.p,
+                                          (uint64_t)(uintptr_t)L.d_gbox2.p, (uint64_t)ngroups2};
                 gsig.insert(gsig.end(), extra, extra + sizeof(extra) / sizeof(extra[0]));
                 if (!L.graph || gsig != L.graph_sig) {
                     L.drop_graph();
@@ -1990,7 +2117,19 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
         std::lock_guard<std::mutex> tlk(ctx->tune_mu);
         ctx->tuned[key] = shape;
     } else {
-        count_with(shape, graphs);
+        count_with(shape, graphs && !pipeline);  // (the first count of a pipelined plan is not captured)
+    }
+    if (pipeline) {
+        // the parts are done: later counts of the batch use the merged plan
+        CK(cudaStreamSynchronize(L.side2));
+        L.d_tasks.swap(L.d_tasks3);
+        L.d_groups.swap(L.d_groups3);
+        L.d_gbox.swap(L.d_gbox3);
+        L.plan_sig = sig;
+        L.plan_ntasks = ntasks + ntasks2;
+        L.plan_ngroups = ngroups + ngroups2;
+        L.plan_ntasks2 = L.plan_ngroups2 = 0;
+        L.plan_evaluated = evaluated;
     }
     L.stats.tuned_shapes = tuned_runs;
     L.stats.hist_copies = (uint64_t)shape.copies;
@@ -2020,11 +2159,22 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
     const bool fast_kernel = (sp.kind == TPCF_TRIANGLE || sp.kind == TPCF_TRIANGLE_JBJ) && !fp64;
     L.stats.evaluated_units = fast_kernel ? dev_evaluated : evaluated;
     L.stats.binned_units = fast_kernel ? dev_binned : evaluated;
-    L.stats.tasks = ntasks;
+    L.stats.tasks = ntasks + ntasks2;
     L.stats.kernel_launches = launches * std::max<uint64_t>(1, tuned_runs);
     L.stats.recheck_regrows = regrows;
     L.stats.total_ms =
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_wall0).count();
+    if (plan_trace()) {
+        std::string line = "tpcf plan: tasks " + std::to_string(ntasks + ntasks2) + " groups " +
+                           std::to_string(ngroups + ngroups2) + (pipeline ? " (two parts)" : "");
+        double prev = 0;
+        for (auto& ph : phases) {
+            line += std::string(" ") + ph.first + " " + std::to_string(ph.second - prev);
+            prev = ph.second;
+        }
+        line += " total " + std::to_string(L.stats.total_ms);
+        fprintf(stderr, "%s\n", line.c_str());
+    }
 }
 
 void validate(const tpcf_spec* sp, const tpcf_job* job) {

@@ -27,7 +27,10 @@ def test_graph_replay_matches_direct_launches(monkeypatch):
         hd, hr = eng.catalog(d), eng.catalog(r)
         specs, jobs = _batch(eng, hd, hr)
         first = eng.count_batch(specs, jobs)
-        assert eng.stats()["graph_replays"] == 1
+        # the first count of a newly planned batch of several fast-kernel jobs
+        # is pipelined (the later jobs are planned while the first counts) and
+        # launched directly; the repeated batch replays a graph of both parts
+        assert eng.stats()["graph_replays"] == 0
         again = eng.count_batch(specs, jobs)
         assert eng.stats()["graph_replays"] == 1
         for a, b in zip(first, again):
@@ -41,6 +44,19 @@ def test_graph_replay_matches_direct_launches(monkeypatch):
         direct = eng.count_batch(specs, jobs)
         assert eng.stats()["graph_replays"] == 0
         for a, b in zip(first, direct):
+            assert np.array_equal(a, b)
+        # one launch over all the batch's tasks (no pipelining): the same counts
+        monkeypatch.setenv("TPCF_PIPELINE", "0")
+        monkeypatch.setenv("TPCF_GRAPHS", "1")
+        e1 = tpcf.Engine(0)
+        try:
+            ha, hb = e1.catalog(d), e1.catalog(r)
+            s1, j1 = _batch(e1, ha, hb)
+            single = e1.count_batch(s1, j1)
+            assert e1.stats()["graph_replays"] == 1
+        finally:
+            e1.close()
+        for a, b in zip(first, single):
             assert np.array_equal(a, b)
         assert np.array_equal(pair, eng.count(tpcf.make_spec(tpcf.PAIR, tpcf.LOOP_SAME, [(700, 0.0, 70.0)]),
                                               eng.job([hd, hd])))
