@@ -903,7 +903,7 @@ __device__ void triangle_group_fast(const DevJob& J, const uint4* __restrict__ g
             // plus j and the weight bit of two-array jobs)
             const uint32_t klo = ((uint32_t)lane << 6) | (1u << 12), khi = ((uint32_t)(lane + 32) << 6) | (1u << 12);
             int qn = 0;  // queued candidates (warp-uniform)
-    #pragma unroll
+#pragma unroll
             for (int h = 0; h < 2; h++) {
                 unsigned live = __ballot_sync(0xffffffffu, (h ? cm1 : cm0) != 0ull);
                 const unsigned long long cmv = h ? cm1 : cm0, w2v = h ? w21 : w20;

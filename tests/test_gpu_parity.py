@@ -617,3 +617,26 @@ def test_many_s_bins_counted_exactly(kind):
         got = e.count(s, e.job([hd, hd, hr]))
     assert want.sum() > 0
     assert np.array_equal(got, want)
+
+
+def test_catalogs_built_in_the_background():
+    """A catalog's spatial view is built on a library thread: releasing it before
+    any use, counting right after creation, counting many new catalogs in one
+    batch and asking for the resident bytes all see the finished view."""
+    d = synth.blobs(700, n_blobs=3, sigma=4.0, box=40.0, seed=95)
+    r = synth.uniform(600, box=40.0, seed=96)
+    spec = ((8, 2.0, 10.0), (8, 1.0, 3.0), (16, 0.0, 1.0))
+    want = oracle.triangle([d, d, r], 1, spec, nan_zero=NATIVE_NAN == tpcf.NAN_ZERO)[0]
+    with tpcf.Engine(0) as e:
+        for _ in range(5):
+            e.release(e.catalog(d))  # released while (or after) its view is built
+        hs = [(e.catalog(d), e.catalog(r)) for _ in range(4)]
+        assert e.resident_bytes() >= 4 * (700 + 600) * 16
+        s = tpcf.make_spec(tpcf.TRIANGLE, tpcf.LOOP_ONE, spec, nan_policy=NATIVE_NAN)
+        got = e.count_batch([s] * 4, [e.job([hd, hd, hr]) for hd, hr in hs])
+        for g in got:
+            assert np.array_equal(g, want)
+        for hd, hr in hs:
+            e.release(hd)
+            e.release(hr)
+        assert e.resident_bytes() == 0
