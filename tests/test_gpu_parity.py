@@ -640,3 +640,33 @@ def test_catalogs_built_in_the_background():
             e.release(hd)
             e.release(hr)
         assert e.resident_bytes() == 0
+
+
+def test_pipelined_batches_with_empty_jobs():
+    """A new batch of a few fast-kernel jobs launches its first job while the
+    rest are planned; an empty first or later job (a zero-length catalog
+    range) leaves its histogram zero and the others exact."""
+    d = synth.blobs(600, n_blobs=3, sigma=4.0, box=40.0, seed=97)
+    r = synth.uniform(500, box=40.0, seed=98)
+    spec = ((8, 2.0, 10.0), (8, 1.0, 3.0), (16, 0.0, 1.0))
+    nz = NATIVE_NAN == tpcf.NAN_ZERO
+    want_ddr = oracle.triangle([d, d, r], 1, spec, nan_zero=nz)[0]
+    want_rrr = oracle.triangle([r, r, r], 0, spec, nan_zero=nz)[0]
+    s_one = tpcf.make_spec(tpcf.TRIANGLE, tpcf.LOOP_ONE, spec, nan_policy=NATIVE_NAN)
+    s_same = tpcf.make_spec(tpcf.TRIANGLE, tpcf.LOOP_SAME, spec, nan_policy=NATIVE_NAN)
+    with tpcf.Engine(0) as e:
+        hd, hr = e.catalog(d), e.catalog(r)
+        empty = e.job([hd, hd, hd], [(0, 0)] * 3)
+        for specs, jobs, wants in (
+                ([s_same, s_one, s_same], [empty, e.job([hd, hd, hr]), e.job([hr, hr, hr])],
+                 [None, want_ddr, want_rrr]),
+                ([s_one, s_same, s_same], [e.job([hd, hd, hr]), empty, e.job([hr, hr, hr])],
+                 [want_ddr, None, want_rrr])):
+            got = e.count_batch(specs, jobs)
+            again = e.count_batch(specs, jobs)  # the merged plan of the repeat
+            for g, a, w in zip(got, again, wants):
+                assert np.array_equal(g, a)
+                if w is None:
+                    assert g.sum() == 0
+                else:
+                    assert w.sum() > 0 and np.array_equal(g, w)
