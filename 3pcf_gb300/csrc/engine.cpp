@@ -883,8 +883,12 @@ struct tpcf_ctx {
     // (catalog, begin, end, tile points, global loop indices) -> view
     std::map<std::tuple<uint64_t, int64_t, int64_t, int, bool>, std::shared_ptr<View>> views;
     // full views of new catalogs being built in the background
-    std::map<std::tuple<uint64_t, int64_t, int64_t, int, bool>, std::shared_future<std::shared_ptr<View>>>
-        pending_views;
+    struct PendingView {
+        std::shared_future<std::shared_ptr<View>> fut;
+        uint64_t id;
+        int64_t n;
+    };
+    std::map<std::tuple<uint64_t, int64_t, int64_t, int, bool>, PendingView> pending_views;
     int tile_points = TILE;  // points per spatial tile (<= TILE)
     uint64_t next_view_id = 0;
     // acos table
@@ -1005,11 +1009,20 @@ std::shared_ptr<View> build_view(const Catalog& c, int64_t begin, int64_t end, i
     return v;
 }
 
+// Id and point count of the view of catalog `handle` over [begin, end): a
+// view being built in the background is not waited for (its id was assigned
+// when it was started); any other is made now.
+struct ViewRef {
+    uint64_t id;
+    int64_t n;
+};
+
 // The view of catalog `handle` over [begin, end) for the context's tile size:
 // cached, being built in the background (a new catalog's full view), or built
-// now on the lane's stream.
+// now on the lane's stream.  With ref != nullptr and the view still being
+// built, returns nullptr at once and fills ref.
 std::shared_ptr<View> get_view(tpcf_ctx* ctx, Lane& L, uint64_t handle, int64_t begin, int64_t end,
-                               bool global = false) {
+                               bool global = false, ViewRef* ref = nullptr) {
     std::unique_lock<std::recursive_mutex> vlk(ctx->view_mu);
     auto it = ctx->catalogs.find(handle);
     if (it == ctx->catalogs.end()) throw InvalidArg{"unknown catalog handle"};
@@ -1020,10 +1033,17 @@ std::shared_ptr<View> get_view(tpcf_ctx* ctx, Lane& L, uint64_t handle, int64_t 
     if (begin == 0) global = false;  // the same loop indices
     auto key = std::make_tuple(handle, begin, end, tile, global);
     auto vi = ctx->views.find(key);
-    if (vi != ctx->views.end()) return vi->second;
+    if (vi != ctx->views.end()) {
+        if (ref) *ref = {vi->second->id, vi->second->n};
+        return vi->second;
+    }
     auto pi = ctx->pending_views.find(key);
     if (pi != ctx->pending_views.end()) {
-        std::shared_future<std::shared_ptr<View>> fut = pi->second;
+        if (ref) {
+            *ref = {pi->second.id, pi->second.n};
+            return nullptr;
+        }
+        std::shared_future<std::shared_ptr<View>> fut = pi->second.fut;
         vlk.unlock();
         std::shared_ptr<View> v;
         try {
@@ -1043,6 +1063,7 @@ std::shared_ptr<View> get_view(tpcf_ctx* ctx, Lane& L, uint64_t handle, int64_t 
     auto v = build_view(*cat, begin, end, tile, global, ++ctx->next_view_id, L.stream);
     L.h2d += v->upload_bytes;
     ctx->views[key] = v;
+    if (ref) *ref = {v->id, v->n};
     return v;
 }
 
@@ -1325,26 +1346,27 @@ class HostPool {
         static HostPool pool;
         return pool;
     }
+    // Runs fn(0..n) on this thread and the pool's threads.  Several callers
+    // (a count's planning, background view builds, serving lanes) share the
+    // pool: idle threads help whichever jobs have items left.
     void run(size_t n, const std::function<void(size_t)>& fn) {
         if (n == 0) return;
-        std::unique_lock<std::mutex> busy(run_mu_, std::try_to_lock);
-        if (!busy.owns_lock() || workers_.empty() || n == 1) {
+        if (workers_.empty() || n == 1) {
             for (size_t i = 0; i < n; i++) fn(i);
             return;
         }
+        Job job;
+        job.fn = &fn;
+        job.n = n;
         {
             std::lock_guard<std::mutex> lk(mu_);
-            job_ = &fn;
-            n_ = n;
-            next_ = 0;
-            done_ = 0;
-            gen_++;
+            jobs_.push_back(&job);
         }
         cv_.notify_all();
-        work();
+        work(job);
         std::unique_lock<std::mutex> lk(mu_);
-        done_cv_.wait(lk, [&] { return done_ == workers_.size(); });
-        job_ = nullptr;
+        jobs_.erase(std::find(jobs_.begin(), jobs_.end(), &job));  // no new helpers
+        done_cv_.wait(lk, [&] { return job.users == 0 && job.done.load() == n; });
     }
     ~HostPool() {
         {
@@ -1356,42 +1378,50 @@ class HostPool {
     }
 
   private:
+    struct Job {
+        const std::function<void(size_t)>* fn = nullptr;
+        size_t n = 0;
+        std::atomic<size_t> next{0}, done{0};
+        size_t users = 0;  // pool threads working on it (under mu_)
+    };
     HostPool() {
         const unsigned n = std::max(1u, std::thread::hardware_concurrency()) - 1;
         for (unsigned t = 0; t < n; t++) workers_.emplace_back([this] { loop(); });
     }
-    void work() {
+    void work(Job& j) {
         for (;;) {
-            size_t i = next_.fetch_add(1);
-            if (i >= n_) break;
-            (*job_)(i);
+            size_t i = j.next.fetch_add(1);
+            if (i >= j.n) break;
+            (*j.fn)(i);
+            j.done.fetch_add(1);
         }
     }
+    Job* open_job() {  // under mu_
+        for (Job* j : jobs_)
+            if (j->next.load() < j->n) return j;
+        return nullptr;
+    }
     void loop() {
-        uint64_t seen = 0;
         for (;;) {
+            Job* j = nullptr;
             {
                 std::unique_lock<std::mutex> lk(mu_);
-                cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
+                cv_.wait(lk, [&] { return stop_ || (j = open_job()) != nullptr; });
                 if (stop_) return;
-                seen = gen_;
+                j->users++;
             }
-            work();
+            work(*j);
             {
                 std::lock_guard<std::mutex> lk(mu_);
-                done_++;
+                j->users--;
             }
             done_cv_.notify_all();
         }
     }
-    std::mutex run_mu_, mu_;
+    std::mutex mu_;
     std::condition_variable cv_, done_cv_;
     std::vector<std::thread> workers_;
-    const std::function<void(size_t)>* job_ = nullptr;
-    size_t n_ = 0;
-    std::atomic<size_t> next_{0};
-    size_t done_ = 0;
-    uint64_t gen_ = 0;
+    std::vector<Job*> jobs_;
     bool stop_ = false;
 };
 
@@ -1645,32 +1675,34 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
     sig.push_back((uint64_t)(uintptr_t)L.d_hist.p);
     const char* rdd_env = getenv("TPCF_RDD");
     const bool rdd = !(rdd_env && rdd_env[0] == '0');
+    // The batch signature takes the jobs' view ids; views still being built
+    // (new catalogs) are waited for only when a job's planning needs them.
     for (size_t g = 0; g < group.size(); g++) {
         const tpcf_job& job = *group[g].job;
         const tpcf_spec& jsp = *group[g].spec;  // same binning as sp; the loop nest may differ
         int64_t n[3] = {0, 0, 0};
+        uint64_t vid[3] = {0, 0, 0};
         for (int r = 0; r < ncat; r++) {
-            pj[g].v[r] = get_view(ctx, L, job.catalog[r], job.begin[r], job.end[r],
-                                  (job.flags & TPCF_JOB_GLOBAL_INDEX) != 0);
-            n[r] = pj[g].v[r]->n;
+            ViewRef ref{};
+            get_view(ctx, L, job.catalog[r], job.begin[r], job.end[r], (job.flags & TPCF_JOB_GLOBAL_INDEX) != 0,
+                     &ref);
+            vid[r] = ref.id;
+            n[r] = ref.n;
         }
-        if (ncat == 2) pj[g].v[2] = pj[g].v[1];
+        if (ncat == 2) vid[2] = vid[1];
         pj[g].loop_units = loop_units(jsp.kind, jsp.loop, n);
         units += pj[g].loop_units;
         pj[g].swap = 0;
         if (rdd && (jsp.kind == TPCF_TRIANGLE || jsp.kind == TPCF_TRIANGLE_JBJ) &&
             guarded_fp32(jsp, bin) && jsp.loop == TPCF_LOOP_ONE) {
-            if (pj[g].v[0] == pj[g].v[1] && pj[g].v[1] != pj[g].v[2]) pj[g].swap = 1;
-            else if (pj[g].v[1] == pj[g].v[2] && pj[g].v[0] != pj[g].v[1]) pj[g].swap = 2;
+            if (vid[0] == vid[1] && vid[1] != vid[2]) pj[g].swap = 1;
+            else if (vid[1] == vid[2] && vid[0] != vid[1]) pj[g].swap = 2;
         }
-        for (int r = 0; r < 3; r++) {
-            const View* rv = pj[g].role(r);
-            dj[g].pts[r] = rv->pts.p;
-            dj[g].tile_start[r] = rv->tile_start.p;
-            sig.push_back(rv->id);
+        for (int r = 0; r < 3; r++) {  // role r's view (PlannedJob::role)
+            const int v = pj[g].swap == 1 ? (r == 0 ? 2 : 0) : pj[g].swap == 2 ? (r == 2 ? 0 : 1) : r;
+            sig.push_back(vid[v]);
         }
         sig.push_back(pj[g].swap);
-        dj[g].hist = L.d_hist.p + (size_t)bin.len * slot_of[g];
         sig.push_back(slot_of[g]);
         uint64_t f[6] = {(uint64_t)jsp.kind, (uint64_t)jsp.loop, (uint64_t)jsp.prune, (uint64_t)jsp.precision,
                          (uint64_t)jsp.nan_policy, (uint64_t)jsp.overflow};
@@ -1680,6 +1712,20 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
             sig.push_back((uint64_t)(uint32_t)jsp.axis[a].nbins);
         }
     }
+    // the views of job g (waiting for any still being built) and its device job
+    auto attach = [&](size_t g) {
+        const tpcf_job& job = *group[g].job;
+        for (int r = 0; r < ncat; r++)
+            pj[g].v[r] = get_view(ctx, L, job.catalog[r], job.begin[r], job.end[r],
+                                  (job.flags & TPCF_JOB_GLOBAL_INDEX) != 0);
+        if (ncat == 2) pj[g].v[2] = pj[g].v[1];
+        for (int r = 0; r < 3; r++) {
+            const View* rv = pj[g].role(r);
+            dj[g].pts[r] = rv->pts.p;
+            dj[g].tile_start[r] = rv->tile_start.p;
+        }
+        dj[g].hist = L.d_hist.p + (size_t)bin.len * slot_of[g];
+    };
     cudaStream_t st = L.stream;
     L.d_counters.reserve(8);
     size_t ntasks = 0, ngroups = 0;
@@ -1690,7 +1736,6 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
             phases.push_back({name, std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() -
                                                                               t_wall0).count()});
     };
-    phase("views");
     const bool pairs = sp.kind == TPCF_PAIR;
     const bool fast_tri = (sp.kind == TPCF_TRIANGLE || sp.kind == TPCF_TRIANGLE_JBJ) && guarded_fp32(sp, bin);
     // A newly planned batch of two to eight fast-kernel jobs (an estimator's
@@ -1701,6 +1746,9 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
     const char* pl_env = getenv("TPCF_PIPELINE");
     const bool pipeline = !plan_hit && fast_tri && group.size() >= 2 && group.size() <= 8 && !L.slice_batches &&
                           !(pl_env && pl_env[0] == '0');
+    // a pipelined batch waits here for the first job's views only
+    for (size_t g = 0; g < (pipeline ? 1 : group.size()); g++) attach(g);
+    phase("views");
     size_t ntasks2 = 0, ngroups2 = 0;
     uint64_t evaluated2 = 0;
     // planning state shared by the parts of a plan: bound tables by view pair
@@ -1853,8 +1901,8 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
         const size_t g_first = pipeline ? 1 : group.size();
         evaluated = plan_jobs(0, g_first, S.tasks, S.groups, S.gbox);
         L.d_jobs.reserve(dj.size());
-        CK(cudaMemcpyAsync(L.d_jobs.p, dj.data(), dj.size() * sizeof(DevJob), cudaMemcpyHostToDevice, st));
-        L.h2d += dj.size() * sizeof(DevJob);
+        CK(cudaMemcpyAsync(L.d_jobs.p, dj.data(), g_first * sizeof(DevJob), cudaMemcpyHostToDevice, st));
+        L.h2d += g_first * sizeof(DevJob);
         ngroups = upload_part(S.tasks, S.groups, S.gbox, L.d_tasks, L.d_groups, L.d_gbox, st);
         ntasks = S.tasks.size();
         CK(cudaStreamSynchronize(st));
@@ -1872,11 +1920,15 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
     bool second_pending = pipeline;
     auto plan_second = [&]() {
         PlanScratch& S = L.scratch;
+        for (size_t g = 1; g < group.size(); g++) attach(g);
         evaluated2 = plan_jobs(1, group.size(), S.tasks2, S.groups2, S.gbox2);
         if (!L.side) {
             CK(cudaStreamCreateWithFlags(&L.side, cudaStreamNonBlocking));
             CK(cudaEventCreateWithFlags(&L.ev_side, cudaEventDisableTiming));
         }
+        CK(cudaMemcpyAsync(L.d_jobs.p + 1, dj.data() + 1, (group.size() - 1) * sizeof(DevJob),
+                           cudaMemcpyHostToDevice, L.side));
+        L.h2d += (group.size() - 1) * sizeof(DevJob);
         ngroups2 = upload_part(S.tasks2, S.groups2, S.gbox2, L.d_tasks2, L.d_groups2, L.d_gbox2, L.side);
         ntasks2 = S.tasks2.size();
         evaluated += evaluated2;
@@ -2512,7 +2564,7 @@ tpcf_status tpcf_destroy(tpcf_ctx* ctx) {
         std::lock_guard<std::recursive_mutex> lk(ctx->mu);
         std::lock_guard<std::recursive_mutex> vlk(ctx->view_mu);
         cudaSetDevice(ctx->device);
-        for (auto& kv : ctx->pending_views) kv.second.wait();
+        for (auto& kv : ctx->pending_views) kv.second.fut.wait();
         ctx->pending_views.clear();
         ctx->views.clear();
         for (auto& L : ctx->lanes) L->release();
@@ -2546,7 +2598,9 @@ tpcf_status tpcf_catalog_create(tpcf_ctx* ctx, const float* x, const float* y, c
         // host copy.
         const int dev = ctx->device, tile = ctx->tile_points;
         const uint64_t id = ++ctx->next_view_id;
-        ctx->pending_views[std::make_tuple(h, (int64_t)0, n, tile, false)] =
+        ctx->pending_views[std::make_tuple(h, (int64_t)0, n, tile, false)].id = id;
+        ctx->pending_views[std::make_tuple(h, (int64_t)0, n, tile, false)].n = n;
+        ctx->pending_views[std::make_tuple(h, (int64_t)0, n, tile, false)].fut =
             std::async(std::launch::async, [c, n, tile, dev, id] {
                 CK(cudaSetDevice(dev));
                 cudaStream_t st = nullptr;
@@ -2577,7 +2631,7 @@ tpcf_status tpcf_catalog_release(tpcf_ctx* ctx, uint64_t handle) {
     // with the last reference), whatever its outcome
     for (auto it = ctx->pending_views.begin(); it != ctx->pending_views.end();) {
         if (std::get<0>(it->first) == handle) {
-            it->second.wait();
+            it->second.fut.wait();
             it = ctx->pending_views.erase(it);
         } else {
             ++it;
@@ -2593,7 +2647,7 @@ tpcf_status tpcf_resident_bytes(tpcf_ctx* ctx, int64_t* bytes) {
     for (auto& kv : ctx->views) b += (int64_t)kv.second->bytes();
     for (auto& kv : ctx->pending_views) {  // (a failed build holds nothing)
         try {
-            b += (int64_t)kv.second.get()->bytes();
+            b += (int64_t)kv.second.fut.get()->bytes();
         } catch (...) {
         }
     }
