@@ -915,7 +915,7 @@ struct tpcf_ctx {
     int reserve_sms = 0;       // SMs a heavy serving batch leaves free for light jobs
     bool slice_heavy = true;   // heavy serving batches count in slices (light lanes run between them)
     int slice_tasks = 0;       // tasks per slice (0: at least 8 per CTA and at most 64 slices)
-    int group_tasks = 4;       // fast triangle kernel: most tasks sharing one j-k table
+    int group_tasks = 0;       // fast triangle kernel: most tasks sharing one j-k table (0: by the batch)
     int64_t inflight_bytes = 0;  // device bytes of batches running on serving lanes
     // autotuner: launch shape per batch signature
     std::mutex tune_mu;
@@ -1816,11 +1816,25 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
                 tp[it[0]].enumerate(it[1], it[2], part[i], part_eval[i]);
         });
         phase("enumerate");
+        std::vector<size_t> off(items.size() + 1, 0);  // each item's first task
+        for (size_t i = 0; i < items.size(); i++) {
+            ev += part_eval[i];
+            off[i + 1] = off[i] + part[i].size();
+        }
+        const size_t total = off[items.size()];
+        // tasks per group of the fast triangle kernel: 4, or 16 for batches
+        // of thousands of tasks per CTA (voxel sets of light tasks: the j-k
+        // tables are the larger share there, and the tail of a few large
+        // groups a small one; tp10k 12.91 ms with 4, 13.00 with 8; voxel100k
+        // 267 ms with 4, 236 with 16)
+        const size_t group_max =
+            ctx->group_tasks > 0 ? (size_t)ctx->group_tasks
+                                 : (total >= (size_t)ctx->num_sms * 4 * 4096 ? 16 : 4);
         // fast triangle kernel: groups form in windows of consecutive items of
         // one job spanning twice the group size in A tiles
         std::vector<std::array<size_t, 2>> windows;  // first item, item count
         if (fast_tri) {
-            const size_t per = (size_t)std::max(1, ctx->group_tasks);
+            const size_t per = group_max;
             for (size_t i = 0; i < items.size();) {
                 size_t e = i + 1;
                 while (e < items.size() && e - i < per && items[e][0] == items[i][0]) e++;
@@ -1828,12 +1842,6 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
                 i = e;
             }
         }
-        std::vector<size_t> off(items.size() + 1, 0);  // each item's first task
-        for (size_t i = 0; i < items.size(); i++) {
-            ev += part_eval[i];
-            off[i + 1] = off[i] + part[i].size();
-        }
-        const size_t total = off[items.size()];
         h_tasks.resize(total);
         h_groups.clear();
         h_gbox.clear();
@@ -1844,7 +1852,7 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
             toff[windows.size()] = total;
             parallel_items(windows.size(), [&](size_t w) {
                 group_parts(&part[windows[w][0]], windows[w][1], pj[items[windows[w][0]][0]],
-                            (size_t)ctx->group_tasks, h_tasks.data() + toff[w], S.gpart[w]);
+                            group_max, h_tasks.data() + toff[w], S.gpart[w]);
             });
             assemble_groups(S.gpart, windows.size(), toff, total <= (size_t)ctx->num_sms * 3 * 64, h_tasks, h_groups,
                             h_gbox);
