@@ -50,6 +50,7 @@
 #include <string>
 #include <thread>
 #include <tuple>
+#include <unordered_map>
 #include <vector>
 
 using namespace tpcf;
@@ -1677,17 +1678,38 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
     const bool rdd = !(rdd_env && rdd_env[0] == '0');
     // The batch signature takes the jobs' view ids; views still being built
     // (new catalogs) are waited for only when a job's planning needs them.
+    // (A batch of many jobs names few distinct catalog ranges: each is looked
+    // up once.)
+    struct RangeKey {
+        uint64_t h;
+        int64_t b, e;
+        bool gl;
+        bool operator==(const RangeKey& o) const { return h == o.h && b == o.b && e == o.e && gl == o.gl; }
+    };
+    struct RangeHash {
+        size_t operator()(const RangeKey& k) const {
+            uint64_t x = k.h * 0x9E3779B97F4A7C15ull ^ (uint64_t)k.b * 0xC2B2AE3D27D4EB4Full ^
+                         (uint64_t)k.e * 0x165667B19E3779F9ull ^ (uint64_t)k.gl;
+            return (size_t)(x ^ (x >> 29));
+        }
+    };
+    std::unordered_map<RangeKey, ViewRef, RangeHash> refs;
+    sig.reserve(1 + group.size() * 22);
     for (size_t g = 0; g < group.size(); g++) {
         const tpcf_job& job = *group[g].job;
         const tpcf_spec& jsp = *group[g].spec;  // same binning as sp; the loop nest may differ
         int64_t n[3] = {0, 0, 0};
         uint64_t vid[3] = {0, 0, 0};
         for (int r = 0; r < ncat; r++) {
-            ViewRef ref{};
-            get_view(ctx, L, job.catalog[r], job.begin[r], job.end[r], (job.flags & TPCF_JOB_GLOBAL_INDEX) != 0,
-                     &ref);
-            vid[r] = ref.id;
-            n[r] = ref.n;
+            const RangeKey k{job.catalog[r], job.begin[r], job.end[r], (job.flags & TPCF_JOB_GLOBAL_INDEX) != 0};
+            auto it = refs.find(k);
+            if (it == refs.end()) {
+                ViewRef ref{};
+                get_view(ctx, L, k.h, k.b, k.e, k.gl, &ref);
+                it = refs.emplace(k, ref).first;
+            }
+            vid[r] = it->second.id;
+            n[r] = it->second.n;
         }
         if (ncat == 2) vid[2] = vid[1];
         pj[g].loop_units = loop_units(jsp.kind, jsp.loop, n);
@@ -1746,8 +1768,10 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
     const char* pl_env = getenv("TPCF_PIPELINE");
     const bool pipeline = !plan_hit && fast_tri && group.size() >= 2 && group.size() <= 8 && !L.slice_batches &&
                           !(pl_env && pl_env[0] == '0');
-    // a pipelined batch waits here for the first job's views only
-    for (size_t g = 0; g < (pipeline ? 1 : group.size()); g++) attach(g);
+    // a pipelined batch waits here for the first job's views only (a planned
+    // batch needs none: its device jobs are in place)
+    if (!plan_hit)
+        for (size_t g = 0; g < (pipeline ? 1 : group.size()); g++) attach(g);
     phase("views");
     size_t ntasks2 = 0, ngroups2 = 0;
     uint64_t evaluated2 = 0;
