@@ -1846,14 +1846,15 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
             off[i + 1] = off[i] + part[i].size();
         }
         const size_t total = off[items.size()];
-        // tasks per group of the fast triangle kernel: 4, or 16 for batches
-        // of thousands of tasks per CTA (voxel sets of light tasks: the j-k
-        // tables are the larger share there, and the tail of a few large
-        // groups a small one; tp10k 12.91 ms with 4, 13.00 with 8; voxel100k
-        // 267 ms with 4, 236 with 16)
+        // tasks per group of the fast triangle kernel: 4, or 16 for sets of
+        // many jobs with thousands of tasks per CTA (voxel and jackknife sets
+        // of light tasks: the j-k tables are the larger share there, and the
+        // tail of a few large groups a small one; tp10k 12.91 ms with 4, 13.00
+        // with 8; voxel100k 267 ms with 4, 236 with 16; a heavy serving batch
+        // of a few dense jobs keeps 4)
         const size_t group_max =
             ctx->group_tasks > 0 ? (size_t)ctx->group_tasks
-                                 : (total >= (size_t)ctx->num_sms * 4 * 4096 ? 16 : 4);
+                                 : (g1 - g0 > 64 && total >= (size_t)ctx->num_sms * 4 * 4096 ? 16 : 4);
         // fast triangle kernel: groups form in windows of consecutive items of
         // one job spanning twice the group size in A tiles
         std::vector<std::array<size_t, 2>> windows;  // first item, item count
@@ -1955,7 +1956,11 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
         for (size_t g = 1; g < group.size(); g++) attach(g);
         evaluated2 = plan_jobs(1, group.size(), S.tasks2, S.groups2, S.gbox2);
         if (!L.side) {
-            CK(cudaStreamCreateWithFlags(&L.side, cudaStreamNonBlocking));
+            // (the lane's priority: a light serving lane's second part must
+            // not queue behind a heavy batch's CTAs)
+            int prio = 0;
+            CK(cudaStreamGetPriority(st, &prio));
+            CK(cudaStreamCreateWithPriority(&L.side, cudaStreamNonBlocking, prio));
             CK(cudaEventCreateWithFlags(&L.ev_side, cudaEventDisableTiming));
         }
         CK(cudaMemcpyAsync(L.d_jobs.p + 1, dj.data() + 1, (group.size() - 1) * sizeof(DevJob),
