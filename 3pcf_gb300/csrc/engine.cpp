@@ -1185,6 +1185,7 @@ struct PairTable {
     const View* x = nullptr;
     const View* y = nullptr;
     bool prune = false, need_nb = false;
+    int listed = -1;  // the planning pass whose row list holds it
     double lmax = INFINITY;
     PairBounds pb;
     std::vector<std::vector<int>> nb;
@@ -1777,8 +1778,15 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
     uint64_t evaluated2 = 0;
     // planning state shared by the parts of a plan: bound tables by view pair
     std::vector<TripletPlan> tp(pairs ? 0 : group.size());
-    std::map<std::pair<const View*, const View*>, std::unique_ptr<PairTable>> tables;
+    struct ViewPairHash {
+        size_t operator()(const std::pair<const View*, const View*>& k) const {
+            const uint64_t x = (uint64_t)(uintptr_t)k.first * 0x9E3779B97F4A7C15ull ^ (uint64_t)(uintptr_t)k.second;
+            return (size_t)(x ^ (x >> 31));
+        }
+    };
+    std::unordered_map<std::pair<const View*, const View*>, std::unique_ptr<PairTable>, ViewPairHash> tables;
     std::vector<PairTable*> table_list;
+    int plan_pass = 0;
     // Plans jobs [g0, g1) into task list, group starts and group boxes (the
     // last two for the fast triangle kernel); returns the evaluated units.
     auto plan_jobs = [&](size_t g0, size_t g1, std::vector<uint4>& h_tasks, std::vector<uint32_t>& h_groups,
@@ -1788,16 +1796,20 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
         uint64_t ev = 0;
         if (!pairs) {
             const size_t t_first = table_list.size();
+            const int pass = plan_pass++;
             auto table = [&](const View* x, const View* y, bool nb) {
                 auto& t = tables[std::make_pair(x, y)];
                 if (!t) {
                     t.reset(new PairTable());
                     t->init(*x, *y, bin.lmax);
+                    t->listed = pass;
                     table_list.push_back(t.get());
                 }
                 if (nb && !t->need_nb) {
-                    if (table_list.end() == std::find(table_list.begin() + t_first, table_list.end(), t.get()))
-                        table_list.push_back(t.get());  // filled before without neighbour lists: fill again
+                    if (t->listed != pass) {  // filled by an earlier pass without neighbour lists: fill again
+                        t->listed = pass;
+                        table_list.push_back(t.get());
+                    }
                     t->need_nb = true;
                     t->nb.assign(x->ntiles, {});
                 }
