@@ -1858,15 +1858,15 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
             off[i + 1] = off[i] + part[i].size();
         }
         const size_t total = off[items.size()];
-        // tasks per group of the fast triangle kernel: 4, or 16 for sets of
+        // tasks per group of the fast triangle kernel: 4, or 64 for sets of
         // many jobs with thousands of tasks per CTA (voxel and jackknife sets
         // of light tasks: the j-k tables are the larger share there, and the
         // tail of a few large groups a small one; tp10k 12.91 ms with 4, 13.00
-        // with 8; voxel100k 267 ms with 4, 236 with 16; a heavy serving batch
-        // of a few dense jobs keeps 4)
+        // with 8; voxel100k 267 ms with 4, 236 with 16, 230 with 32, 226 with
+        // 64; a heavy serving batch of a few dense jobs keeps 4)
         const size_t group_max =
             ctx->group_tasks > 0 ? (size_t)ctx->group_tasks
-                                 : (g1 - g0 > 64 && total >= (size_t)ctx->num_sms * 4 * 4096 ? 16 : 4);
+                                 : (g1 - g0 > 64 && total >= (size_t)ctx->num_sms * 4 * 4096 ? MAX_GROUP_TASKS : 4);
         // fast triangle kernel: groups form in windows of consecutive items of
         // one job spanning twice the group size in A tiles
         std::vector<std::array<size_t, 2>> windows;  // first item, item count
