@@ -1240,13 +1240,25 @@ struct TripletPlan {
         if (empty) return;  // a role without tiles: no triple (and no neighbour lists)
         const View &A = *pj->role(0), &B = *pj->role(1), &C = *pj->role(2);
         const double lmax = bin->lmax;
-        auto add = [&](int a, int b, int c, uint32_t pred, uint32_t flags) {
+        // bounds of the pair (a, b), looked up once for all its c
+        struct AB_ {
+            double l = 0, u = 0;
+        };
+        auto ab_bounds = [&](int a, int b) {
+            AB_ r;
             if (prune) {
-                double lab = AB->pb.L(a, b), lac = AC->pb.L(a, c), lbc = BC->pb.L(b, c);
+                r.l = AB->pb.L(a, b);
+                r.u = AB->pb.U(a, b);
+            }
+            return r;
+        };
+        auto add = [&](int a, int b, int c, const AB_& ab, uint32_t pred, uint32_t flags) {
+            if (prune) {
+                const double lbc = BC->pb.L(b, c);
                 if (!(lbc < lmax)) return;
-                const double uab = AB->pb.U(a, b), uac = AC->pb.U(a, c);
-                if (bin->tri_prune && !tri_triple_possible(*bin, lab, lac, lbc, uab, uac, BC->pb.U(b, c))) return;
-                if (uab >= lmax) flags |= TASK_CHECK_B;
+                const double lac = AC->pb.L(a, c), uac = AC->pb.U(a, c);
+                if (bin->tri_prune && !tri_triple_possible(*bin, ab.l, lac, lbc, ab.u, uac, BC->pb.U(b, c))) return;
+                if (ab.u >= lmax) flags |= TASK_CHECK_B;
                 if (uac >= lmax) flags |= TASK_CHECK_C;
             }
             uint64_t u = task_units3(A, a, B, b, C, c, flags);
@@ -1255,6 +1267,8 @@ struct TripletPlan {
             tasks.push_back({u, make_uint4(slot | (pred << TASK_PRED_SHIFT) | flags, (uint32_t)a, (uint32_t)b,
                                            (uint32_t)c)});
         };
+        // the entries >= from of an ascending neighbour list
+        auto from = [](const std::vector<int>& l, int v) { return std::lower_bound(l.begin(), l.end(), v); };
         const tpcf_spec& s = *sp;
         // three-side histogram of one catalog in all roles: the kernel counts
         // each multiset {i, j, k} once for all its orderings
@@ -1263,54 +1277,55 @@ struct TripletPlan {
             // roles (C, A, A) of a D-D-R job: each point of C with every
             // unordered pair of the single array, weight [k_c >= j] + [k_c >= k]
             for (int a = a0; a < a1; a++)
-                for (int b : AB->nb[a])
-                    for (int c : AC->nb[a]) {
-                        if (c < b) continue;
-                        add(a, b, c, PRED_RDD, b == c ? TASK_DIAG_JK : 0);
-                    }
+                for (int b : AB->nb[a]) {
+                    const AB_ ab = ab_bounds(a, b);
+                    for (auto c = from(AC->nb[a], b); c != AC->nb[a].end(); ++c)
+                        add(a, b, *c, ab, PRED_RDD, b == *c ? TASK_DIAG_JK : 0);
+                }
         } else if (pj->swap == 2) {
             // roles (B, B, A) of a D-R-R job: every unordered pair of the pair
             // array with each point of the other
             for (int a = a0; a < a1; a++)
-                for (int b : AB->nb[a]) {
-                    if (b < a) continue;
-                    for (int c : AC->nb[a]) add(a, b, c, PRED_NONE, a == b ? TASK_DIAG_IJ : 0);
+                for (auto b = from(AB->nb[a], a); b != AB->nb[a].end(); ++b) {
+                    const AB_ ab = ab_bounds(a, *b);
+                    for (int c : AC->nb[a]) add(a, *b, c, ab, PRED_NONE, a == *b ? TASK_DIAG_IJ : 0);
                 }
         } else if ((tri && s.loop == TPCF_LOOP_SAME || sym3) && sameAB && sameBC) {
             // i <= j <= k over one array: unordered distinct triples (triangle
             // programs), or every multiset of three points counted for each of
             // its orderings (three-side: PRED_SAME marks the task)
             for (int a = a0; a < a1; a++)
-                for (int b : AB->nb[a]) {
-                    if (b < a) continue;
-                    for (int c : AC->nb[a]) {
-                        if (c < b) continue;
-                        uint32_t f = (a == b ? TASK_DIAG_IJ : 0) | (b == c ? TASK_DIAG_JK : 0);
-                        add(a, b, c, sym3 ? PRED_SAME : PRED_NONE, f);
+                for (auto b = from(AB->nb[a], a); b != AB->nb[a].end(); ++b) {
+                    const AB_ ab = ab_bounds(a, *b);
+                    for (auto c = from(AC->nb[a], *b); c != AC->nb[a].end(); ++c) {
+                        uint32_t f = (a == *b ? TASK_DIAG_IJ : 0) | (*b == *c ? TASK_DIAG_JK : 0);
+                        add(a, *b, *c, ab, sym3 ? PRED_SAME : PRED_NONE, f);
                     }
                 }
         } else if (tri && s.loop == TPCF_LOOP_ONE && sameBC) {
             // j <= k over one array (j == k has a zero side): unordered pairs
             for (int a = a0; a < a1; a++)
-                for (int b : AB->nb[a])
-                    for (int c : AC->nb[a]) {
-                        if (c < b) continue;
-                        add(a, b, c, PRED_NONE, b == c ? TASK_DIAG_JK : 0);
-                    }
+                for (int b : AB->nb[a]) {
+                    const AB_ ab = ab_bounds(a, b);
+                    for (auto c = from(AC->nb[a], b); c != AC->nb[a].end(); ++c)
+                        add(a, b, *c, ab, PRED_NONE, b == *c ? TASK_DIAG_JK : 0);
+                }
         } else if (tri && s.loop == TPCF_LOOP_ONE && sameAB) {
             // every ordered (i, j) of one array, k >= j: unordered {i, j} with
             // weight [k >= i] + [k >= j]
             for (int a = a0; a < a1; a++)
-                for (int b : AB->nb[a]) {
-                    if (b < a) continue;
-                    for (int c : AC->nb[a]) add(a, b, c, PRED_DDR, a == b ? TASK_DIAG_IJ : 0);
+                for (auto b = from(AB->nb[a], a); b != AB->nb[a].end(); ++b) {
+                    const AB_ ab = ab_bounds(a, *b);
+                    for (int c : AC->nb[a]) add(a, *b, c, ab, PRED_DDR, a == *b ? TASK_DIAG_IJ : 0);
                 }
         } else {
             uint32_t pred = PRED_NONE;
             if (tri) pred = s.loop == TPCF_LOOP_SAME ? PRED_SAME : s.loop == TPCF_LOOP_ONE ? PRED_ONE : PRED_NONE;
             for (int a = a0; a < a1; a++)
-                for (int b : AB->nb[a])
-                    for (int c : AC->nb[a]) add(a, b, c, pred, 0);
+                for (int b : AB->nb[a]) {
+                    const AB_ ab = ab_bounds(a, b);
+                    for (int c : AC->nb[a]) add(a, b, c, ab, pred, 0);
+                }
         }
     }
 };
