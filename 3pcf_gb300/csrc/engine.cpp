@@ -1378,6 +1378,7 @@ class HostPool {
         {
             std::lock_guard<std::mutex> lk(mu_);
             jobs_.push_back(&job);
+            posted_.fetch_add(1);
         }
         cv_.notify_all();
         work(job);
@@ -1389,6 +1390,7 @@ class HostPool {
         {
             std::lock_guard<std::mutex> lk(mu_);
             stop_ = true;
+            stop_flag_.store(true);
         }
         cv_.notify_all();
         for (auto& t : workers_) t.join();
@@ -1419,12 +1421,22 @@ class HostPool {
         return nullptr;
     }
     void loop() {
+        uint64_t seen = 0;
         for (;;) {
+            // the phases of a planning pass follow one another within
+            // microseconds: watch for the next job for a while before sleeping
+            // (a wake-up from the condition variable costs tens of microseconds)
+            const auto spin_end = std::chrono::steady_clock::now() + std::chrono::microseconds(300);
+            while (posted_.load() == seen && !stop_flag_.load() && std::chrono::steady_clock::now() < spin_end)
+                std::this_thread::yield();
             Job* j = nullptr;
             {
                 std::unique_lock<std::mutex> lk(mu_);
-                cv_.wait(lk, [&] { return stop_ || (j = open_job()) != nullptr; });
+                cv_.wait(lk, [&] { return stop_ || (j = open_job()) != nullptr || posted_.load() != seen; });
                 if (stop_) return;
+                seen = posted_.load();
+                if (!j) j = open_job();
+                if (!j) continue;
                 j->users++;
             }
             work(*j);
@@ -1439,6 +1451,8 @@ class HostPool {
     std::condition_variable cv_, done_cv_;
     std::vector<std::thread> workers_;
     std::vector<Job*> jobs_;
+    std::atomic<uint64_t> posted_{0};  // jobs posted so far
+    std::atomic<bool> stop_flag_{false};
     bool stop_ = false;
 };
 
