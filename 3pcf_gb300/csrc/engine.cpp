@@ -38,6 +38,8 @@
 #include <array>
 #include <atomic>
 #include <chrono>
+#include <climits>
+#include <cstdint>
 #include <cmath>
 #include <condition_variable>
 #include <deque>
@@ -1236,7 +1238,10 @@ struct TripletPlan {
         AC = ac;
         BC = bc;
     }
-    void enumerate(int a0, int a1, TaskList& tasks, uint64_t& evaluated) const {
+    // Tile triples of A tiles [a0, a1); with one A tile, only its neighbour-list
+    // entries [blo, bhi) as tile B (a heavy tile's triples in several parts).
+    void enumerate(int a0, int a1, TaskList& tasks, uint64_t& evaluated, size_t blo = 0,
+                   size_t bhi = SIZE_MAX) const {
         if (empty) return;  // a role without tiles: no triple (and no neighbour lists)
         const View &A = *pj->role(0), &B = *pj->role(1), &C = *pj->role(2);
         const double lmax = bin->lmax;
@@ -1269,6 +1274,19 @@ struct TripletPlan {
         };
         // the entries >= from of an ascending neighbour list
         auto from = [](const std::vector<int>& l, int v) { return std::lower_bound(l.begin(), l.end(), v); };
+        // tile B's entries of the list: positions [blo, bhi), at least v
+        struct Span {
+            std::vector<int>::const_iterator b, e;
+            std::vector<int>::const_iterator begin() const { return b; }
+            std::vector<int>::const_iterator end() const { return e; }
+        };
+        auto bspan = [&](const std::vector<int>& l, int v) {
+            auto lo = l.begin() + (ptrdiff_t)std::min(blo, l.size());
+            auto hi = l.begin() + (ptrdiff_t)std::min(bhi, l.size());
+            auto f = from(l, v);
+            if (f > lo) lo = f;
+            return Span{lo, std::max(lo, hi)};
+        };
         const tpcf_spec& s = *sp;
         // three-side histogram of one catalog in all roles: the kernel counts
         // each multiset {i, j, k} once for all its orderings
@@ -1277,7 +1295,7 @@ struct TripletPlan {
             // roles (C, A, A) of a D-D-R job: each point of C with every
             // unordered pair of the single array, weight [k_c >= j] + [k_c >= k]
             for (int a = a0; a < a1; a++)
-                for (int b : AB->nb[a]) {
+                for (int b : bspan(AB->nb[a], INT_MIN)) {
                     const AB_ ab = ab_bounds(a, b);
                     for (auto c = from(AC->nb[a], b); c != AC->nb[a].end(); ++c)
                         add(a, b, *c, ab, PRED_RDD, b == *c ? TASK_DIAG_JK : 0);
@@ -1286,26 +1304,26 @@ struct TripletPlan {
             // roles (B, B, A) of a D-R-R job: every unordered pair of the pair
             // array with each point of the other
             for (int a = a0; a < a1; a++)
-                for (auto b = from(AB->nb[a], a); b != AB->nb[a].end(); ++b) {
-                    const AB_ ab = ab_bounds(a, *b);
-                    for (int c : AC->nb[a]) add(a, *b, c, ab, PRED_NONE, a == *b ? TASK_DIAG_IJ : 0);
+                for (int b : bspan(AB->nb[a], a)) {
+                    const AB_ ab = ab_bounds(a, b);
+                    for (int c : AC->nb[a]) add(a, b, c, ab, PRED_NONE, a == b ? TASK_DIAG_IJ : 0);
                 }
         } else if ((tri && s.loop == TPCF_LOOP_SAME || sym3) && sameAB && sameBC) {
             // i <= j <= k over one array: unordered distinct triples (triangle
             // programs), or every multiset of three points counted for each of
             // its orderings (three-side: PRED_SAME marks the task)
             for (int a = a0; a < a1; a++)
-                for (auto b = from(AB->nb[a], a); b != AB->nb[a].end(); ++b) {
-                    const AB_ ab = ab_bounds(a, *b);
-                    for (auto c = from(AC->nb[a], *b); c != AC->nb[a].end(); ++c) {
-                        uint32_t f = (a == *b ? TASK_DIAG_IJ : 0) | (*b == *c ? TASK_DIAG_JK : 0);
-                        add(a, *b, *c, ab, sym3 ? PRED_SAME : PRED_NONE, f);
+                for (int b : bspan(AB->nb[a], a)) {
+                    const AB_ ab = ab_bounds(a, b);
+                    for (auto c = from(AC->nb[a], b); c != AC->nb[a].end(); ++c) {
+                        uint32_t f = (a == b ? TASK_DIAG_IJ : 0) | (b == *c ? TASK_DIAG_JK : 0);
+                        add(a, b, *c, ab, sym3 ? PRED_SAME : PRED_NONE, f);
                     }
                 }
         } else if (tri && s.loop == TPCF_LOOP_ONE && sameBC) {
             // j <= k over one array (j == k has a zero side): unordered pairs
             for (int a = a0; a < a1; a++)
-                for (int b : AB->nb[a]) {
+                for (int b : bspan(AB->nb[a], INT_MIN)) {
                     const AB_ ab = ab_bounds(a, b);
                     for (auto c = from(AC->nb[a], b); c != AC->nb[a].end(); ++c)
                         add(a, b, *c, ab, PRED_NONE, b == *c ? TASK_DIAG_JK : 0);
@@ -1314,15 +1332,15 @@ struct TripletPlan {
             // every ordered (i, j) of one array, k >= j: unordered {i, j} with
             // weight [k >= i] + [k >= j]
             for (int a = a0; a < a1; a++)
-                for (auto b = from(AB->nb[a], a); b != AB->nb[a].end(); ++b) {
-                    const AB_ ab = ab_bounds(a, *b);
-                    for (int c : AC->nb[a]) add(a, *b, c, ab, PRED_DDR, a == *b ? TASK_DIAG_IJ : 0);
+                for (int b : bspan(AB->nb[a], a)) {
+                    const AB_ ab = ab_bounds(a, b);
+                    for (int c : AC->nb[a]) add(a, b, c, ab, PRED_DDR, a == b ? TASK_DIAG_IJ : 0);
                 }
         } else {
             uint32_t pred = PRED_NONE;
             if (tri) pred = s.loop == TPCF_LOOP_SAME ? PRED_SAME : s.loop == TPCF_LOOP_ONE ? PRED_ONE : PRED_NONE;
             for (int a = a0; a < a1; a++)
-                for (int b : AB->nb[a]) {
+                for (int b : bspan(AB->nb[a], INT_MIN)) {
                     const AB_ ab = ab_bounds(a, b);
                     for (int c : AC->nb[a]) add(a, b, c, ab, pred, 0);
                 }
@@ -1860,10 +1878,25 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
             });
         }
         phase("tables");
-        std::vector<std::array<int, 3>> items;  // job, A-tile begin, end
+        // items: job, A-tile begin, end, and for a heavy single tile the
+        // part [lo, hi) of its neighbour list taken as tile B (the work of a
+        // tile grows with the square of its neighbour count: the densest
+        // tiles of a clustered catalog would otherwise each be one long item)
+        std::vector<std::array<int, 5>> items;
         for (size_t g = g0; g < g1; g++) {
             const int na = pj[g].role(0)->ntiles, step = pairs ? 16 : 2;
-            for (int a0 = 0; a0 < na; a0 += step) items.push_back({(int)g, a0, std::min(a0 + step, na)});
+            const PairTable* ab = pairs || tp[g].empty ? nullptr : tp[g].AB;
+            for (int a0 = 0; a0 < na;) {
+                const int nb = ab && ab->need_nb ? (int)ab->nb[a0].size() : 0;
+                if (nb > 48) {
+                    for (int lo = 0; lo < nb; lo += 24) items.push_back({(int)g, a0, a0 + 1, lo, lo + 24});
+                    a0++;
+                } else {
+                    const int a1 = std::min(a0 + step, na);
+                    items.push_back({(int)g, a0, a1, 0, INT_MAX});
+                    a0 = a1;
+                }
+            }
         }
         // one task list per item, so that the concatenation keeps job order
         // (a CTA flushes its shared histogram whenever the job changes)
@@ -1878,7 +1911,7 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
                 plan_pairs(*group[it[0]].spec, pj[it[0]], (uint32_t)it[0], bin.lmax, it[1], it[2], part[i],
                            part_eval[i]);
             else
-                tp[it[0]].enumerate(it[1], it[2], part[i], part_eval[i]);
+                tp[it[0]].enumerate(it[1], it[2], part[i], part_eval[i], (size_t)it[3], (size_t)it[4]);
         });
         phase("enumerate");
         std::vector<size_t> off(items.size() + 1, 0);  // each item's first task
@@ -1897,13 +1930,14 @@ void run_group(tpcf_ctx* ctx, Lane& L, const std::vector<GroupJob>& group) {
             ctx->group_tasks > 0 ? (size_t)ctx->group_tasks
                                  : (g1 - g0 > 64 && total >= (size_t)ctx->num_sms * 4 * 4096 ? MAX_GROUP_TASKS : 4);
         // fast triangle kernel: groups form in windows of consecutive items of
-        // one job spanning twice the group size in A tiles
+        // one job whose first A tiles lie in one aligned span of twice the
+        // group size
         std::vector<std::array<size_t, 2>> windows;  // first item, item count
         if (fast_tri) {
-            const size_t per = group_max;
+            const int span = 2 * (int)group_max;
             for (size_t i = 0; i < items.size();) {
                 size_t e = i + 1;
-                while (e < items.size() && e - i < per && items[e][0] == items[i][0]) e++;
+                while (e < items.size() && items[e][0] == items[i][0] && items[e][1] / span == items[i][1] / span) e++;
                 windows.push_back({i, e - i});
                 i = e;
             }
