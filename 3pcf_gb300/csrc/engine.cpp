@@ -1399,7 +1399,17 @@ class HostPool {
             posted_.fetch_add(1);
         }
         cv_.notify_all();
-        work(job);
+        try {
+            work(job);
+        } catch (...) {
+            // no further items; wait for the helpers to leave the job (it lives
+            // on this frame) before the exception leaves it
+            job.next.store(n);
+            std::unique_lock<std::mutex> lk(mu_);
+            jobs_.erase(std::find(jobs_.begin(), jobs_.end(), &job));
+            done_cv_.wait(lk, [&] { return job.users == 0; });
+            throw;
+        }
         std::unique_lock<std::mutex> lk(mu_);
         jobs_.erase(std::find(jobs_.begin(), jobs_.end(), &job));  // no new helpers
         done_cv_.wait(lk, [&] { return job.users == 0 && job.done.load() == n; });
